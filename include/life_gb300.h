@@ -1,0 +1,196 @@
+/*
+ * life_gb300.h -- C-ABI of the GB300 LIFE hot path.
+ *
+ * The LIFE reference (joconnor22/LIFE v1.0.3) has no plugin or FFI layer: its
+ * boundary is the class interface that main() drives (reference
+ * src/main.cpp:42-86) -- GridClass() (src/Grid.cpp:1232), ObjectsClass(GridClass&)
+ * (src/Objects.cpp:1589), GridClass::solver() (src/Grid.cpp:25), the
+ * IBMBodyClass constructors (src/IBMBody.cpp:27,45,79) and the restart
+ * readers/writers (src/Grid.cpp:1072-1229, src/Objects.cpp:979-1371). Each entry
+ * point below replaces one of those; the comment on each names which.
+ *
+ * Conventions
+ *   - Plain C types only; every function returns an int status (LIFE_OK = 0).
+ *     life_last_error() gives the message the reference would have printed
+ *     through ERROR() before exit(99) (reference inc/Utils.h:72-77).
+ *   - Device memory is owned by the library; host buffers by the caller.
+ *   - Field buffers use the reference's host layout: site id = i*Ny + j
+ *     (y fastest), populations f[id*9 + v], velocity u[id*2 + d].
+ *   - A LifeCase handle is not thread-safe; distinct handles are independent.
+ */
+#ifndef LIFE_GB300_H
+#define LIFE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LIFE_ABI_VERSION 1
+
+/* Status codes */
+enum {
+    LIFE_OK = 0,
+    LIFE_ERR_INVALID = 1,       /* bad argument or unsupported case option */
+    LIFE_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+    LIFE_ERR_NAN = 3,           /* "Simulation blew up" (reference src/Grid.cpp:573-581) */
+    LIFE_ERR_SUBITER = 4,       /* subiteration cap hit (src/Objects.cpp:58-59) */
+    LIFE_ERR_SUPPORT = 5,       /* support buffer overflow (src/IBMNode.cpp:171-172) */
+    LIFE_ERR_GEOMETRY = 6,      /* geometry.config / body construction errors */
+    LIFE_ERR_DEFLECT = 7,       /* static pre-deflection cap (src/FEMBody.cpp:427-428) */
+    LIFE_ERR_NOMEM = 8,         /* device allocation failed */
+    LIFE_ERR_TIMEOUT = 9,       /* a bounded device wait gave up */
+    LIFE_ERR_BUSY = 10          /* serving queue full / slot not ready */
+};
+
+/* eLatType (reference inc/defs.h:163); LIFE_FLUID on a wall means periodic. */
+enum { LIFE_FLUID = 0, LIFE_WALL = 1, LIFE_VELOCITY = 2, LIFE_FREESLIP = 3,
+       LIFE_PRESSURE = 4, LIFE_CONVECTIVE = 5 };
+/* eProfileType (reference inc/defs.h:164); UNIFORM = PROFILE undefined. */
+enum { LIFE_PROFILE_UNIFORM = -1, LIFE_PROFILE_PARABOLIC = 0, LIFE_PROFILE_SHEAR = 1,
+       LIFE_PROFILE_BOUNDARY_LAYER = 2 };
+/* Population storage/arithmetic form on the GPU. */
+enum { LIFE_PREC_F64 = 0, LIFE_PREC_F32 = 1, LIFE_PREC_F16 = 2 };
+/* geometry.config keywords (reference src/Objects.cpp:374-382) */
+enum { LIFE_BODY_CIRCLE = 0, LIFE_BODY_FILAMENT = 1 };
+
+/* Every value of the reference's params.h that the solver reads
+ * (reference inc/params.h:26-110). Switches that are #define'd or not in
+ * params.h become has_* flags. include/life_params_pack.h fills this struct
+ * from a params.h at compile time. */
+typedef struct LifeCaseParams {
+    int32_t Nx, Ny;
+    double height_p, rho_p, nu_p, omega;
+    double ux0_p, uy0_p;
+    double gravityX, gravityY, dpdx, dpdy;
+    int32_t wall_left, wall_right, wall_bottom, wall_top;
+    int32_t profile;
+    double uxInlet_p, uyInlet_p;
+    double alpha, delta;          /* Newmark */
+    double relaxMax, subTol;      /* FSI coupling */
+    int32_t central_moments;
+    int32_t has_inlet_ramp;  double inlet_ramp;
+    int32_t has_womersley;   double womersley;
+    int32_t uni_epsilon, ordered;
+    int32_t has_initial_deflect; double initial_deflect;
+    int32_t nSteps, tinfo, tVTK, tRestart;
+    double ref_nu, ref_rho, ref_P, ref_L, ref_U;
+    int32_t precision;            /* LIFE_PREC_* (GPU only; not a params.h value) */
+    int32_t reserved[7];
+} LifeCaseParams;
+
+/* One geometry.config line (reference input/geometry.config:8-13):
+ *   CIRCLE   NUMBER ID X Y DX DY RADIUS
+ *   FILAMENT NUMBER ID X Y DX DY LENGTH HEIGHT ANGLE FLEXIBLE|RIGID
+ *            N_ELEMENTS|CONFORMING CLAMPED|SUPPORTED DENSITY YOUNG_MODULUS */
+typedef struct LifeBodyDesc {
+    int32_t kind;         /* LIFE_BODY_CIRCLE / LIFE_BODY_FILAMENT */
+    int32_t number;       /* NUMBER of bodies in this line */
+    int32_t id;           /* STARTID */
+    int32_t flexible;     /* FILAMENT: 1 FLEXIBLE, 0 RIGID */
+    int32_t n_elements;   /* FILAMENT: element count, 0 = CONFORMING */
+    int32_t clamped;      /* FILAMENT: 1 CLAMPED, 0 SUPPORTED */
+    double x, y, dx, dy;  /* start position and spacing (physical units) */
+    double radius;        /* CIRCLE */
+    double length, height, angle_deg;  /* FILAMENT */
+    double rho, E;        /* FILAMENT density and Young's modulus */
+} LifeBodyDesc;
+
+/* Sizes of a created case (after marker de-overlap). */
+typedef struct LifeCaseInfo {
+    int32_t Nx, Ny;
+    int32_t n_bodies, n_markers, n_flex, sim_dofs;
+    int32_t precision;
+    int32_t t;                 /* current time step */
+    double Dx, Dt, Dm, Drho, tau, nu, c_s;
+    size_t device_bytes;       /* device memory held by the case */
+} LifeCaseInfo;
+
+/* Device-side status flags and per-step diagnostics. */
+typedef struct LifeStatus {
+    int32_t code;              /* first error seen (LIFE_ERR_*), 0 if none */
+    int32_t t;                 /* time step at which it was raised */
+    int32_t last_subits;       /* subiterations taken in the last step */
+    int32_t last_nr_its;       /* NR iterations of body 0 in the last subiteration */
+    double last_subres;        /* FSI residual reached */
+    double relax;              /* current Aitken factor */
+} LifeStatus;
+
+typedef struct LifeCase LifeCase;
+
+/* Version of this ABI (LIFE_ABI_VERSION). */
+int life_abi_version(void);
+
+/* Message for the last error raised on this thread (never NULL). */
+const char* life_last_error(void);
+
+/* Replaces GridClass::GridClass (src/Grid.cpp:1232-1289) followed by
+ * ObjectsClass::ObjectsClass (src/Objects.cpp:1589-1624): builds the lattice,
+ * the type map and inlet profiles (initialiseGrid, src/Grid.cpp:916-1062), the
+ * IBM bodies from the geometry lines (geometryReadIn, src/Objects.cpp:324-488;
+ * IBMBodyClass ctors src/IBMBody.cpp:45-135), removes overlapping markers
+ * (src/Objects.cpp:867-938) and runs initialiseObjects (src/Objects.cpp:941-961).
+ * All state is then uploaded to device 0 (or the current device). */
+int life_case_create(const LifeCaseParams* params, const LifeBodyDesc* bodies,
+                     int32_t n_bodies, LifeCase** out);
+
+/* Releases the case and its device memory. */
+int life_case_destroy(LifeCase* c);
+
+/* Replaces nsteps iterations of the main loop's grid.solver()
+ * (src/main.cpp:70-73, GridClass::solver src/Grid.cpp:25-33). Asynchronous with
+ * respect to the host unless an error must be reported; t advances by nsteps. */
+int life_case_step(LifeCase* c, int32_t nsteps);
+
+/* Blocks until all queued work of the case has finished; returns the device
+ * status code (LIFE_ERR_SUBITER etc.) if one was raised. */
+int life_case_sync(LifeCase* c);
+
+int life_case_info(const LifeCase* c, LifeCaseInfo* info);
+int life_case_status(LifeCase* c, LifeStatus* st);
+
+/* Copies the reference's grid state after the current step into host buffers
+ * in the reference layout (any pointer may be NULL to skip it): rho[Nx*Ny],
+ * u[Nx*Ny*2], f[Nx*Ny*9], force_ibm[Nx*Ny*2]. These are exactly the arrays
+ * GridClass::writeRestart dumps (src/Grid.cpp:1191-1222). */
+int life_case_get_fields(LifeCase* c, double* rho, double* u, double* f, double* force_ibm);
+
+/* Replaces GridClass::readRestart (src/Grid.cpp:1072-1160): loads rho, u,
+ * force_ibm and f (reference layout) and sets the time step to t. */
+int life_case_set_fields(LifeCase* c, int32_t t, const double* rho, const double* u,
+                         const double* f, const double* force_ibm);
+
+/* Marker arrays in global marker order (iNode order after de-overlap):
+ * pos/vel/force [n*2], epsilon/ds [n], body_index [n]. NULL skips a field. */
+int life_case_get_markers(LifeCase* c, double* pos, double* vel, double* force,
+                          double* epsilon, double* ds, int32_t* body_index);
+/* Body table: reference body IDs, flexible flags and marker counts. */
+int life_case_get_bodies(LifeCase* c, int32_t* ids, int32_t* flexible, int32_t* n_markers,
+                         int32_t* n_fem_nodes);
+
+/* FEM state of flexible body k (in body order): each array has 3*n_fem_nodes
+ * entries, or n_el / n_node entries for the element and node arrays.
+ * The set mirrors FEM.restart (src/Objects.cpp:1289-1362). */
+int life_case_get_fem(LifeCase* c, int32_t k, double* U, double* Udot, double* Udotdot,
+                      double* U_n, double* U_nm1, double* R_k, double* el_L,
+                      double* el_angle, double* node_pos, double* node_angle);
+int life_case_get_relax(LifeCase* c, double* relax);
+
+/* Scalar observables computed on the device without copying the field:
+ * max |u| over the lattice with a NaN check (GridClass::writeInfo,
+ * src/Grid.cpp:562-588) and the total IBM force (writeTotalForces,
+ * src/Objects.cpp:518-528). */
+int life_case_max_velocity(LifeCase* c, double* max_vel, int32_t* has_nan);
+int life_case_total_force(LifeCase* c, double* fx, double* fy);
+
+/* Parses geometry.config text with the reference's rules (leading '#' lines
+ * skipped, whitespace tokens; src/Objects.cpp:338-458). Writes at most cap
+ * descriptors, returns the number found in *n. */
+int life_parse_geometry(const char* text, LifeBodyDesc* out, int32_t cap, int32_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LIFE_GB300_H */
