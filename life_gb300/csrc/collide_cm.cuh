@@ -1,0 +1,75 @@
+// Central-moments collision in FP64 (De Rosis 2019), the reference's
+// CENTRAL_MOMENTS branch of GridClass::streamCollide.
+#pragma once
+#include "lbm_device.cuh"
+
+namespace life {
+
+// Inverse central-moment transform (De Rosis 2019), term order as in the
+// reference (src/Grid.cpp:109-223); FP64 parity depends on that order.
+__device__ __forceinline__ void collide_cm(const double f[9], double rho, double ux, double uy, double Fx, double Fy,
+                           double omega, double cs, double fs[9]) {
+    double k4Pre = 0.0, k5Pre = 0.0;
+#pragma unroll
+    for (int v = 0; v < 9; v++) {
+        double cx = cx_of(v) - ux;
+        double cy = cy_of(v) - uy;
+        k4Pre += f[v] * (LSQ(cx) - LSQ(cy));
+        k5Pre += f[v] * cx * cy;
+    }
+    const double k0 = rho;
+    const double k1 = 0.5 * Fx;
+    const double k2 = 0.5 * Fy;
+    const double k3 = 2.0 * rho * LSQ(cs);
+    const double k4 = (1.0 - omega) * k4Pre;
+    const double k5 = (1.0 - omega) * k5Pre;
+    const double k6 = 0.5 * Fy * LSQ(cs);
+    const double k7 = 0.5 * Fx * LSQ(cs);
+    const double k8 = rho * LQU(cs);
+    const double X2 = LSQ(ux), Y2 = LSQ(uy);
+    fs[0] = (X2 * Y2 - X2 - Y2 + 1.0) * k0 + (2.0 * ux * Y2 - 2.0 * ux) * k1 + (2.0 * uy * X2 - 2.0 * uy) * k2 +
+            (0.5 * X2 + 0.5 * Y2 - 1.0) * k3 + (0.5 * Y2 - 0.5 * X2) * k4 + 4.0 * ux * uy * k5 + 2.0 * uy * k6 +
+            2.0 * ux * k7 + k8;
+    fs[1] = (0.5 * X2 - 0.5 * (X2 * Y2) - 0.5 * (ux * Y2) + 0.5 * ux) * k0 + (ux - ux * Y2 - 0.5 * Y2 + 0.5) * k1 +
+            (-uy * X2 - uy * ux) * k2 + (-0.25 * X2 - 0.25 * ux - 0.25 * Y2 + 0.25) * k3 +
+            (0.25 * X2 + 0.25 * ux - 0.25 * Y2 + 0.25) * k4 + (-uy - 2.0 * ux * uy) * k5 + (-uy) * k6 +
+            (-ux - 0.5) * k7 - 0.5 * k8;
+    fs[2] = (-0.5 * (X2 * Y2) + 0.5 * X2 + 0.5 * (ux * Y2) - 0.5 * ux) * k0 + (ux - ux * Y2 + 0.5 * Y2 - 0.5) * k1 +
+            (-uy * X2 + uy * ux) * k2 + (-0.25 * X2 + 0.25 * ux - 0.25 * Y2 + 0.25) * k3 +
+            (0.25 * X2 - 0.25 * ux - 0.25 * Y2 + 0.25) * k4 + (uy - 2.0 * ux * uy) * k5 + (-uy) * k6 +
+            (0.5 - ux) * k7 - 0.5 * k8;
+    fs[3] = (0.5 * Y2 - 0.5 * (X2 * uy) - 0.5 * (X2 * Y2) + 0.5 * uy) * k0 + (-ux * Y2 - ux * uy) * k1 +
+            (uy - X2 * uy - 0.5 * X2 + 0.5) * k2 + (-0.25 * X2 - 0.25 * Y2 - 0.25 * uy + 0.25) * k3 +
+            (0.25 * X2 - 0.25 * Y2 - 0.25 * uy - 0.25) * k4 + (-ux - 2.0 * ux * uy) * k5 + (-uy - 0.5) * k6 +
+            (-ux) * k7 - 0.5 * k8;
+    fs[4] = (-0.5 * (X2 * Y2) + 0.5 * (X2 * uy) + 0.5 * Y2 - 0.5 * uy) * k0 + (-ux * Y2 + ux * uy) * k1 +
+            (uy - X2 * uy + 0.5 * X2 - 0.5) * k2 + (-0.25 * X2 - 0.25 * Y2 + 0.25 * uy + 0.25) * k3 +
+            (0.25 * X2 - 0.25 * Y2 + 0.25 * uy - 0.25) * k4 + (ux - 2.0 * ux * uy) * k5 + (0.5 - uy) * k6 +
+            (-ux) * k7 - 0.5 * k8;
+    fs[5] = (0.25 * (X2 * Y2) + 0.25 * (X2 * uy) + 0.25 * (ux * Y2) + 0.25 * (ux * uy)) * k0 +
+            (0.25 * uy + 0.5 * (ux * uy) + 0.5 * (ux * Y2) + 0.25 * Y2) * k1 +
+            (0.25 * ux + 0.5 * (ux * uy) + 0.5 * (X2 * uy) + 0.25 * X2) * k2 +
+            (0.125 * X2 + 0.125 * ux + 0.125 * Y2 + 0.125 * uy) * k3 +
+            (-0.125 * X2 - 0.125 * ux + 0.125 * Y2 + 0.125 * uy) * k4 + (0.5 * ux + 0.5 * uy + ux * uy + 0.25) * k5 +
+            (0.5 * uy + 0.25) * k6 + (0.5 * ux + 0.25) * k7 + 0.25 * k8;
+    fs[6] = (0.25 * (X2 * Y2) - 0.25 * (X2 * uy) - 0.25 * (ux * Y2) + 0.25 * (ux * uy)) * k0 +
+            (0.25 * uy - 0.5 * (ux * uy) + 0.5 * (ux * Y2) - 0.25 * Y2) * k1 +
+            (0.25 * ux - 0.5 * (ux * uy) + 0.5 * (X2 * uy) - 0.25 * X2) * k2 +
+            (0.125 * X2 - 0.125 * ux + 0.125 * Y2 - 0.125 * uy) * k3 +
+            (-0.125 * X2 + 0.125 * ux + 0.125 * Y2 - 0.125 * uy) * k4 + (ux * uy - 0.5 * uy - 0.5 * ux + 0.25) * k5 +
+            (0.5 * uy - 0.25) * k6 + (0.5 * ux - 0.25) * k7 + 0.25 * k8;
+    fs[7] = (0.25 * (X2 * Y2) - 0.25 * (X2 * uy) + 0.25 * (ux * Y2) - 0.25 * (ux * uy)) * k0 +
+            (0.5 * (ux * Y2) - 0.5 * (ux * uy) - 0.25 * uy + 0.25 * Y2) * k1 +
+            (0.5 * (ux * uy) - 0.25 * ux + 0.5 * (X2 * uy) - 0.25 * X2) * k2 +
+            (0.125 * X2 + 0.125 * ux + 0.125 * Y2 - 0.125 * uy) * k3 +
+            (-0.125 * X2 - 0.125 * ux + 0.125 * Y2 - 0.125 * uy) * k4 + (0.5 * uy - 0.5 * ux + ux * uy - 0.25) * k5 +
+            (0.5 * uy - 0.25) * k6 + (0.5 * ux + 0.25) * k7 + 0.25 * k8;
+    fs[8] = (0.25 * (X2 * Y2) + 0.25 * (X2 * uy) - 0.25 * (ux * Y2) - 0.25 * (ux * uy)) * k0 +
+            (0.5 * (ux * uy) - 0.25 * uy + 0.5 * (ux * Y2) - 0.25 * Y2) * k1 +
+            (0.5 * (X2 * uy) - 0.5 * (ux * uy) - 0.25 * ux + 0.25 * X2) * k2 +
+            (0.125 * X2 - 0.125 * ux + 0.125 * Y2 + 0.125 * uy) * k3 +
+            (-0.125 * X2 + 0.125 * ux + 0.125 * Y2 + 0.125 * uy) * k4 + (0.5 * ux - 0.5 * uy + ux * uy - 0.25) * k5 +
+            (0.5 * uy + 0.25) * k6 + (0.5 * ux - 0.25) * k7 + 0.25 * k8;
+}
+
+}  // namespace life

@@ -1,0 +1,167 @@
+// Immersed-boundary kernels (FP64), rigid and flexible markers.
+//
+//   k_ibm_interp    one thread per marker: rho and rho*u at the marker's
+//                   support sites (reconstructed from P_t exactly as the step
+//                   kernel computed them), then the direct force
+//                   (IBMNodeClass::interpolate + forceCalc,
+//                   reference src/IBMNode.cpp:26-58)
+//   k_ibm_clear     zero last step's IBM force at its support sites
+//   k_ibm_mark      list the 16x16 lattice tiles touched by any support
+//   k_ibm_spread    one CTA per touched tile: every site of the tile sums the
+//                   contributions of the markers that reach it in marker order
+//                   (the reference's ORDERED reduction, src/IBMNode.cpp:61-94)
+//                   without atomics, applies the IBM velocity correction
+//                   (updateMacroscopic, src/IBMNode.cpp:97-136) and collides
+//                   the site again for the next step with the IBM force.
+#include <cuda_runtime.h>
+
+#include "collide_cm.cuh"
+#include "ibm_kernels.h"
+#include "lbm_device.cuh"
+
+namespace life {
+
+constexpr int TILE = 16;
+
+template <bool CM>
+__global__ void k_ibm_interp(const double* __restrict__ P, LatDev L, int t, MarkerDev M, double velScale) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= M.n) return;
+    double iRho = 0.0, iMx = 0.0, iMy = 0.0;
+    const int ns = M.nsupp[k];
+    int imin = 1 << 30, imax = -(1 << 30), jmin = 1 << 30, jmax = -(1 << 30);
+    for (int s = 0; s < ns; s++) {
+        const int i = M.si[k * 9 + s], j = M.sj[k * 9 + s];
+        const double d = M.sd[k * 9 + s];
+        double f[9], rho, ux, uy;
+        site_state<CM>(P, L, t, i, j, f, rho, ux, uy);
+        iRho += rho * d * 1.0 * 1.0;
+        iMx += rho * ux * d * 1.0 * 1.0;
+        iMy += rho * uy * d * 1.0 * 1.0;
+        imin = min(imin, i); imax = max(imax, i);
+        jmin = min(jmin, j); jmax = max(jmax, j);
+    }
+    const double sc = velScale * iRho;
+    M.force[k * 2 + 0] = 2.0 * (sc * M.vel[k * 2 + 0] - iMx);
+    M.force[k * 2 + 1] = 2.0 * (sc * M.vel[k * 2 + 1] - iMy);
+    M.bbox[k] = make_int4(imin, imax, jmin, jmax);
+}
+
+__global__ void k_ibm_clear(IbmScratch W, LatDev L) {
+    const int n = *W.nsites_prev;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const long long s = W.sites_prev[q];
+        W.force_ibm[s] = 0.0;
+        W.force_ibm[L.S + s] = 0.0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *W.nsites = 0;
+        *W.ntiles = 0;
+    }
+}
+
+__global__ void k_ibm_mark(MarkerDev M, IbmScratch W) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= M.n) return;
+    const int ns = M.nsupp[k];
+    for (int s = 0; s < ns; s++) {
+        const int tile = (M.sj[k * 9 + s] / TILE) * W.ntx + (M.si[k * 9 + s] / TILE);
+        if (atomicCAS(&W.tile_flag[tile], 0u, 1u) == 0u) W.tiles[atomicAdd(W.ntiles, 1)] = tile;
+    }
+}
+
+template <bool CM>
+__global__ void __launch_bounds__(256) k_ibm_spread(const double* __restrict__ A, double* __restrict__ B, LatDev L,
+                                                    int t, MarkerDev M, IbmScratch W) {
+    __shared__ int list[256];
+    __shared__ int warp_cnt[8];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ntiles = *W.ntiles;
+    for (int q = blockIdx.x; q < ntiles; q += gridDim.x) {
+        const int tile = W.tiles[q];
+        const int ti0 = (tile % W.ntx) * TILE, tj0 = (tile / W.ntx) * TILE;
+        const int i = ti0 + (tid % TILE), j = tj0 + (tid / TILE);
+        double ax = 0.0, ay = 0.0;
+        bool touched = false;
+        for (int c0 = 0; c0 < M.n; c0 += 256) {
+            const int k = c0 + tid;
+            bool hit = false;
+            if (k < M.n) {
+                const int4 bb = M.bbox[k];
+                hit = bb.x <= ti0 + TILE - 1 && bb.y >= ti0 && bb.z <= tj0 + TILE - 1 && bb.w >= tj0;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, hit);
+            if (lane == 0) warp_cnt[warp] = __popc(bal);
+            __syncthreads();
+            int off = 0, cnt = 0;
+            for (int w = 0; w < 8; w++) {
+                if (w < warp) off += warp_cnt[w];
+                cnt += warp_cnt[w];
+            }
+            if (hit) list[off + __popc(bal & ((1u << lane) - 1u))] = k;
+            __syncthreads();
+            // Marker order within the chunk is preserved by the ordered compaction.
+            for (int r = 0; r < cnt; r++) {
+                const int m = list[r];
+                const int ns = M.nsupp[m];
+                for (int s = 0; s < ns; s++)
+                    if (M.si[m * 9 + s] == i && M.sj[m * 9 + s] == j) {
+                        const double d = M.sd[m * 9 + s];
+                        const double e = M.eps[m], ds = M.ds[m];
+                        ax += M.force[m * 2 + 0] * e * ds * 1.0 * d;
+                        ay += M.force[m * 2 + 1] * e * ds * 1.0 * d;
+                        touched = true;
+                        break;
+                    }
+            }
+            __syncthreads();
+        }
+        if (tid == 0) W.tile_flag[tile] = 0u;
+        if (touched && i < L.Nx && j < L.Ny) {
+            const long long s = (long long)j * L.pitch + i;
+            W.force_ibm[s] = ax;
+            W.force_ibm[L.S + s] = ay;
+            W.sites[atomicAdd(W.nsites, 1)] = s;
+            double f[9], rho, ux, uy, Fx, Fy;
+            site_state<CM>(A, L, t, i, j, f, rho, ux, uy);
+            force_xy_at(L, t, Fx, Fy);
+            macroscopic_ibm(f, Fx, Fy, ax, ay, rho, ux, uy);
+            if (L.convective && i >= L.Nx - 3) {
+                const int c = i - (L.Nx - 3);
+                L.outlet_u[((size_t)c * L.Ny + j) * 2 + 0] = ux;
+                L.outlet_u[((size_t)c * L.Ny + j) * 2 + 1] = uy;
+            }
+            double Gx, Gy, fs[9];
+            force_xy_at(L, t + 1, Gx, Gy);
+            collide<CM>(f, rho, ux, uy, Gx + ax, Gy + ay, L.omega, L.cs, fs);
+#pragma unroll
+            for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = fs[v];
+        }
+    }
+}
+
+// ------------------------------------------------------------ launchers
+
+cudaError_t launch_ibm_interp(const double* P, const LatDev& L, int t, const MarkerDev& M, double velScale,
+                              cudaStream_t s) {
+    if (M.n == 0) return cudaSuccess;
+    const int nb = (M.n + 127) / 128;
+    if (L.cm) k_ibm_interp<true><<<nb, 128, 0, s>>>(P, L, t, M, velScale);
+    else k_ibm_interp<false><<<nb, 128, 0, s>>>(P, L, t, M, velScale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ibm_spread(const double* A, double* B, const LatDev& L, int t, const MarkerDev& M,
+                              const IbmScratch& W, cudaStream_t s) {
+    k_ibm_clear<<<8, 256, 0, s>>>(W, L);
+    if (M.n > 0) {
+        k_ibm_mark<<<(M.n + 127) / 128, 128, 0, s>>>(M, W);
+        int grid = W.max_tiles < 4 * 152 ? W.max_tiles : 4 * 152;
+        if (grid < 1) grid = 1;
+        if (L.cm) k_ibm_spread<true><<<grid, 256, 0, s>>>(A, B, L, t, M, W);
+        else k_ibm_spread<false><<<grid, 256, 0, s>>>(A, B, L, t, M, W);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace life

@@ -1,0 +1,242 @@
+// Host side of the immersed bodies: device upload of the markers, the
+// per-step IBM sequence (ObjectsClass::objectKernel, reference
+// src/Objects.cpp:26-60) and the marker/body accessors of the C-ABI.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fem_kernels.h"
+#include "ibm_kernels.h"
+#include "life_internal.h"
+
+using namespace life;
+
+#define CK(call)                                              \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+    } while (0)
+
+static int alloc_track(LifeCase* c, void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 8);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return set_error(LIFE_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    c->allocs.push_back(*p);
+    c->dev_bytes += bytes;
+    return LIFE_OK;
+}
+template <class T>
+static int alloc_t(LifeCase* c, T** p, size_t n) {
+    return alloc_track(c, (void**)p, sizeof(T) * n);
+}
+
+// Copies the host marker table to the device arrays.
+int push_markers(LifeCase* c) {
+    const auto& m = c->obj.m;
+    const int n = (int)m.size();
+    std::vector<double> pos(2 * n), vel(2 * n), force(2 * n), eps(n), ds(n), sd(9 * n);
+    std::vector<int> ns(n), si(9 * n), sj(9 * n), body(n);
+    for (int k = 0; k < n; k++) {
+        for (int d = 0; d < 2; d++) {
+            pos[2 * k + d] = m[k].pos[d];
+            vel[2 * k + d] = m[k].vel[d];
+            force[2 * k + d] = m[k].force[d];
+        }
+        eps[k] = m[k].eps;
+        ds[k] = m[k].ds;
+        ns[k] = m[k].nsupp;
+        body[k] = m[k].body;
+        for (int s = 0; s < 9; s++) {
+            si[9 * k + s] = m[k].si[s];
+            sj[9 * k + s] = m[k].sj[s];
+            sd[9 * k + s] = m[k].sd[s];
+        }
+    }
+    MarkerDev& M = c->M;
+    cudaStream_t s = c->stream;
+    CK(cudaMemcpyAsync(M.pos, pos.data(), 16 * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(M.vel, vel.data(), 16 * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(M.force, force.data(), 16 * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(M.eps, eps.data(), 8 * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(M.ds, ds.data(), 8 * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(M.nsupp, ns.data(), 4 * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(M.si, si.data(), 36 * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(M.sj, sj.data(), 36 * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(M.sd, sd.data(), 72 * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(M.body, body.data(), 4 * n, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    return LIFE_OK;
+}
+
+int upload_markers(LifeCase* c) {
+    const int n = (int)c->obj.m.size();
+    MarkerDev& M = c->M;
+    M.n = n;
+    int rc;
+    if ((rc = alloc_t(c, &M.pos, 2 * n)) || (rc = alloc_t(c, &M.vel, 2 * n)) || (rc = alloc_t(c, &M.force, 2 * n)) ||
+        (rc = alloc_t(c, &M.eps, n)) || (rc = alloc_t(c, &M.ds, n)) || (rc = alloc_t(c, &M.nsupp, n)) ||
+        (rc = alloc_t(c, &M.si, 9 * n)) || (rc = alloc_t(c, &M.sj, 9 * n)) || (rc = alloc_t(c, &M.sd, 9 * n)) ||
+        (rc = alloc_t(c, &M.bbox, n)) || (rc = alloc_t(c, &M.body, n)))
+        return rc;
+    if ((rc = push_markers(c))) return rc;
+    IbmScratch& W = c->W;
+    W.ntx = (c->Nx + 15) / 16;
+    W.nty = (c->Ny + 15) / 16;
+    W.max_tiles = W.ntx * W.nty;
+    if ((rc = alloc_t(c, &W.force_ibm, (size_t)2 * c->S)) || (rc = alloc_t(c, &W.sites, (size_t)9 * n + 1)) ||
+        (rc = alloc_t(c, &W.sites_prev, (size_t)9 * n + 1)) || (rc = alloc_t(c, &W.nsites, 1)) ||
+        (rc = alloc_t(c, &W.nsites_prev, 1)) || (rc = alloc_t(c, &W.tile_flag, (size_t)W.max_tiles)) ||
+        (rc = alloc_t(c, &W.tiles, (size_t)W.max_tiles)) || (rc = alloc_t(c, &W.ntiles, 1)))
+        return rc;
+    CK(cudaMemsetAsync(W.force_ibm, 0, sizeof(double) * 2 * c->S, c->stream));
+    CK(cudaMemsetAsync(W.nsites, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(W.nsites_prev, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(W.tile_flag, 0, sizeof(unsigned) * W.max_tiles, c->stream));
+    CK(cudaMemsetAsync(W.ntiles, 0, sizeof(int), c->stream));
+    if ((rc = alloc_t(c, &c->d_fsi, 1)) || (rc = alloc_t(c, &c->d_status, 4))) return rc;
+    FsiScalars f{};
+    f.relax = c->p.relaxMax;
+    CK(cudaMemcpyAsync(c->d_fsi, &f, sizeof f, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->d_status, 0, 4 * sizeof(int), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return LIFE_OK;
+}
+
+// One step of ObjectsClass::objectKernel on the device.
+int ibm_step(LifeCase* c, int t, const double* A, double* B) {
+    LatDev L = lattice_view(c, t);
+    cudaError_t e;
+    if (c->obj.hasFlex) {
+        int rc = fem_fsi_loop(c, t, A, L);
+        if (rc) return rc;
+    } else {
+        e = launch_ibm_interp(A, L, t, c->M, c->Dt / c->Dx, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "ibm_interp");
+    }
+    e = launch_ibm_spread(A, B, L, t, c->M, c->W, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "ibm_spread");
+    std::swap(c->W.sites, c->W.sites_prev);
+    std::swap(c->W.nsites, c->W.nsites_prev);
+    return LIFE_OK;
+}
+
+extern "C" int life_case_get_markers(LifeCase* c, double* pos, double* vel, double* force, double* epsilon,
+                                     double* ds, int32_t* body_index) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    const int n = c->M.n;
+    if (n == 0) return LIFE_OK;
+    cudaStream_t s = c->stream;
+    if (pos) CK(cudaMemcpyAsync(pos, c->M.pos, 16 * n, cudaMemcpyDeviceToHost, s));
+    if (vel) CK(cudaMemcpyAsync(vel, c->M.vel, 16 * n, cudaMemcpyDeviceToHost, s));
+    if (force) CK(cudaMemcpyAsync(force, c->M.force, 16 * n, cudaMemcpyDeviceToHost, s));
+    if (epsilon) CK(cudaMemcpyAsync(epsilon, c->M.eps, 8 * n, cudaMemcpyDeviceToHost, s));
+    if (ds) CK(cudaMemcpyAsync(ds, c->M.ds, 8 * n, cudaMemcpyDeviceToHost, s));
+    if (body_index) CK(cudaMemcpyAsync(body_index, c->M.body, 4 * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return LIFE_OK;
+}
+
+extern "C" int life_case_get_bodies(LifeCase* c, int32_t* ids, int32_t* flexible, int32_t* n_markers,
+                                    int32_t* n_fem_nodes) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    for (size_t k = 0; k < c->obj.b.size(); k++) {
+        const HBody& b = c->obj.b[k];
+        if (ids) ids[k] = b.ID;
+        if (flexible) flexible[k] = b.flex;
+        if (n_markers) n_markers[k] = (int)b.nodes.size();
+        if (n_fem_nodes) n_fem_nodes[k] = b.fem ? b.fem->nNodes : 0;
+    }
+    return LIFE_OK;
+}
+
+// ObjectsClass::writeTotalForces (src/Objects.cpp:517-528): sequential sum
+// over markers, in lattice units scaled to newtons.
+extern "C" int life_case_total_force(LifeCase* c, double* fx, double* fy) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    const int n = c->M.n;
+    std::vector<double> force(2 * n), eps(n), ds(n);
+    if (n) {
+        int rc = life_case_get_markers(c, nullptr, nullptr, force.data(), eps.data(), ds.data(), nullptr);
+        if (rc) return rc;
+    }
+    const double forceScale = c->Dm * c->Dx / (c->Dt * c->Dt) * 1.0 / c->Dx;
+    double F[2] = {0.0, 0.0};
+    for (int k = 0; k < n; k++)
+        for (int d = 0; d < 2; d++) F[d] -= force[2 * k + d] * 1.0 * eps[k] * ds[k] * forceScale;
+    if (fx) *fx = F[0];
+    if (fy) *fy = F[1];
+    return LIFE_OK;
+}
+
+extern "C" int life_parse_geometry(const char* text, LifeBodyDesc* out, int32_t cap, int32_t* n) {
+    if (!text || !n) return set_error(LIFE_ERR_INVALID, "NULL argument");
+    // Skip the leading comment lines (src/Objects.cpp:338-353).
+    const char* p = text;
+    while (*p == '#') {
+        while (*p && *p != '\n') p++;
+        if (*p == '\n') p++;
+    }
+    std::vector<std::string> tok;
+    std::string cur;
+    for (; *p; p++) {
+        if (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r') {
+            if (!cur.empty()) tok.push_back(cur);
+            cur.clear();
+        } else {
+            cur += *p;
+        }
+    }
+    if (!cur.empty()) tok.push_back(cur);
+    int count = 0;
+    size_t q = 0;
+    try {
+        while (q < tok.size()) {
+            LifeBodyDesc d{};
+            if (tok[q] == "CIRCLE") {
+                if (q + 8 > tok.size()) return set_error(LIFE_ERR_GEOMETRY, "truncated CIRCLE line");
+                d.kind = LIFE_BODY_CIRCLE;
+                d.number = std::stoi(tok[q + 1]);
+                d.id = std::stoi(tok[q + 2]);
+                d.x = std::stod(tok[q + 3]);
+                d.y = std::stod(tok[q + 4]);
+                d.dx = std::stod(tok[q + 5]);
+                d.dy = std::stod(tok[q + 6]);
+                d.radius = std::stod(tok[q + 7]);
+                q += 8;
+            } else if (tok[q] == "FILAMENT") {
+                if (q + 15 > tok.size()) return set_error(LIFE_ERR_GEOMETRY, "truncated FILAMENT line");
+                d.kind = LIFE_BODY_FILAMENT;
+                d.number = std::stoi(tok[q + 1]);
+                d.id = std::stoi(tok[q + 2]);
+                d.x = std::stod(tok[q + 3]);
+                d.y = std::stod(tok[q + 4]);
+                d.dx = std::stod(tok[q + 5]);
+                d.dy = std::stod(tok[q + 6]);
+                d.length = std::stod(tok[q + 7]);
+                d.height = std::stod(tok[q + 8]);
+                d.angle_deg = std::stod(tok[q + 9]);
+                if (tok[q + 10] == "FLEXIBLE") d.flexible = 1;
+                else if (tok[q + 10] == "RIGID") d.flexible = 0;
+                else return set_error(LIFE_ERR_GEOMETRY, "Not a proper flexible type set...exiting");
+                d.n_elements = tok[q + 11] == "CONFORMING" ? 0 : (int)std::stod(tok[q + 11]);
+                d.clamped = tok[q + 12] == "CLAMPED" ? 1 : 0;
+                d.rho = std::stod(tok[q + 13]);
+                d.E = std::stod(tok[q + 14]);
+                q += 15;
+            } else {
+                return set_error(LIFE_ERR_GEOMETRY, "unknown geometry keyword '" + tok[q] + "'");
+            }
+            if (out && count < cap) out[count] = d;
+            count++;
+        }
+    } catch (...) {
+        return set_error(LIFE_ERR_GEOMETRY, "malformed number in geometry.config");
+    }
+    *n = count;
+    return LIFE_OK;
+}

@@ -1,0 +1,43 @@
+// Device marker state and the IBM kernel launchers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "life_types.h"
+
+namespace life {
+
+// Markers in global order (the reference's iNode order after de-overlap).
+struct MarkerDev {
+    int n;
+    double* pos;    // [n][2]
+    double* vel;    // [n][2]
+    double* force;  // [n][2]
+    double* eps;    // [n]
+    double* ds;     // [n]
+    int* nsupp;     // [n]
+    int* si;        // [n][9]
+    int* sj;        // [n][9]
+    double* sd;     // [n][9] delta weights
+    int4* bbox;     // [n] support bounding box (imin, imax, jmin, jmax)
+    int* body;      // [n] owning body
+};
+
+// Scratch of the tile-owner spread.
+struct IbmScratch {
+    double* force_ibm;        // [2][S] dense IBM force of the current step
+    long long* sites;         // support sites written this step
+    long long* sites_prev;    // support sites of the previous step
+    int* nsites;
+    int* nsites_prev;
+    unsigned* tile_flag;      // [ntx*nty]
+    int* tiles;               // touched tiles
+    int* ntiles;
+    int ntx, nty, max_tiles;
+};
+
+cudaError_t launch_ibm_interp(const double* P, const LatDev& L, int t, const MarkerDev& M, double velScale,
+                              cudaStream_t s);
+cudaError_t launch_ibm_spread(const double* A, double* B, const LatDev& L, int t, const MarkerDev& M,
+                              const IbmScratch& W, cudaStream_t s);
+
+}  // namespace life

@@ -1,0 +1,277 @@
+// Device-side lattice primitives shared by the lattice, IBM and export
+// kernels: D2Q9 constants, site classification, the pull gather, macroscopic
+// moments, the regularised / convective boundary conditions and the BGK and
+// central-moment collisions in FP64.
+//
+// State convention. The device keeps P_t: the post-collision populations of
+// step t, before streaming, in structure-of-arrays layout
+//   P[v*S + j*pitch + i]   (x fastest; S = pitch*Ny).
+// The reference's state after step t (post-stream f, rho, u; reference
+// GridClass::lbmKernel, src/Grid.cpp:36-100) is a pure function of P_t plus a
+// few per-step scalars, and site_state() computes it for any site. Every
+// kernel that needs rho/u/f at a site (the fused step kernel, boundary sites,
+// IBM interpolation, field export) calls the same function, so all of them see
+// bit-identical values.
+//
+// FP64 translation units are compiled with --fmad=false and keep the
+// reference's operation order, so a + b*c is rounded twice as g++ does on x86.
+#pragma once
+#include <cstdint>
+
+#include "life_types.h"
+
+namespace life {
+
+__host__ __device__ constexpr int cx_of(int v) { return v == 1 || v == 5 || v == 7 ? 1 : (v == 2 || v == 6 || v == 8 ? -1 : 0); }
+__host__ __device__ constexpr int cy_of(int v) { return v == 3 || v == 5 || v == 8 ? 1 : (v == 4 || v == 6 || v == 7 ? -1 : 0); }
+__host__ __device__ constexpr int opp_of(int v) { return v == 0 ? 0 : (v % 2 == 1 ? v + 1 : v - 1); }
+
+// Lattice weights exactly as GridClass::GridClass builds them (4/9, 1/9, 1/36).
+__device__ __forceinline__ double wgt(int v) {
+    return v == 0 ? 4.0 / 9.0 : (v < 5 ? 1.0 / 9.0 : 1.0 / 36.0);
+}
+
+#define LSQ(x) ((x) * (x))
+#define LQU(x) ((x) * (x) * (x) * (x))
+
+// Site type from the wall configuration; y walls override x walls at the
+// corners (reference src/Grid.cpp:925-951).
+__device__ __forceinline__ int site_type(const LatDev& L, int i, int j) {
+    int t = LIFE_FLUID;
+    if (i == 0) t = L.wall[0];
+    else if (i == L.Nx - 1) t = L.wall[1];
+    if (j == 0) t = L.wall[2];
+    else if (j == L.Ny - 1) t = L.wall[3];
+    return t;
+}
+
+// Outward-facing normal into the fluid and its direction
+// (GridClass::getNormalVector, src/Grid.cpp:498-545). Corners next to a
+// periodic wall become edges. A corner surrounded by periodic sites is
+// rejected when the case is created.
+__device__ __forceinline__ void site_normal(const LatDev& L, int i, int j, int& nx, int& ny, int& nd) {
+    nx = 0; ny = 0; nd = 0;
+    if (i == 0) { nx = 1; nd = 0; }
+    else if (i == L.Nx - 1) { nx = -1; nd = 0; }
+    if (j == 0) { ny = 1; nd = 1; }
+    else if (j == L.Ny - 1) { ny = -1; nd = 1; }
+    if (nx != 0 && ny != 0) {
+        int tx = site_type(L, i + nx, j), ty = site_type(L, i, j + ny);
+        if (tx == LIFE_FLUID && ty != LIFE_FLUID) { nd = 0; ny = 0; }
+        else if (ty == LIFE_FLUID && tx != LIFE_FLUID) { nd = 1; nx = 0; }
+    }
+}
+
+// Pull gather: the post-stream population v at (i,j) is the post-collision
+// population v of the upwind site (i-cx, j-cy), with periodic wrap
+// (the push index of src/Grid.cpp:229,240 read backwards).
+template <class T>
+__device__ __forceinline__ void gather(const T* __restrict__ P, const LatDev& L, int i, int j, double f[9]) {
+#pragma unroll
+    for (int v = 0; v < 9; v++) {
+        int si = i - cx_of(v), sj = j - cy_of(v);
+        si = si < 0 ? si + L.Nx : (si >= L.Nx ? si - L.Nx : si);
+        sj = sj < 0 ? sj + L.Ny : (sj >= L.Ny ? sj - L.Ny : sj);
+        f[v] = (double)P[(size_t)v * L.S + (size_t)sj * L.pitch + si];
+    }
+}
+
+// GridClass::macroscopic (src/Grid.cpp:282-299)
+__device__ __forceinline__ void macroscopic(const double f[9], double Fx, double Fy, double& rho,
+                                            double& ux, double& uy) {
+    double r = 0.0, mx = 0.0, my = 0.0;
+#pragma unroll
+    for (int v = 0; v < 9; v++) {
+        r = r + f[v];
+        mx = mx + (double)cx_of(v) * f[v];
+        my = my + (double)cy_of(v) * f[v];
+    }
+    rho = r;
+    ux = (mx + 0.5 * Fx) / r;
+    uy = (my + 0.5 * Fy) / r;
+}
+
+// IBMNodeClass::updateMacroscopic form (src/IBMNode.cpp:113-122): the IBM
+// force enters the velocity at support sites.
+__device__ __forceinline__ void macroscopic_ibm(const double f[9], double Fx, double Fy, double Ix,
+                                                double Iy, double& rho, double& ux, double& uy) {
+    double r = 0.0, mx = 0.0, my = 0.0;
+#pragma unroll
+    for (int v = 0; v < 9; v++) {
+        r = r + f[v];
+        mx = mx + (double)cx_of(v) * f[v];
+        my = my + (double)cy_of(v) * f[v];
+    }
+    rho = r;
+    ux = (mx + 0.5 * (Fx + Ix)) / r;
+    uy = (my + 0.5 * (Fy + Iy)) / r;
+}
+
+// GridClass::equilibrium (src/Grid.cpp:249-264): 2nd-order Hermite (BGK) or
+// the 4th-order product form used with central moments.
+template <bool CM>
+__device__ __forceinline__ double equilibrium(int v, double rho, double ux, double uy) {
+    const int cx = cx_of(v), cy = cy_of(v);
+    if (CM)
+        return 0.25 * rho * wgt(v) * (9.0 * LSQ(cx) * LSQ(ux) + 6.0 * cx * ux - 3.0 * LSQ(ux) + 2.0) *
+               (9.0 * LSQ(cy) * LSQ(uy) + 6.0 * cy * uy - 3.0 * LSQ(uy) + 2.0);
+    return rho * wgt(v) *
+           (1.0 + 3.0 * (cx * ux + cy * uy) + 4.5 * (LSQ(ux) * (LSQ(cx) - 1.0 / 3.0) + LSQ(uy) * (LSQ(cy) - 1.0 / 3.0)) +
+            9.0 * cx * cy * ux * uy);
+}
+
+// GridClass::latticeForce (src/Grid.cpp:267-279), Guo forcing for BGK.
+__device__ __forceinline__ double lattice_force(int v, double ux, double uy, double Fx, double Fy) {
+    const int cx = cx_of(v), cy = cy_of(v);
+    return 3.0 * wgt(v) *
+           (Fx * (cx - ux + cx * 3.0 * (cx * ux + cy * uy)) + (Fy * (cy - uy + cy * 3.0 * (cx * ux + cy * uy))));
+}
+
+// BGK collision (src/Grid.cpp:236-244).
+__device__ __forceinline__ void collide_bgk(const double f[9], double rho, double ux, double uy, double Fx,
+                                            double Fy, double omega, double fs[9]) {
+#pragma unroll
+    for (int v = 0; v < 9; v++)
+        fs[v] = f[v] + omega * (equilibrium<false>(v, rho, ux, uy) - f[v]) +
+                (1.0 - 0.5 * omega) * lattice_force(v, ux, uy, Fx, Fy);
+}
+
+// Central-moments collision (De Rosis 2019; src/Grid.cpp:106-233), in collide_cm.cuh.
+__device__ __forceinline__ void collide_cm(const double f[9], double rho, double ux, double uy, double Fx,
+                                           double Fy, double omega, double cs, double fs[9]);
+
+// One time step's scalars: the inlet ramp used by the boundary conditions of
+// step t and the uniform pressure-gradient force of step t (Womersley).
+__device__ __forceinline__ void force_xy_at(const LatDev& L, int t, double& Fx, double& Fy) {
+    if (L.womersley) {
+        const StepScalars& s = L.steps[t - L.t_base];
+        Fx = s.fx;
+        Fy = s.fy;
+    } else {
+        Fx = L.Fx0;
+        Fy = L.Fy0;
+    }
+}
+
+// Post-macroscopic moments of a fluid site of step t (read by boundary sites:
+// Utils::extrapolate / zeroGradient, inc/Utils.h:137-217).
+template <class T>
+__device__ __forceinline__ void fluid_moments(const T* __restrict__ P, const LatDev& L, int i, int j, double Fx,
+                                              double Fy, double& rho, double& ux, double& uy) {
+    double f[9];
+    gather(P, L, i, j, f);
+    macroscopic(f, Fx, Fy, rho, ux, uy);
+}
+
+// GridClass::regularisedBC (src/Grid.cpp:387-465) on a local copy of the
+// site's populations; rn/uxn/uyn are the site's rho_n/u_n values as applyBCs
+// left them.
+template <bool CM>
+__device__ __forceinline__ void regularised(double f[9], int type, int nx, int ny, int nd, double& rn, double un[2],
+                                            double cs, double rho_x1, double rho_x2) {
+    const bool corner = (nx != 0 && ny != 0);
+    const int nn = nd == 0 ? nx : ny;
+    if (corner) {
+        if (type == LIFE_VELOCITY || type == LIFE_WALL || type == LIFE_FREESLIP) rn = 2.0 * rho_x1 - rho_x2;
+    } else {
+        double fplus = 0.0, fzero = 0.0;
+#pragma unroll
+        for (int v = 0; v < 9; v++) {
+            int cn = nd == 0 ? cx_of(v) : cy_of(v);
+            if (cn == -nn) fplus += f[v];
+            else if (cn == 0) fzero += f[v];
+        }
+        if (type == LIFE_VELOCITY || type == LIFE_WALL || type == LIFE_FREESLIP)
+            rn = (2.0 * fplus + fzero) / (1.0 - nn * un[nd]);
+        else if (type == LIFE_PRESSURE)
+            un[nd] = nn * (1.0 - (2.0 * fplus + fzero) / rn);
+    }
+    double Sxx = 0.0, Syy = 0.0, Sxy = 0.0;
+#pragma unroll
+    for (int v = 0; v < 9; v++) {
+        const int cx = cx_of(v), cy = cy_of(v);
+        double feq = equilibrium<CM>(v, rn, un[0], un[1]);
+        if (corner) {
+            if (cx == nx || cy == ny) {
+                if (nx * cx + ny * cy == 0) f[v] = feq;
+                else f[v] = feq + (f[opp_of(v)] - equilibrium<CM>(opp_of(v), rn, un[0], un[1]));
+            }
+        } else {
+            int cn = nd == 0 ? cx : cy;
+            if (cn == nn) f[v] = feq + (f[opp_of(v)] - equilibrium<CM>(opp_of(v), rn, un[0], un[1]));
+        }
+        double fneq = f[v] - feq;
+        Sxx += (double)(cx * cx) * fneq;
+        Syy += (double)(cy * cy) * fneq;
+        Sxy += (double)(cx * cy) * fneq;
+    }
+    const double cs2 = LSQ(cs);
+#pragma unroll
+    for (int v = 0; v < 9; v++) {
+        const int cx = cx_of(v), cy = cy_of(v);
+        f[v] = equilibrium<CM>(v, rn, un[0], un[1]) +
+               (wgt(v) / (2.0 * LQU(cs))) *
+                   ((((double)(cx * cx) - cs2) * Sxx) + (((double)(cy * cy) - cs2) * Syy) + (2.0 * cx * cy * Sxy));
+    }
+}
+
+// The reference state of step t at site (i,j): post-stream populations after
+// the boundary condition (GridClass::applyBCs, src/Grid.cpp:302-384;
+// convectiveBC :468-474) and the macroscopic moments (without the IBM
+// correction, which support sites receive afterwards).
+template <bool CM, class T>
+__device__ __forceinline__ void site_state(const T* __restrict__ P, const LatDev& L, int t, int i, int j, double f[9],
+                                           double& rho, double& ux, double& uy) {
+    gather(P, L, i, j, f);
+    double Fx, Fy;
+    force_xy_at(L, t, Fx, Fy);
+    const int type = site_type(L, i, j);
+    if (type != LIFE_FLUID) {
+        if (type == LIFE_CONVECTIVE) {
+            const double* fp = L.outlet_f_prev + (size_t)j * 3;
+            const double dU0 = L.delU[j * 2 + 0], dU1 = L.delU[j * 2 + 1];
+            f[2] = fp[0] + 3.0 * wgt(2) * (dU0 * cx_of(2) + dU1 * cy_of(2));
+            f[6] = fp[1] + 3.0 * wgt(6) * (dU0 * cx_of(6) + dU1 * cy_of(6));
+            f[8] = fp[2] + 3.0 * wgt(8) * (dU0 * cx_of(8) + dU1 * cy_of(8));
+        } else {
+            int nx, ny, nd;
+            site_normal(L, i, j, nx, ny, nd);
+            double rn = 0.0, un[2] = {0.0, 0.0};
+            double r1 = 0.0, r2 = 0.0;
+            const bool corner = (nx != 0 && ny != 0);
+            if (type == LIFE_VELOCITY) {
+                const double ramp = L.steps[t - L.t_base].ramp;
+                un[0] = L.u_in[j * 2 + 0] * ramp;
+                un[1] = L.u_in[j * 2 + 1] * ramp;
+            } else if (type == LIFE_FREESLIP || type == LIFE_PRESSURE) {
+                // zeroGradient order 2 along the normal on the new velocity field
+                double q1, a1x, a1y, q2, a2x, a2y;
+                fluid_moments(P, L, i + nx, j + ny, Fx, Fy, q1, a1x, a1y);
+                fluid_moments(P, L, i + 2 * nx, j + 2 * ny, Fx, Fy, q2, a2x, a2y);
+                if (type == LIFE_FREESLIP) un[nd] = 0.0;
+                else rn = L.rho_in[j];
+                const int d = 1 - nd;
+                const double a1 = d == 0 ? a1x : a1y, a2 = d == 0 ? a2x : a2y;
+                un[d] = (4.0 / 3.0) * a1 - (1.0 / 3.0) * a2;
+                r1 = q1;
+                r2 = q2;
+            }
+            if (corner && (type == LIFE_VELOCITY || type == LIFE_WALL)) {
+                double a, b;
+                fluid_moments(P, L, i + nx, j + ny, Fx, Fy, r1, a, b);
+                fluid_moments(P, L, i + 2 * nx, j + 2 * ny, Fx, Fy, r2, a, b);
+            }
+            regularised<CM>(f, type, nx, ny, nd, rn, un, L.cs, r1, r2);
+        }
+    }
+    macroscopic(f, Fx, Fy, rho, ux, uy);
+}
+
+template <bool CM>
+__device__ __forceinline__ void collide(const double f[9], double rho, double ux, double uy, double Fx, double Fy,
+                                        double omega, double cs, double fs[9]) {
+    if (CM) collide_cm(f, rho, ux, uy, Fx, Fy, omega, cs, fs);
+    else collide_bgk(f, rho, ux, uy, Fx, Fy, omega, fs);
+}
+
+}  // namespace life

@@ -1,0 +1,243 @@
+// FP64 lattice kernels: the plain form that reproduces the reference's CPU
+// FP64 results. Compiled with --fmad=false (see the header of lbm_device.cuh).
+//
+//   k_init_f64      initial equilibrium state and the first collision
+//   k_step_f64      fused pull-stream + macroscopic + boundary conditions +
+//                   collision of the next step (one read and one write of the
+//                   nine populations per site)
+//   k_outlet_f64    convective outlet speed (sequential mean, as the reference)
+//   k_state_f64     collision from an explicit state (restart read)
+//   k_export_f64    reference-layout fields of the current step
+//   k_maxvel_f64    max |u| and NaN scan
+#include <cuda_runtime.h>
+
+#include "collide_cm.cuh"
+#include "lbm_device.cuh"
+#include "lbm_kernels.h"
+
+namespace life {
+
+// Outlet side outputs of step t: final u of the last three columns and the
+// post-BC f[2,6,8] of the outlet column.
+__device__ __forceinline__ void outlet_outputs(const LatDev& L, int i, int j, const double f[9], double ux, double uy) {
+    if (!L.convective) return;
+    int c = i - (L.Nx - 3);
+    if (c >= 0) {
+        L.outlet_u[((size_t)c * L.Ny + j) * 2 + 0] = ux;
+        L.outlet_u[((size_t)c * L.Ny + j) * 2 + 1] = uy;
+    }
+    if (i == L.Nx - 1) {
+        double* o = L.outlet_f_next + (size_t)j * 3;
+        o[0] = f[2];
+        o[1] = f[6];
+        o[2] = f[8];
+    }
+}
+
+template <bool CM>
+__device__ __forceinline__ void store_collided(double* __restrict__ B, const LatDev& L, int t_next, int i, int j,
+                                               const double f[9], double rho, double ux, double uy, double Ix,
+                                               double Iy) {
+    double Fx, Fy, fs[9];
+    force_xy_at(L, t_next, Fx, Fy);
+    collide<CM>(f, rho, ux, uy, Fx + Ix, Fy + Iy, L.omega, L.cs, fs);
+    const size_t s = (size_t)j * L.pitch + i;
+#pragma unroll
+    for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = fs[v];
+}
+
+// GridClass::initialiseGrid (reference src/Grid.cpp:998-1061): rho = 1,
+// initial velocity, f = feq; then the collision of step t0+1.
+template <bool CM>
+__global__ void k_init_f64(double* __restrict__ B, LatDev L, int t0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= L.Nx) return;
+    double ux, uy;
+    if (L.init_mode == 0) { ux = 0.0; uy = 0.0; }
+    else if (L.init_mode == 1) { ux = L.u_in[j * 2]; uy = L.u_in[j * 2 + 1]; }
+    else { ux = L.u0x; uy = L.u0y; }
+    if (site_type(L, i, j) == LIFE_WALL) { ux = 0.0; uy = 0.0; }
+    const double rho = 1.0;
+    double f[9];
+#pragma unroll
+    for (int v = 0; v < 9; v++) f[v] = equilibrium<CM>(v, rho, ux, uy);
+    outlet_outputs(L, i, j, f, ux, uy);
+    store_collided<CM>(B, L, t0 + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
+}
+
+// One time step: S_t from P_t (A), then P_{t+1} into B. IBM support sites are
+// collided again by the IBM fix-up kernel once the spread force is known.
+template <bool CM>
+__global__ void __launch_bounds__(128) k_step_f64(const double* __restrict__ A, double* __restrict__ B, LatDev L, int t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= L.Nx) return;
+    double f[9], rho, ux, uy;
+    site_state<CM>(A, L, t, i, j, f, rho, ux, uy);
+    outlet_outputs(L, i, j, f, ux, uy);
+    store_collided<CM>(B, L, t + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
+}
+
+// GridClass::convectiveSpeed (src/Grid.cpp:477-495): the mean outlet speed is
+// a sequential sum over j, as in the reference.
+__global__ void k_outlet_f64(LatDev L, double* __restrict__ delU) {
+    __shared__ double uOut_s;
+    const int Ny = L.Ny;
+    const double* u1 = L.outlet_u + (size_t)2 * Ny * 2;  // column Nx-1
+    const double* u2 = L.outlet_u + (size_t)1 * Ny * 2;  // column Nx-2
+    const double* u3 = L.outlet_u;                       // column Nx-3
+    if (threadIdx.x == 0) {
+        double uOut = 0.0;
+        for (int j = 0; j < Ny; j++) uOut += u1[j * 2];
+        uOut /= (double)Ny;
+        uOut_s = uOut;
+    }
+    __syncthreads();
+    const double uOut = uOut_s;
+    for (int j = threadIdx.x; j < Ny; j += blockDim.x)
+        for (int d = 0; d < 2; d++)
+            delU[j * 2 + d] = (-uOut / 2.0) * (3.0 * u1[j * 2 + d] - 4.0 * u2[j * 2 + d] + u3[j * 2 + d]);
+}
+
+// Collision from an explicit reference-layout state (GridClass::readRestart,
+// src/Grid.cpp:1072-1160, followed by the next step's collision).
+template <bool CM>
+__global__ void k_state_f64(double* __restrict__ B, LatDev L, int t, const double* __restrict__ rho_in,
+                            const double* __restrict__ u_in, const double* __restrict__ f_in,
+                            const double* __restrict__ fibm_in) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= L.Nx) return;
+    const size_t id = (size_t)i * L.Ny + j;
+    double f[9];
+#pragma unroll
+    for (int v = 0; v < 9; v++) f[v] = f_in[id * 9 + v];
+    const double rho = rho_in[id], ux = u_in[id * 2], uy = u_in[id * 2 + 1];
+    outlet_outputs(L, i, j, f, ux, uy);
+    store_collided<CM>(B, L, t + 1, i, j, f, rho, ux, uy, fibm_in[id * 2], fibm_in[id * 2 + 1]);
+}
+
+// Reference-layout export of the state after step t (what
+// GridClass::writeRestart dumps, src/Grid.cpp:1191-1222).
+template <bool CM>
+__global__ void k_export_f64(const double* __restrict__ P, LatDev L, int t, double* __restrict__ rho_out,
+                             double* __restrict__ u_out, double* __restrict__ f_out, double* __restrict__ fibm_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= L.Nx) return;
+    double f[9], rho, ux, uy;
+    site_state<CM>(P, L, t, i, j, f, rho, ux, uy);
+    double Ix = 0.0, Iy = 0.0;
+    if (L.force_ibm) {
+        const size_t s = (size_t)j * L.pitch + i;
+        Ix = L.force_ibm[s];
+        Iy = L.force_ibm[L.S + s];
+        if (Ix != 0.0 || Iy != 0.0) {
+            double Fx, Fy;
+            force_xy_at(L, t, Fx, Fy);
+            macroscopic_ibm(f, Fx, Fy, Ix, Iy, rho, ux, uy);
+        }
+    }
+    const size_t id = (size_t)i * L.Ny + j;
+    if (rho_out) rho_out[id] = rho;
+    if (u_out) { u_out[id * 2] = ux; u_out[id * 2 + 1] = uy; }
+    if (f_out)
+        for (int v = 0; v < 9; v++) f_out[id * 9 + v] = f[v];
+    if (fibm_out) { fibm_out[id * 2] = Ix; fibm_out[id * 2 + 1] = Iy; }
+}
+
+// Initial state (before any step) in reference layout.
+template <bool CM>
+__global__ void k_export_init_f64(LatDev L, double* __restrict__ rho_out, double* __restrict__ u_out,
+                                  double* __restrict__ f_out, double* __restrict__ fibm_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= L.Nx) return;
+    double ux, uy;
+    if (L.init_mode == 0) { ux = 0.0; uy = 0.0; }
+    else if (L.init_mode == 1) { ux = L.u_in[j * 2]; uy = L.u_in[j * 2 + 1]; }
+    else { ux = L.u0x; uy = L.u0y; }
+    if (site_type(L, i, j) == LIFE_WALL) { ux = 0.0; uy = 0.0; }
+    const size_t id = (size_t)i * L.Ny + j;
+    if (rho_out) rho_out[id] = 1.0;
+    if (u_out) { u_out[id * 2] = ux; u_out[id * 2 + 1] = uy; }
+    if (f_out)
+        for (int v = 0; v < 9; v++) f_out[id * 9 + v] = equilibrium<CM>(v, 1.0, ux, uy);
+    if (fibm_out) { fibm_out[id * 2] = 0.0; fibm_out[id * 2 + 1] = 0.0; }
+}
+
+// max |u| and NaN flag over the current state (GridClass::writeInfo,
+// src/Grid.cpp:562-588). out[0] = max as ordered bits, out[1] = NaN count.
+template <bool CM>
+__global__ void k_maxvel_f64(const double* __restrict__ P, LatDev L, int t, unsigned long long* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    double vel = 0.0;
+    bool nan = false;
+    if (i < L.Nx) {
+        double f[9], rho, ux, uy;
+        site_state<CM>(P, L, t, i, j, f, rho, ux, uy);
+        if (L.force_ibm) {
+            const size_t s = (size_t)j * L.pitch + i;
+            double Ix = L.force_ibm[s], Iy = L.force_ibm[L.S + s];
+            if (Ix != 0.0 || Iy != 0.0) {
+                double Fx, Fy;
+                force_xy_at(L, t, Fx, Fy);
+                macroscopic_ibm(f, Fx, Fy, Ix, Iy, rho, ux, uy);
+            }
+        }
+        vel = sqrt(ux * ux + uy * uy);
+        nan = vel != vel;
+        if (nan) vel = 0.0;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        vel = fmax(vel, __shfl_xor_sync(0xffffffffu, vel, o));
+        nan = __any_sync(0xffffffffu, nan);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&out[0], (unsigned long long)__double_as_longlong(vel));
+        if (nan) atomicAdd(&out[1], 1ull);
+    }
+}
+
+// ------------------------------------------------------------ launchers
+static inline dim3 grid_of(const LatDev& L) { return dim3((L.Nx + 127) / 128, L.Ny); }
+
+cudaError_t launch_init_f64(double* B, const LatDev& L, int t0, cudaStream_t s) {
+    if (L.cm) k_init_f64<true><<<grid_of(L), 128, 0, s>>>(B, L, t0);
+    else k_init_f64<false><<<grid_of(L), 128, 0, s>>>(B, L, t0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step_f64(const double* A, double* B, const LatDev& L, int t, cudaStream_t s) {
+    if (L.cm) k_step_f64<true><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
+    else k_step_f64<false><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_outlet_f64(const LatDev& L, double* delU, cudaStream_t s) {
+    k_outlet_f64<<<1, 256, 0, s>>>(L, delU);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_state_f64(double* B, const LatDev& L, int t, const double* rho, const double* u,
+                             const double* f, const double* fibm, cudaStream_t s) {
+    if (L.cm) k_state_f64<true><<<grid_of(L), 128, 0, s>>>(B, L, t, rho, u, f, fibm);
+    else k_state_f64<false><<<grid_of(L), 128, 0, s>>>(B, L, t, rho, u, f, fibm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export_f64(const double* P, const LatDev& L, int t, bool initial, double* rho, double* u,
+                              double* f, double* fibm, cudaStream_t s) {
+    if (initial) {
+        if (L.cm) k_export_init_f64<true><<<grid_of(L), 128, 0, s>>>(L, rho, u, f, fibm);
+        else k_export_init_f64<false><<<grid_of(L), 128, 0, s>>>(L, rho, u, f, fibm);
+    } else {
+        if (L.cm) k_export_f64<true><<<grid_of(L), 128, 0, s>>>(P, L, t, rho, u, f, fibm);
+        else k_export_f64<false><<<grid_of(L), 128, 0, s>>>(P, L, t, rho, u, f, fibm);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_maxvel_f64(const double* P, const LatDev& L, int t, unsigned long long* out, cudaStream_t s) {
+    if (L.cm) k_maxvel_f64<true><<<grid_of(L), 128, 0, s>>>(P, L, t, out);
+    else k_maxvel_f64<false><<<grid_of(L), 128, 0, s>>>(P, L, t, out);
+    return cudaGetLastError();
+}
+
+}  // namespace life

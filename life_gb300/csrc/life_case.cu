@@ -1,0 +1,504 @@
+// C-ABI implementation: case lifecycle, time stepping and field access.
+//
+// One LifeCase owns its device state on the device that was current when it
+// was created, and one CUDA stream on which every kernel of the case runs in
+// order. The state after step t is kept as P_{t+1} (post-collision
+// populations, structure of arrays) plus the small side buffers the next step
+// reads; see lbm_device.cuh.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/life_gb300.h"
+#include "ibm_kernels.h"
+#include "lbm_kernels.h"
+#include "life_internal.h"
+#include "objects.h"
+
+using namespace life;
+
+namespace {
+thread_local std::string g_err;
+const double PI = 3.14159265358979323846;
+}  // namespace
+
+namespace life {
+int set_error(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+int cuda_fail(cudaError_t e, const char* where) {
+    return set_error(LIFE_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+}  // namespace life
+
+#define CK(call)                                              \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+    } while (0)
+
+extern "C" int life_abi_version(void) { return LIFE_ABI_VERSION; }
+extern "C" const char* life_last_error(void) { return g_err.c_str(); }
+
+static int dev_alloc(LifeCase* c, void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return set_error(e == cudaErrorMemoryAllocation ? LIFE_ERR_NOMEM : LIFE_ERR_CUDA,
+                         std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+    }
+    c->allocs.push_back(*p);
+    c->dev_bytes += bytes;
+    return LIFE_OK;
+}
+
+template <class T>
+static int dev_alloc_t(LifeCase* c, T** p, size_t count) {
+    return dev_alloc(c, (void**)p, sizeof(T) * (count ? count : 1));
+}
+
+// Per-step scalars for absolute steps [t0, t0+n): inlet ramp
+// (GridClass::getRampCoefficient, src/Grid.cpp:548-556) and the Womersley force
+// (src/Grid.cpp:52-62), both with the C library's cos() as in the reference.
+int life::ensure_steps(LifeCase* c, int t0, int n) {
+    if (n > c->steps_cap) {
+        if (c->d_steps) {
+            cudaFree(c->d_steps);
+            for (auto& p : c->allocs)
+                if (p == c->d_steps) p = nullptr;
+        }
+        int cap = n < 1024 ? 1024 : n;
+        if (int rc = dev_alloc_t(c, &c->d_steps, (size_t)cap)) return rc;
+        c->steps_cap = cap;
+    }
+    const LifeCaseParams& p = c->p;
+    std::vector<StepScalars> h(n);
+    for (int k = 0; k < n; k++) {
+        const int t = t0 + k;
+        StepScalars s{};
+        s.ramp = 1.0;
+        if (p.has_inlet_ramp && c->Dt * t <= p.inlet_ramp) s.ramp = (1.0 - std::cos(PI * c->Dt * t / p.inlet_ramp)) / 2.0;
+        if (p.has_womersley) {
+            const double ph = std::cos(2.0 * PI * t * c->Dt /
+                                       ((p.height_p * p.height_p * PI) / (2.0 * (p.womersley * p.womersley) * p.nu_p)));
+            const double sc = (c->Dx * c->Dt) * (c->Dx * c->Dt);
+            s.fx = (0.0 + p.dpdx * ph) * sc / c->Dm;
+            s.fy = (0.0 + p.dpdy * ph) * sc / c->Dm;
+        }
+        h[k] = s;
+    }
+    CK(cudaMemcpyAsync(c->d_steps, h.data(), sizeof(StepScalars) * n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->t_base = t0;
+    c->steps_n = n;
+    return LIFE_OK;
+}
+
+LatDev life::lattice_view(const LifeCase* c, int t) {
+    LatDev L{};
+    L.Nx = c->Nx;
+    L.Ny = c->Ny;
+    L.pitch = c->pitch;
+    L.S = c->S;
+    L.wall[0] = c->p.wall_left;
+    L.wall[1] = c->p.wall_right;
+    L.wall[2] = c->p.wall_bottom;
+    L.wall[3] = c->p.wall_top;
+    L.cm = c->p.central_moments;
+    L.womersley = c->p.has_womersley;
+    L.convective = c->p.wall_right == LIFE_CONVECTIVE;
+    L.has_ibm = c->obj.hasIBM;
+    L.omega = c->p.omega;
+    L.cs = c->cs;
+    L.Fx0 = c->Fx0;
+    L.Fy0 = c->Fy0;
+    L.u0x = c->u0x;
+    L.u0y = c->u0y;
+    L.init_mode = c->init_mode;
+    L.t_base = c->t_base;
+    L.steps = c->d_steps;
+    L.u_in = c->d_u_in;
+    L.rho_in = c->d_rho_in;
+    L.outlet_u = c->d_outlet_u;
+    L.outlet_f_prev = c->d_outlet_f[(t - 1) & 1];
+    L.outlet_f_next = c->d_outlet_f[t & 1];
+    L.delU = c->d_delU;
+    L.force_ibm = c->W.force_ibm;
+    return L;
+}
+
+static int validate(const LifeCaseParams* p) {
+    if (!p) return set_error(LIFE_ERR_INVALID, "params is NULL");
+    if (p->Nx < 4 || p->Ny < 4) return set_error(LIFE_ERR_INVALID, "lattice must be at least 4 x 4 sites");
+    if (p->Ny > 65535) return set_error(LIFE_ERR_INVALID, "Ny above 65535 is not supported");
+    for (int w : {p->wall_left, p->wall_right, p->wall_bottom, p->wall_top})
+        if (w < LIFE_FLUID || w > LIFE_CONVECTIVE) return set_error(LIFE_ERR_INVALID, "unknown wall type");
+    if (p->wall_left == LIFE_CONVECTIVE || p->wall_bottom == LIFE_CONVECTIVE || p->wall_top == LIFE_CONVECTIVE)
+        return set_error(LIFE_ERR_INVALID, "Currently convective BC only supported for right boundary...exiting");
+    if (p->wall_right == LIFE_CONVECTIVE && p->Nx < 4)
+        return set_error(LIFE_ERR_INVALID, "convective outlet needs at least 4 columns");
+    // Pressure walls at y corners keep the previous step's normal velocity in
+    // the reference (u_n[eY] is never reset there); the device state does not
+    // carry that history.
+    for (int yw : {p->wall_bottom, p->wall_top})
+        if (yw == LIFE_PRESSURE && (p->wall_left != LIFE_FLUID || p->wall_right != LIFE_FLUID))
+            return set_error(LIFE_ERR_INVALID,
+                             "pressure boundary on a y wall with non-periodic x walls (corner velocity history) is not "
+                             "supported");
+    if (p->has_womersley && (p->gravityX != 0.0 || p->gravityY != 0.0))
+        return set_error(LIFE_ERR_INVALID, "WOMERSLEY with nonzero gravity is not supported on the GPU path");
+    if (p->precision != LIFE_PREC_F64 && p->precision != LIFE_PREC_F32 && p->precision != LIFE_PREC_F16)
+        return set_error(LIFE_ERR_INVALID, "unknown precision");
+    if (p->omega <= 0.0) return set_error(LIFE_ERR_INVALID, "omega must be positive");
+    return LIFE_OK;
+}
+
+static void free_case(LifeCase* c) {
+    if (!c) return;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (c->device >= 0) cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (void* p : c->allocs)
+        if (p) cudaFree(p);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    if (prev >= 0) cudaSetDevice(prev);
+    delete c;
+}
+
+int upload_markers(LifeCase* c);
+int setup_fem(LifeCase* c);
+int ibm_step(LifeCase* c, int t, const double* A, double* B);
+
+extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc* bodies, int32_t n_bodies,
+                                LifeCase** out) {
+    if (!out) return set_error(LIFE_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (int rc = validate(params)) return rc;
+    if (n_bodies < 0 || (n_bodies > 0 && !bodies)) return set_error(LIFE_ERR_INVALID, "bad body list");
+    LifeCase* c = new LifeCase();
+    c->p = *params;
+    const LifeCaseParams& p = c->p;
+    cudaGetDevice(&c->device);
+    c->Nx = p.Nx;
+    c->Ny = p.Ny;
+    c->pitch = (p.Nx + 31) / 32 * 32;
+    c->S = (long long)c->pitch * p.Ny;
+    // GridClass::GridClass (src/Grid.cpp:1243-1260)
+    const double rho0 = 1.0;
+    c->cs = 1.0 / std::sqrt(3.0);
+    c->tau = 1.0 / p.omega;
+    c->nu = (c->tau - 0.5) * (c->cs * c->cs);
+    c->Dx = p.height_p / (p.Ny - 1);
+    c->Dt = (c->Dx * c->Dx) * c->nu / p.nu_p;
+    c->Dm = (p.rho_p / rho0) * (c->Dx * c->Dx * c->Dx);
+    c->Drho = (p.rho_p / rho0);
+    const double sc = (c->Dx * c->Dt) * (c->Dx * c->Dt);
+    c->Fx0 = (rho0 * c->Drho * p.gravityX + p.dpdx) * sc / c->Dm;
+    c->Fy0 = (rho0 * c->Drho * p.gravityY + p.dpdy) * sc / c->Dm;
+    c->u0x = p.ux0_p * c->Dt / c->Dx;
+    c->u0y = p.uy0_p * c->Dt / c->Dx;
+    c->init_mode = p.has_inlet_ramp ? 0 : (p.profile >= 0 ? 1 : 2);
+    if (p.precision != LIFE_PREC_F64) {
+        delete c;
+        return set_error(LIFE_ERR_INVALID, "only the FP64 form is built into this library version");
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    // Immersed bodies on the host (geometryReadIn + initialiseObjects).
+    Grid0 g{p.Nx, p.Ny, c->Dx, c->Dt, c->Dm, p.gravityX, p.gravityY, p.ref_L, p.alpha, p.delta};
+    c->g0 = g;
+    std::string err;
+    int rc = build_objects(g, p, bodies, n_bodies, c->obj, &err);
+    if (rc) {
+        free_case(c);
+        return set_error(rc, err);
+    }
+    // Inlet profile (src/Grid.cpp:954-996)
+    std::vector<double> u_in((size_t)p.Ny * 2), rho_in(p.Ny, rho0);
+    for (int j = 0; j < p.Ny; j++) {
+        const double Dt = c->Dt, Dx = c->Dx;
+        double ux = 0.0, uy = 0.0;
+        if (p.profile < 0) {
+            ux = p.uxInlet_p * Dt / Dx;
+            uy = p.uyInlet_p * Dt / Dx;
+        } else if (p.profile == LIFE_PROFILE_PARABOLIC) {
+            const double R = p.height_p / 2.0, Y = j * Dx - R;
+            ux = 1.5 * (p.uxInlet_p * Dt / Dx) * (1.0 - (Y / R) * (Y / R));
+            uy = 1.5 * (p.uyInlet_p * Dt / Dx) * (1.0 - (Y / R) * (Y / R));
+        } else if (p.profile == LIFE_PROFILE_SHEAR) {
+            const double H = p.height_p, Y = j * Dx;
+            ux = (p.uxInlet_p * Dt / Dx) * (Y / H);
+            uy = (p.uyInlet_p * Dt / Dx) * (Y / H);
+        } else if (p.profile == LIFE_PROFILE_BOUNDARY_LAYER) {
+            const double H = p.height_p, Y = j * Dx;
+            ux = ((1.5 * p.uxInlet_p * Dt / Dx) / (H * H)) * Y * (2.0 * H - Y);
+            uy = ((1.5 * p.uyInlet_p * Dt / Dx) / (H * H)) * Y * (2.0 * H - Y);
+        }
+        u_in[j * 2] = ux;
+        u_in[j * 2 + 1] = uy;
+    }
+    // Device buffers
+    const size_t plane = (size_t)c->S;
+    if ((rc = dev_alloc_t(c, &c->P[0], plane * 9)) || (rc = dev_alloc_t(c, &c->P[1], plane * 9)) ||
+        (rc = dev_alloc_t(c, &c->d_u_in, (size_t)p.Ny * 2)) || (rc = dev_alloc_t(c, &c->d_rho_in, (size_t)p.Ny)) ||
+        (rc = dev_alloc_t(c, &c->d_outlet_u, (size_t)3 * p.Ny * 2)) ||
+        (rc = dev_alloc_t(c, &c->d_outlet_f[0], (size_t)p.Ny * 3)) ||
+        (rc = dev_alloc_t(c, &c->d_outlet_f[1], (size_t)p.Ny * 3)) ||
+        (rc = dev_alloc_t(c, &c->d_delU, (size_t)p.Ny * 2)) || (rc = dev_alloc_t(c, &c->d_red, 4))) {
+        free_case(c);
+        return rc;
+    }
+    cudaMemcpyAsync(c->d_u_in, u_in.data(), sizeof(double) * u_in.size(), cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(c->d_rho_in, rho_in.data(), sizeof(double) * rho_in.size(), cudaMemcpyHostToDevice, c->stream);
+    cudaMemsetAsync(c->d_delU, 0, sizeof(double) * p.Ny * 2, c->stream);
+    if (c->obj.hasIBM) {
+        if ((rc = upload_markers(c))) {
+            free_case(c);
+            return rc;
+        }
+        if (c->obj.hasFlex && (rc = setup_fem(c))) {
+            free_case(c);
+            return rc;
+        }
+    }
+    c->t = 0;
+    c->t_set = 0;
+    if ((rc = ensure_steps(c, 0, 2))) {
+        free_case(c);
+        return rc;
+    }
+    LatDev L = lattice_view(c, 0);
+    e = launch_init_f64(c->P[0], L, 0, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        free_case(c);
+        return cuda_fail(e, "init");
+    }
+    c->cur = 0;
+    *out = c;
+    return LIFE_OK;
+}
+
+extern "C" int life_case_destroy(LifeCase* c) {
+    free_case(c);
+    return LIFE_OK;
+}
+
+static int check_device_status(LifeCase* c) {
+    if (!c->d_status) return LIFE_OK;
+    int h[4];
+    CK(cudaMemcpyAsync(h, c->d_status, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (h[0] != 0 && c->status_code == 0) {
+        c->status_code = h[0];
+        c->status_t = h[1];
+    }
+    return LIFE_OK;
+}
+
+extern "C" int life_case_step(LifeCase* c, int32_t nsteps) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    if (nsteps < 0) return set_error(LIFE_ERR_INVALID, "negative step count");
+    if (nsteps == 0) return LIFE_OK;
+    if (c->status_code) return set_error(c->status_code, c->status_msg);
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev != c->device) cudaSetDevice(c->device);
+    int rc = ensure_steps(c, c->t, nsteps + 2);
+    if (rc) return rc;
+    const bool conv = c->p.wall_right == LIFE_CONVECTIVE;
+    for (int k = 0; k < nsteps; k++) {
+        const int tt = c->t + 1;
+        LatDev L = lattice_view(c, tt);
+        const double* A = c->P[c->cur];
+        double* B = c->P[c->cur ^ 1];
+        if (conv) {
+            cudaError_t e = launch_outlet_f64(L, c->d_delU, c->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "outlet");
+        }
+        cudaError_t e = launch_step_f64(A, B, L, tt, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "step");
+        if (c->obj.hasIBM) {
+            if ((rc = ibm_step(c, tt, A, B))) return rc;
+        }
+        c->cur ^= 1;
+        c->t = tt;
+    }
+    if (c->obj.hasFlex) {
+        if ((rc = check_device_status(c))) return rc;
+        if (c->status_code) {
+            c->status_msg = "Subiteration scheme hit 20 iterations...exiting";
+            return set_error(c->status_code, c->status_msg);
+        }
+    }
+    if (prev >= 0 && prev != c->device) cudaSetDevice(prev);
+    return LIFE_OK;
+}
+
+extern "C" int life_case_sync(LifeCase* c) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    CK(cudaStreamSynchronize(c->stream));
+    if (int rc = check_device_status(c)) return rc;
+    if (c->status_code) return set_error(c->status_code, c->status_msg);
+    return LIFE_OK;
+}
+
+extern "C" int life_case_info(const LifeCase* c, LifeCaseInfo* info) {
+    if (!c || !info) return set_error(LIFE_ERR_INVALID, "NULL argument");
+    std::memset(info, 0, sizeof *info);
+    info->Nx = c->Nx;
+    info->Ny = c->Ny;
+    info->n_bodies = (int)c->obj.b.size();
+    info->n_markers = (int)c->obj.m.size();
+    info->n_flex = c->obj.nFlex;
+    info->sim_dofs = c->obj.simDOFs;
+    info->precision = c->p.precision;
+    info->t = c->t;
+    info->Dx = c->Dx;
+    info->Dt = c->Dt;
+    info->Dm = c->Dm;
+    info->Drho = c->Drho;
+    info->tau = c->tau;
+    info->nu = c->nu;
+    info->c_s = c->cs;
+    info->device_bytes = c->dev_bytes;
+    return LIFE_OK;
+}
+
+extern "C" int life_case_status(LifeCase* c, LifeStatus* st) {
+    if (!c || !st) return set_error(LIFE_ERR_INVALID, "NULL argument");
+    if (int rc = check_device_status(c)) return rc;
+    std::memset(st, 0, sizeof *st);
+    st->code = c->status_code;
+    st->t = c->status_t;
+    if (c->d_fsi) {
+        FsiScalars h{};
+        CK(cudaMemcpyAsync(&h, c->d_fsi, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        st->last_subits = h.subIt;
+        st->last_subres = h.subRes;
+        st->relax = h.relax;
+        st->last_nr_its = h.lastNR;
+    }
+    return LIFE_OK;
+}
+
+extern "C" int life_case_get_fields(LifeCase* c, double* rho, double* u, double* f, double* force_ibm) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    const size_t n = (size_t)c->Nx * c->Ny;
+    if (c->t == c->t_set && c->host_state) {
+        if (rho) std::memcpy(rho, c->h_rho.data(), n * sizeof(double));
+        if (u) std::memcpy(u, c->h_u.data(), n * 2 * sizeof(double));
+        if (f) std::memcpy(f, c->h_f.data(), n * 9 * sizeof(double));
+        if (force_ibm) std::memcpy(force_ibm, c->h_fibm.data(), n * 2 * sizeof(double));
+        return LIFE_OK;
+    }
+    double *d_rho = nullptr, *d_u = nullptr, *d_f = nullptr, *d_fi = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(d_rho);
+        cudaFree(d_u);
+        cudaFree(d_f);
+        cudaFree(d_fi);
+    };
+    if ((rho && cudaMalloc(&d_rho, n * sizeof(double)) != cudaSuccess) ||
+        (u && cudaMalloc(&d_u, n * 2 * sizeof(double)) != cudaSuccess) ||
+        (f && cudaMalloc(&d_f, n * 9 * sizeof(double)) != cudaSuccess) ||
+        (force_ibm && cudaMalloc(&d_fi, n * 2 * sizeof(double)) != cudaSuccess)) {
+        cleanup();
+        return set_error(LIFE_ERR_NOMEM, "no device memory for the field export");
+    }
+    LatDev L = lattice_view(c, c->t);
+    const bool initial = (c->t == c->t_set);
+    cudaError_t e = launch_export_f64(c->P[c->cur ^ 1], L, c->t, initial, d_rho, d_u, d_f, d_fi, c->stream);
+    if (e == cudaSuccess && rho) e = cudaMemcpyAsync(rho, d_rho, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && u) e = cudaMemcpyAsync(u, d_u, n * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && f) e = cudaMemcpyAsync(f, d_f, n * 9 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && force_ibm)
+        e = cudaMemcpyAsync(force_ibm, d_fi, n * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cleanup();
+    if (e != cudaSuccess) return cuda_fail(e, "get_fields");
+    return LIFE_OK;
+}
+
+extern "C" int life_case_set_fields(LifeCase* c, int32_t t, const double* rho, const double* u, const double* f,
+                                    const double* force_ibm) {
+    if (!c || !rho || !u || !f) return set_error(LIFE_ERR_INVALID, "NULL argument");
+    const size_t n = (size_t)c->Nx * c->Ny;
+    c->h_rho.assign(rho, rho + n);
+    c->h_u.assign(u, u + 2 * n);
+    c->h_f.assign(f, f + 9 * n);
+    if (force_ibm) c->h_fibm.assign(force_ibm, force_ibm + 2 * n);
+    else c->h_fibm.assign(2 * n, 0.0);
+    c->host_state = true;
+    double *d_rho = nullptr, *d_u = nullptr, *d_f = nullptr, *d_fi = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(d_rho);
+        cudaFree(d_u);
+        cudaFree(d_f);
+        cudaFree(d_fi);
+    };
+    if (cudaMalloc(&d_rho, n * 8) != cudaSuccess || cudaMalloc(&d_u, n * 16) != cudaSuccess ||
+        cudaMalloc(&d_f, n * 72) != cudaSuccess || cudaMalloc(&d_fi, n * 16) != cudaSuccess) {
+        cleanup();
+        return set_error(LIFE_ERR_NOMEM, "no device memory for the field import");
+    }
+    cudaMemcpyAsync(d_rho, c->h_rho.data(), n * 8, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(d_u, c->h_u.data(), n * 16, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(d_f, c->h_f.data(), n * 72, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(d_fi, c->h_fibm.data(), n * 16, cudaMemcpyHostToDevice, c->stream);
+    c->t = t;
+    c->t_set = t;
+    int rc = ensure_steps(c, t, 2);
+    if (rc) {
+        cleanup();
+        return rc;
+    }
+    LatDev L = lattice_view(c, t);
+    cudaError_t e = launch_state_f64(c->P[0], L, t, d_rho, d_u, d_f, d_fi, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cleanup();
+    if (e != cudaSuccess) return cuda_fail(e, "set_fields");
+    c->cur = 0;
+    return LIFE_OK;
+}
+
+extern "C" int life_case_max_velocity(LifeCase* c, double* max_vel, int32_t* has_nan) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    unsigned long long h[2] = {0, 0};
+    CK(cudaMemsetAsync(c->d_red, 0, 2 * sizeof(unsigned long long), c->stream));
+    LatDev L = lattice_view(c, c->t);
+    if (c->t == c->t_set) {
+        // Before the first step the state is the initial (or restart) one:
+        // export it and reduce on the host side of this call.
+        std::vector<double> u((size_t)c->Nx * c->Ny * 2);
+        if (int rc = life_case_get_fields(c, nullptr, u.data(), nullptr, nullptr)) return rc;
+        double m = 0.0;
+        int nan = 0;
+        for (size_t k = 0; k < u.size() / 2; k++) {
+            double v = std::sqrt(u[2 * k] * u[2 * k] + u[2 * k + 1] * u[2 * k + 1]);
+            if (v != v) nan = 1;
+            else if (v > m) m = v;
+        }
+        if (max_vel) *max_vel = m;
+        if (has_nan) *has_nan = nan;
+        return LIFE_OK;
+    }
+    CK(launch_maxvel_f64(c->P[c->cur ^ 1], L, c->t, c->d_red, c->stream));
+    CK(cudaMemcpyAsync(h, c->d_red, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    double m;
+    std::memcpy(&m, &h[0], sizeof m);
+    if (max_vel) *max_vel = m;
+    if (has_nan) *has_nan = h[1] ? 1 : 0;
+    return LIFE_OK;
+}

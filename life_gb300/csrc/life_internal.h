@@ -1,0 +1,72 @@
+// Internal state of a LifeCase (host side of the C-ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/life_gb300.h"
+#include "ibm_kernels.h"
+#include "life_types.h"
+#include "objects.h"
+
+namespace life {
+
+// FSI loop scalars kept on the device (ObjectsClass members subIt, relax,
+// subRes, subNum, subDen; reference inc/Objects.h:66-71).
+struct FsiScalars {
+    int subIt;
+    int lastNR;
+    int pad[2];
+    double relax, subRes, subNum, subDen;
+};
+
+struct FemDev;  // fem_kernels.h
+
+int set_error(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* where);
+
+}  // namespace life
+
+struct LifeCase {
+    LifeCaseParams p{};
+    int device = -1;
+    int Nx = 0, Ny = 0, pitch = 0;
+    long long S = 0;
+    double Dx = 0, Dt = 0, Dm = 0, Drho = 0, tau = 0, nu = 0, cs = 0;
+    double Fx0 = 0, Fy0 = 0, u0x = 0, u0y = 0;
+    int init_mode = 0;
+    int t = 0;        // time step of the current state
+    int t_set = 0;    // time step at which the state was created or loaded
+    bool host_state = false;  // state loaded from host arrays (kept for export)
+    std::vector<double> h_rho, h_u, h_f, h_fibm;
+    // device lattice state
+    double* P[2] = {nullptr, nullptr};
+    int cur = 0;      // P[cur] holds P_{t+1}
+    double* d_u_in = nullptr;
+    double* d_rho_in = nullptr;
+    life::StepScalars* d_steps = nullptr;
+    int steps_cap = 0, steps_n = 0, t_base = 0;
+    double* d_outlet_u = nullptr;
+    double* d_outlet_f[2] = {nullptr, nullptr};
+    double* d_delU = nullptr;
+    unsigned long long* d_red = nullptr;
+    cudaStream_t stream = nullptr;
+    size_t dev_bytes = 0;
+    std::vector<void*> allocs;
+    // immersed bodies
+    life::Grid0 g0{};
+    life::HObjects obj;
+    life::MarkerDev M{};
+    life::IbmScratch W{};
+    life::FemDev* fem = nullptr;
+    life::FsiScalars* d_fsi = nullptr;
+    int* d_status = nullptr;  // [code, t, ...]
+    int status_code = 0, status_t = 0;
+    std::string status_msg;
+};
+
+namespace life {
+LatDev lattice_view(const LifeCase* c, int t);
+int ensure_steps(LifeCase* c, int t0, int n);
+}  // namespace life

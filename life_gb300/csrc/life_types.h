@@ -1,0 +1,48 @@
+// Plain structs shared by host and device code of the GB300 LIFE library.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/life_gb300.h"
+
+namespace life {
+
+// Per-time-step scalars computed on the host with the C library's cos()
+// (so they equal the reference's values bit for bit): the inlet ramp
+// coefficient used by step t's boundary conditions (GridClass::getRampCoefficient,
+// reference src/Grid.cpp:548-556) and step t's uniform Womersley force
+// (src/Grid.cpp:52-62).
+struct StepScalars {
+    double ramp;
+    double fx, fy;
+    double pad;
+};
+
+// Everything a lattice kernel needs, passed by value.
+struct LatDev {
+    int Nx, Ny, pitch;
+    int wall[4];          // left, right, bottom, top (LIFE_* lattice types)
+    long long S;          // sites per population plane (pitch * Ny)
+    int cm;               // central moments collision
+    int womersley;        // force_xy(t) from steps[]; else the constant Fx0/Fy0
+    int convective;       // right wall is a convective outlet
+    int has_ibm;
+    double omega, cs;
+    double Fx0, Fy0;      // constant force_xy (reference src/Grid.cpp:1035-1045)
+    double u0x, u0y;      // initial uniform velocity (ux0_p*Dt/Dx, uy0_p*Dt/Dx)
+    int init_mode;        // 0: zero velocity (ramp), 1: inlet profile, 2: uniform u0
+    int t_base;           // steps[t - t_base]
+    const StepScalars* steps;
+    const double* u_in;   // [Ny][2] inlet profile
+    const double* rho_in; // [Ny]
+    // Convective outlet side state (reference GridClass::convectiveSpeed,
+    // src/Grid.cpp:477-495, reads u of the previous step at the last three
+    // columns; convectiveBC reads f_n[2,6,8] at the outlet column).
+    double* outlet_u;           // [3][Ny][2] final u of columns Nx-3, Nx-2, Nx-1
+    const double* outlet_f_prev;// [Ny][3] post-BC f[2,6,8] at Nx-1 of the previous step
+    double* outlet_f_next;      // [Ny][3] written by the current step
+    const double* delU;         // [Ny][2] convective speed term of the current step
+    const double* force_ibm;    // [2][S] dense IBM force of the current step, or null
+};
+
+}  // namespace life

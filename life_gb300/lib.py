@@ -1,0 +1,206 @@
+"""Python handle on the C-ABI (``liblife_gb300.so``).
+
+:class:`Case` mirrors how the reference's ``main()`` drives a run
+(reference ``src/main.cpp:42-86``): construct it from a ``params.h`` value set
+and the geometry (``GridClass()`` + ``ObjectsClass(grid)``), advance it with
+:meth:`Case.step` (``grid.solver()`` per step) and read the restart-format
+fields, markers and FEM state back. Every call goes through the exported C
+functions; there is no Python or CPU compute path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+
+from .abi import ERRORS, LifeCaseInfo, LifeStatus, body_structs, params_struct
+from .case import CaseParams
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "liblife_gb300.so")
+_lib: Optional[C.CDLL] = None
+_lock = threading.Lock()
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+# Every function the header declares, with its ctypes signature.
+SIGNATURES = {
+    "life_abi_version": (C.c_int, []),
+    "life_last_error": (C.c_char_p, []),
+    "life_case_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "life_case_destroy": (C.c_int, [C.c_void_p]),
+    "life_case_step": (C.c_int, [C.c_void_p, C.c_int32]),
+    "life_case_sync": (C.c_int, [C.c_void_p]),
+    "life_case_info": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "life_case_status": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "life_case_get_fields": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp]),
+    "life_case_set_fields": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp]),
+    "life_case_get_markers": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _ip]),
+    "life_case_get_bodies": (C.c_int, [C.c_void_p, _ip, _ip, _ip, _ip]),
+    "life_case_get_fem": (C.c_int, [C.c_void_p, C.c_int32] + [_dp] * 10),
+    "life_case_get_relax": (C.c_int, [C.c_void_p, _dp]),
+    "life_case_max_velocity": (C.c_int, [C.c_void_p, _dp, _ip]),
+    "life_case_total_force": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "life_parse_geometry": (C.c_int, [C.c_char_p, C.c_void_p, C.c_int32, _ip]),
+}
+
+
+class LifeError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib() -> C.CDLL:
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(f"{LIB_PATH} is missing: run `python -m life_gb300.build` "
+                                   "(the GPU path has no fallback)")
+            L = C.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc:
+        raise LifeError(rc, lib().life_last_error().decode())
+
+
+def _p(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    if a.dtype == np.float64:
+        return a.ctypes.data_as(_dp)
+    return a.ctypes.data_as(_ip)
+
+
+class Case:
+    """A LIFE case running on the GPU through the C-ABI."""
+
+    def __init__(self, params: CaseParams, bodies: Sequence = ()):
+        L = lib()
+        self.params = params
+        ps = params_struct(params)
+        bs = body_structs(bodies)
+        h = C.c_void_p()
+        _check(L.life_case_create(C.byref(ps), C.byref(bs), len(bodies), C.byref(h)))
+        self._h = h
+        info = self.info()
+        self.n_markers, self.n_bodies, self.n_flex = info.n_markers, info.n_bodies, info.n_flex
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().life_case_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def info(self) -> LifeCaseInfo:
+        inf = LifeCaseInfo()
+        _check(lib().life_case_info(self._h, C.byref(inf)))
+        return inf
+
+    def status(self) -> LifeStatus:
+        st = LifeStatus()
+        _check(lib().life_case_status(self._h, C.byref(st)))
+        return st
+
+    @property
+    def t(self) -> int:
+        return self.info().t
+
+    def step(self, n: int = 1) -> None:
+        _check(lib().life_case_step(self._h, int(n)))
+
+    def sync(self) -> None:
+        _check(lib().life_case_sync(self._h))
+
+    def fields(self, which=("rho", "u", "f", "force_ibm")) -> Dict[str, np.ndarray]:
+        n = self.params.Nx * self.params.Ny
+        out = {}
+        rho = np.empty(n) if "rho" in which else None
+        u = np.empty((n, 2)) if "u" in which else None
+        f = np.empty((n, 9)) if "f" in which else None
+        fi = np.empty((n, 2)) if "force_ibm" in which else None
+        _check(lib().life_case_get_fields(self._h, _p(rho), _p(u), _p(f), _p(fi)))
+        for k, v in (("rho", rho), ("u", u), ("f", f), ("force_ibm", fi)):
+            if v is not None:
+                out[k] = v
+        return out
+
+    def set_fields(self, t: int, rho, u, f, force_ibm=None) -> None:
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (rho, u, f)]
+        fi = None if force_ibm is None else np.ascontiguousarray(force_ibm, dtype=np.float64)
+        _check(lib().life_case_set_fields(self._h, int(t), *[_p(a) for a in arrs], _p(fi)))
+
+    def markers(self) -> Dict[str, np.ndarray]:
+        n = self.n_markers
+        pos, vel, force = np.empty((n, 2)), np.empty((n, 2)), np.empty((n, 2))
+        eps, ds = np.empty(n), np.empty(n)
+        body = np.empty(n, dtype=np.int32)
+        _check(lib().life_case_get_markers(self._h, _p(pos), _p(vel), _p(force), _p(eps), _p(ds), _p(body)))
+        return dict(pos=pos, vel=vel, force=force, epsilon=eps, ds=ds, body=body)
+
+    def bodies(self) -> Dict[str, np.ndarray]:
+        nb = self.n_bodies
+        out = {k: np.empty(nb, dtype=np.int32) for k in ("ids", "flexible", "n_markers", "n_fem_nodes")}
+        _check(lib().life_case_get_bodies(self._h, *[_p(out[k]) for k in
+                                                     ("ids", "flexible", "n_markers", "n_fem_nodes")]))
+        return out
+
+    def fem(self, k: int) -> Dict[str, np.ndarray]:
+        b = self.bodies()
+        nn = int(b["n_fem_nodes"][np.flatnonzero(b["flexible"])[k]])
+        dofs = 3 * nn
+        keys = ("U", "Udot", "Udotdot", "U_n", "U_nm1", "R_k")
+        out = {key: np.empty(dofs) for key in keys}
+        out["el_L"], out["el_angle"] = np.empty(nn - 1), np.empty(nn - 1)
+        out["pos"], out["angle"] = np.empty((nn, 2)), np.empty(nn)
+        _check(lib().life_case_get_fem(self._h, k, *[_p(out[key]) for key in keys], _p(out["el_L"]),
+                                       _p(out["el_angle"]), _p(out["pos"]), _p(out["angle"])))
+        return out
+
+    def relax(self) -> float:
+        r = C.c_double()
+        _check(lib().life_case_get_relax(self._h, C.byref(r)))
+        return r.value
+
+    def max_velocity(self):
+        m, nan = C.c_double(), C.c_int32()
+        _check(lib().life_case_max_velocity(self._h, C.byref(m), C.byref(nan)))
+        return m.value, bool(nan.value)
+
+    def total_force(self):
+        fx, fy = C.c_double(), C.c_double()
+        _check(lib().life_case_total_force(self._h, C.byref(fx), C.byref(fy)))
+        return fx.value, fy.value
+
+
+def parse_geometry(text: str):
+    from .abi import LifeBodyDesc
+    n = C.c_int32()
+    _check(lib().life_parse_geometry(text.encode(), None, 0, C.byref(n)))
+    arr = (LifeBodyDesc * max(1, n.value))()
+    _check(lib().life_parse_geometry(text.encode(), C.byref(arr), n.value, C.byref(n)))
+    return [arr[k] for k in range(n.value)]
