@@ -1,0 +1,329 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 LIFE hot path (D2Q9 stream-collide + boundary conditions).
+
+Workload: the lid-driven cavity of the reference's plain-method configuration
+(regularised velocity lid u = 0.1, regularised no-slip walls, BGK, tau = 0.5768)
+scaled to a 4096 x 4096 lattice, the size the headline roofline target is
+quoted on. One "step" is one time step of the whole lattice. The headline form
+is the FP32 shifted-population storage; FP64 (bit-exact with the reference)
+and FP16 storage are measured beside it, with their velocity error against the
+FP64 run after the same steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Each rank runs an independent replica (the reference has no domain
+decomposition and the path is timed replicas-only); `value` is the sum over
+ranks. Timing: W untimed steps, then K steps bracketed by a barrier and a
+device synchronise, measured with CUDA events on the case's stream. The lattice
+state (2 x 9 x 4 B x 16.8M sites = 1.2 GB) is far larger than L2, so no flush
+is needed between steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MLUPS"
+WORKLOAD = "lid_driven_cavity_4096x4096_d2q9_bgk"
+
+
+def cavity_params(n: int, precision: int, cm: bool = False):
+    from life_gb300.case import VELOCITY, WALL, CaseParams
+    omega = 1.0 / 0.5768
+    cs = 1.0 / (3.0 ** 0.5)
+    nu = (1.0 / omega - 0.5) * (cs * cs)
+    return CaseParams(Nx=n, Ny=n, height_p=float(n - 1), rho_p=1.0, nu_p=nu, omega=omega,
+                      wall_left=WALL, wall_right=WALL, wall_bottom=WALL, wall_top=VELOCITY,
+                      uxInlet_p=0.1, central_moments=cm, precision=precision, ref_L=float(n - 1))
+
+
+def cylinder_params(precision: int):
+    """Rigid cylinder channel: 1000 x 400, central moments, D = 40, inlet 0.04,
+    convective outlet, Re = 100 (tau = 0.548)."""
+    from life_gb300.case import CONVECTIVE, VELOCITY, WALL, CaseParams, Circle
+    omega = 1.0 / 0.548
+    cs = 1.0 / (3.0 ** 0.5)
+    nu = (1.0 / omega - 0.5) * (cs * cs)
+    p = CaseParams(Nx=1000, Ny=400, height_p=399.0, rho_p=1.0, nu_p=nu, omega=omega,
+                   wall_left=VELOCITY, wall_right=CONVECTIVE, wall_bottom=WALL, wall_top=WALL,
+                   uxInlet_p=0.04, central_moments=True, precision=precision, ref_L=40.0)
+    return p, [Circle(x=200.0, y=200.0, radius=20.0)]
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        if vis:
+            ids = [x.strip() for x in vis.split(",") if x.strip()]
+            if device < len(ids) and ids[device].isdigit():
+                device = int(ids[device])
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except Exception:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        smax = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_oracle_mlups(params, steps: int, warmup: int):
+    """The oracle (C restatement of the reference, OpenMP over all host
+    cores) timed on the same lattice."""
+    from oracle.pyoracle import Oracle
+    o = Oracle(params)
+    o.step(warmup)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return params.Nx * params.Ny * steps / dt / 1e6, dt
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    from life_gb300.case import PREC_F64
+    n = args.nx
+    p = cavity_params(n, PREC_F64)
+    mlups, dt = cpu_oracle_mlups(p, args.steps, args.warmup)
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(mlups, 3), "unit": "MLUPS",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(dt * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic initial state)",
+        "config": {"workload": f"lid_driven_cavity_{n}x{n}_d2q9_bgk", "lattice": [n, n], "collision": "BGK",
+                   "l2": "state larger than L2"},
+        "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full steps of the {n}x{n} lattice after {args.warmup} warm-up"},
+        "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, world, rank, local):
+    import numpy as np
+    from life_gb300.build import build
+    from life_gb300.case import PREC_F16, PREC_F32, PREC_F64
+    build()
+    from life_gb300.lib import Case
+    n = args.nx
+    sites = n * n
+    hbm, hbm_kind = peaks()
+
+    # ---- headline: FP32 shifted populations
+    c32 = Case(cavity_params(n, PREC_F32))
+    c32.step(args.warmup)
+    c32.sync()
+    barrier(world)
+    with ClockSampler(local) as clk:
+        tot_ms, inner_ms, launches = c32.bench_steps(args.steps)
+    barrier(world)
+    tot_ms = max_over_ranks(world, tot_ms)
+    clocks = clk.summary()
+    ms_step = tot_ms / args.steps
+    value = world * sites * args.steps / (tot_ms * 1e-3) / 1e6
+    bytes_per_site = 18 * 4
+    achieved = bytes_per_site * sites / (inner_ms * 1e-3) / 1e9
+
+    extras = {}
+    if not args.quick:
+        # ---- FP64 (reference-exact) and FP16 storage on the same lattice
+        k2 = max(10, args.steps // 2)
+        c64 = Case(cavity_params(n, PREC_F64))
+        c64.step(args.warmup)
+        t64, i64, _ = c64.bench_steps(k2)
+        extras["fp64_mlups"] = round(sites * k2 / (t64 * 1e-3) / 1e6, 1)
+        extras["fp64_interior_gbs"] = round(144 * sites / (i64 * 1e-3) / 1e9, 1)
+        c16 = Case(cavity_params(n, PREC_F16))
+        c16.step(args.warmup)
+        t16, i16, _ = c16.bench_steps(k2)
+        extras["fp16_mlups"] = round(sites * k2 / (t16 * 1e-3) / 1e6, 1)
+        extras["fp16_interior_gbs"] = round(36 * sites / (i16 * 1e-3) / 1e9, 1)
+        extras["fp32_over_fp64"] = round(value / world / extras["fp64_mlups"], 3)
+        # velocity error after the same number of steps (FP64 GPU = reference bits)
+        done = args.warmup + args.steps
+        c64.step(done - c64.t)
+        c16.step(done - c16.t)
+        u64 = c64.fields(("u",))["u"]
+        umax = np.abs(u64).max()
+        for name, c in (("fp32", c32), ("fp16", c16)):
+            u = c.fields(("u",))["u"]
+            extras[f"{name}_velocity_rel_err"] = float(np.abs(u - u64).max() / umax)
+        extras["error_after_steps"] = done
+        del c64, c16, u64
+        # ---- rigid cylinder channel (1000 x 400, CM, IBM), FP64 and FP32
+        for prec, tag in ((PREC_F64, "fp64"), (PREC_F32, "fp32")):
+            p, b = cylinder_params(prec)
+            cc = Case(p, b)
+            cc.step(args.warmup)
+            tt, _, _ = cc.bench_steps(200)
+            extras[f"cylinder_1000x400_cm_{tag}_mlups"] = round(1000 * 400 * 200 / (tt * 1e-3) / 1e6, 1)
+            del cc
+
+    # ---- end to end through the C-ABI: create from params (host), K steps,
+    # read the velocity field back to host memory
+    t0 = time.perf_counter()
+    ce = Case(cavity_params(n, PREC_F32))
+    ce.step(args.steps)
+    u = ce.fields(("u",))["u"]
+    e2e_s = time.perf_counter() - t0
+    e2e = world * sites * args.steps / e2e_s / 1e6
+    h2d = 376 + 16 * n + 32 * (args.steps + 2)  # params struct, inlet profile, step scalars
+    d2h = u.nbytes
+    del ce, u
+
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            tr = json.load(fh)
+        traffic = round(float(tr["dram_bytes_per_site"]) * sites)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.quick:
+        cp = cavity_params(n, PREC_F64)
+        mlups, dt = cpu_oracle_mlups(cp, 2, 1)
+        cpu = {"value": round(mlups, 3), "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"2 full steps of the {n}x{n} FP64 lattice after 1 warm-up ({dt:.1f} s)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (analytic initial state of the cavity)",
+            "config": {"workload": f"lid_driven_cavity_{n}x{n}_d2q9_bgk", "lattice": [n, n], "collision": "BGK",
+                       "storage": "fp32 shifted populations (f - w)", "lid_velocity": 0.1, "tau": 0.5768,
+                       "parallelism": f"replicas{world}", "l2": "state 1.2 GB > L2 (no flush needed)"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(achieved / hbm, 4), "traffic": traffic,
+                         "peak_source": f"{hbm_kind} hbm_gbs", "kernel": "k_interior_lowp<BGK,F32>",
+                         "algorithmic_bytes_per_site": bytes_per_site, "kernel_ms": round(inner_ms, 4)},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e, 1), "unit": "MLUPS", "h2d_bytes_per_step": round(h2d / args.steps),
+                    "d2h_bytes_per_step": round(d2h / args.steps),
+                    "what": "create from params + K steps + velocity field to host, wall clock"},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "extras": extras,
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nx", type=int, default=4096)
+    ap.add_argument("--quick", action="store_true", help="headline measurement only")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, world, rank)
+        return run_gb300(args, world, rank, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -185,6 +185,14 @@ int life_case_get_relax(LifeCase* c, double* relax);
 int life_case_max_velocity(LifeCase* c, double* max_vel, int32_t* has_nan);
 int life_case_total_force(LifeCase* c, double* fx, double* fy);
 
+/* Measurement hook (no counterpart in the reference, which only prints an
+ * MLUPS figure from wall-clock time, src/Grid.cpp:594-610): runs nsteps steps
+ * like life_case_step and returns the device time of the whole range and the
+ * mean device time of the interior lattice kernel, both from CUDA events
+ * recorded on the case's stream, and the number of kernels launched. */
+int life_case_bench_steps(LifeCase* c, int32_t nsteps, double* total_ms, double* interior_ms,
+                          int32_t* launches);
+
 /* Parses geometry.config text with the reference's rules (leading '#' lines
  * skipped, whitespace tokens; src/Objects.cpp:338-458). Writes at most cap
  * descriptors, returns the number found in *n. */

@@ -7,7 +7,7 @@ int setup_fem(LifeCase* c) {
     return set_error(LIFE_ERR_INVALID, "flexible bodies are not built into this library version");
 }
 
-int fem_fsi_loop(LifeCase* c, int t, const double* A, const LatDev& L) {
+int fem_fsi_loop(LifeCase* c, int t, const void* A, const LatDev& L) {
     (void)c; (void)t; (void)A; (void)L;
     return set_error(LIFE_ERR_INVALID, "flexible bodies are not built into this library version");
 }

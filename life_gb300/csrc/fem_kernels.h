@@ -12,4 +12,4 @@ struct FemDev {
 }  // namespace life
 
 int setup_fem(LifeCase* c);
-int fem_fsi_loop(LifeCase* c, int t, const double* A, const life::LatDev& L);
+int fem_fsi_loop(LifeCase* c, int t, const void* A, const life::LatDev& L);

@@ -23,8 +23,8 @@ namespace life {
 
 constexpr int TILE = 16;
 
-template <bool CM>
-__global__ void k_ibm_interp(const double* __restrict__ P, LatDev L, int t, MarkerDev M, double velScale) {
+template <bool CM, class S>
+__global__ void k_ibm_interp(const typename S::T* __restrict__ P, LatDev L, int t, MarkerDev M, double velScale) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= M.n) return;
     double iRho = 0.0, iMx = 0.0, iMy = 0.0;
@@ -34,7 +34,7 @@ __global__ void k_ibm_interp(const double* __restrict__ P, LatDev L, int t, Mark
         const int i = M.si[k * 9 + s], j = M.sj[k * 9 + s];
         const double d = M.sd[k * 9 + s];
         double f[9], rho, ux, uy;
-        site_state<CM>(P, L, t, i, j, f, rho, ux, uy);
+        site_state<CM, S>(P, L, t, i, j, f, rho, ux, uy);
         iRho += rho * d * 1.0 * 1.0;
         iMx += rho * ux * d * 1.0 * 1.0;
         iMy += rho * uy * d * 1.0 * 1.0;
@@ -70,9 +70,9 @@ __global__ void k_ibm_mark(MarkerDev M, IbmScratch W) {
     }
 }
 
-template <bool CM>
-__global__ void __launch_bounds__(256) k_ibm_spread(const double* __restrict__ A, double* __restrict__ B, LatDev L,
-                                                    int t, MarkerDev M, IbmScratch W) {
+template <bool CM, class S>
+__global__ void __launch_bounds__(256) k_ibm_spread(const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
+                                                    LatDev L, int t, MarkerDev M, IbmScratch W) {
     __shared__ int list[256];
     __shared__ int warp_cnt[8];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) k_ibm_spread(const double* __restrict__ A
             W.force_ibm[L.S + s] = ay;
             W.sites[atomicAdd(W.nsites, 1)] = s;
             double f[9], rho, ux, uy, Fx, Fy;
-            site_state<CM>(A, L, t, i, j, f, rho, ux, uy);
+            site_state<CM, S>(A, L, t, i, j, f, rho, ux, uy);
             force_xy_at(L, t, Fx, Fy);
             macroscopic_ibm(f, Fx, Fy, ax, ay, rho, ux, uy);
             if (L.convective && i >= L.Nx - 3) {
@@ -135,31 +135,53 @@ __global__ void __launch_bounds__(256) k_ibm_spread(const double* __restrict__ A
             force_xy_at(L, t + 1, Gx, Gy);
             collide<CM>(f, rho, ux, uy, Gx + ax, Gy + ay, L.omega, L.cs, fs);
 #pragma unroll
-            for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = fs[v];
+            for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = S::save(fs[v], v);
         }
     }
 }
 
 // ------------------------------------------------------------ launchers
+#define IBM_DISPATCH(KERNEL, GRID, BLOCK, ...)                                                             \
+    do {                                                                                                   \
+        if (L.prec == LIFE_PREC_F64) {                                                                     \
+            if (L.cm) KERNEL<true, StoreF64><<<GRID, BLOCK, 0, s>>>(__VA_ARGS__);                          \
+            else KERNEL<false, StoreF64><<<GRID, BLOCK, 0, s>>>(__VA_ARGS__);                              \
+        } else if (L.prec == LIFE_PREC_F32) {                                                              \
+            if (L.cm) KERNEL<true, StoreF32><<<GRID, BLOCK, 0, s>>>(__VA_ARGS__);                          \
+            else KERNEL<false, StoreF32><<<GRID, BLOCK, 0, s>>>(__VA_ARGS__);                              \
+        } else {                                                                                           \
+            if (L.cm) KERNEL<true, StoreF16><<<GRID, BLOCK, 0, s>>>(__VA_ARGS__);                          \
+            else KERNEL<false, StoreF16><<<GRID, BLOCK, 0, s>>>(__VA_ARGS__);                              \
+        }                                                                                                  \
+    } while (0)
 
-cudaError_t launch_ibm_interp(const double* P, const LatDev& L, int t, const MarkerDev& M, double velScale,
+template <class T>
+struct TypedPtr {
+    const void* p;
+    template <class U>
+    operator const U*() const { return (const U*)p; }
+    template <class U>
+    operator U*() const { return (U*)const_cast<void*>(p); }
+};
+
+cudaError_t launch_ibm_interp(const void* P, const LatDev& L, int t, const MarkerDev& M, double velScale,
                               cudaStream_t s) {
     if (M.n == 0) return cudaSuccess;
     const int nb = (M.n + 127) / 128;
-    if (L.cm) k_ibm_interp<true><<<nb, 128, 0, s>>>(P, L, t, M, velScale);
-    else k_ibm_interp<false><<<nb, 128, 0, s>>>(P, L, t, M, velScale);
+    TypedPtr<void> Pp{P};
+    IBM_DISPATCH(k_ibm_interp, nb, 128, Pp, L, t, M, velScale);
     return cudaGetLastError();
 }
 
-cudaError_t launch_ibm_spread(const double* A, double* B, const LatDev& L, int t, const MarkerDev& M,
+cudaError_t launch_ibm_spread(const void* A, void* B, const LatDev& L, int t, const MarkerDev& M,
                               const IbmScratch& W, cudaStream_t s) {
     k_ibm_clear<<<8, 256, 0, s>>>(W, L);
     if (M.n > 0) {
         k_ibm_mark<<<(M.n + 127) / 128, 128, 0, s>>>(M, W);
         int grid = W.max_tiles < 4 * 152 ? W.max_tiles : 4 * 152;
         if (grid < 1) grid = 1;
-        if (L.cm) k_ibm_spread<true><<<grid, 256, 0, s>>>(A, B, L, t, M, W);
-        else k_ibm_spread<false><<<grid, 256, 0, s>>>(A, B, L, t, M, W);
+        TypedPtr<void> Ap{A}, Bp{B};
+        IBM_DISPATCH(k_ibm_spread, grid, 256, Ap, Bp, L, t, M, W);
     }
     return cudaGetLastError();
 }

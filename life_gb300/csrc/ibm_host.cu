@@ -108,7 +108,7 @@ int upload_markers(LifeCase* c) {
 }
 
 // One step of ObjectsClass::objectKernel on the device.
-int ibm_step(LifeCase* c, int t, const double* A, double* B) {
+int ibm_step(LifeCase* c, int t, const void* A, void* B) {
     LatDev L = lattice_view(c, t);
     cudaError_t e;
     if (c->obj.hasFlex) {
@@ -117,9 +117,11 @@ int ibm_step(LifeCase* c, int t, const double* A, double* B) {
     } else {
         e = launch_ibm_interp(A, L, t, c->M, c->Dt / c->Dx, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "ibm_interp");
+        c->ibm_launches += 1;
     }
     e = launch_ibm_spread(A, B, L, t, c->M, c->W, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "ibm_spread");
+    c->ibm_launches += 3;
     std::swap(c->W.sites, c->W.sites_prev);
     std::swap(c->W.nsites, c->W.nsites_prev);
     return LIFE_OK;

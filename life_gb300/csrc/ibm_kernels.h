@@ -35,9 +35,10 @@ struct IbmScratch {
     int ntx, nty, max_tiles;
 };
 
-cudaError_t launch_ibm_interp(const double* P, const LatDev& L, int t, const MarkerDev& M, double velScale,
+// Population buffers are untyped; their element type follows L.prec.
+cudaError_t launch_ibm_interp(const void* P, const LatDev& L, int t, const MarkerDev& M, double velScale,
                               cudaStream_t s);
-cudaError_t launch_ibm_spread(const double* A, double* B, const LatDev& L, int t, const MarkerDev& M,
+cudaError_t launch_ibm_spread(const void* A, void* B, const LatDev& L, int t, const MarkerDev& M,
                               const IbmScratch& W, cudaStream_t s);
 
 }  // namespace life

@@ -16,6 +16,8 @@
 // FP64 translation units are compiled with --fmad=false and keep the
 // reference's operation order, so a + b*c is rounded twice as g++ does on x86.
 #pragma once
+#include <cuda_fp16.h>
+
 #include <cstdint>
 
 #include "life_types.h"
@@ -33,6 +35,44 @@ __device__ __forceinline__ double wgt(int v) {
 
 #define LSQ(x) ((x) * (x))
 #define LQU(x) ((x) * (x) * (x) * (x))
+
+// Storage forms of the populations. load() returns f_v in FP64, save()
+// stores an FP64 f_v back.
+//   F64: f_v itself (the plain form).
+//   F32: the shifted deviation g_v = f_v - w_v (rest density 1), so the
+//        stored bits resolve the small departure from rest, not w_v.
+//   F16: g_v / s_v with a per-direction power-of-two scale s_v close to w_v
+//        (1/2, 1/8, 1/32), so scaling adds no rounding of its own.
+__device__ __forceinline__ float h16_scale(int v) { return v == 0 ? 0.5f : (v < 5 ? 0.125f : 0.03125f); }
+__device__ __forceinline__ float h16_inv(int v) { return v == 0 ? 2.0f : (v < 5 ? 8.0f : 32.0f); }
+__device__ __forceinline__ float wgt_f(int v) { return v == 0 ? 4.0f / 9.0f : (v < 5 ? 1.0f / 9.0f : 1.0f / 36.0f); }
+
+struct StoreF64 {
+    using T = double;
+    static constexpr int prec = LIFE_PREC_F64;
+    __device__ static __forceinline__ double load(T x, int) { return x; }
+    __device__ static __forceinline__ T save(double f, int) { return f; }
+};
+struct StoreF32 {
+    using T = float;
+    static constexpr int prec = LIFE_PREC_F32;
+    __device__ static __forceinline__ double load(T x, int v) { return (double)x + wgt(v); }
+    __device__ static __forceinline__ T save(double f, int v) { return (float)(f - wgt(v)); }
+    __device__ static __forceinline__ float dev(T x, int) { return x; }      // g_v
+    __device__ static __forceinline__ T put(float g, int) { return g; }
+};
+struct StoreF16 {
+    using T = __half;
+    static constexpr int prec = LIFE_PREC_F16;
+    __device__ static __forceinline__ double load(T x, int v) {
+        return (double)(__half2float(x) * h16_scale(v)) + wgt(v);
+    }
+    __device__ static __forceinline__ T save(double f, int v) {
+        return __float2half_rn((float)(f - wgt(v)) * h16_inv(v));
+    }
+    __device__ static __forceinline__ float dev(T x, int v) { return __half2float(x) * h16_scale(v); }
+    __device__ static __forceinline__ T put(float g, int v) { return __float2half_rn(g * h16_inv(v)); }
+};
 
 // Site type from the wall configuration; y walls override x walls at the
 // corners (reference src/Grid.cpp:925-951).
@@ -65,14 +105,15 @@ __device__ __forceinline__ void site_normal(const LatDev& L, int i, int j, int& 
 // Pull gather: the post-stream population v at (i,j) is the post-collision
 // population v of the upwind site (i-cx, j-cy), with periodic wrap
 // (the push index of src/Grid.cpp:229,240 read backwards).
-template <class T>
-__device__ __forceinline__ void gather(const T* __restrict__ P, const LatDev& L, int i, int j, double f[9]) {
+template <class S>
+__device__ __forceinline__ void gather(const typename S::T* __restrict__ P, const LatDev& L, int i, int j,
+                                       double f[9]) {
 #pragma unroll
     for (int v = 0; v < 9; v++) {
         int si = i - cx_of(v), sj = j - cy_of(v);
         si = si < 0 ? si + L.Nx : (si >= L.Nx ? si - L.Nx : si);
         sj = sj < 0 ? sj + L.Ny : (sj >= L.Ny ? sj - L.Ny : sj);
-        f[v] = (double)P[(size_t)v * L.S + (size_t)sj * L.pitch + si];
+        f[v] = S::load(P[(size_t)v * L.S + (size_t)sj * L.pitch + si], v);
     }
 }
 
@@ -155,11 +196,11 @@ __device__ __forceinline__ void force_xy_at(const LatDev& L, int t, double& Fx, 
 
 // Post-macroscopic moments of a fluid site of step t (read by boundary sites:
 // Utils::extrapolate / zeroGradient, inc/Utils.h:137-217).
-template <class T>
-__device__ __forceinline__ void fluid_moments(const T* __restrict__ P, const LatDev& L, int i, int j, double Fx,
-                                              double Fy, double& rho, double& ux, double& uy) {
+template <class S>
+__device__ __forceinline__ void fluid_moments(const typename S::T* __restrict__ P, const LatDev& L, int i, int j,
+                                              double Fx, double Fy, double& rho, double& ux, double& uy) {
     double f[9];
-    gather(P, L, i, j, f);
+    gather<S>(P, L, i, j, f);
     macroscopic(f, Fx, Fy, rho, ux, uy);
 }
 
@@ -219,10 +260,10 @@ __device__ __forceinline__ void regularised(double f[9], int type, int nx, int n
 // the boundary condition (GridClass::applyBCs, src/Grid.cpp:302-384;
 // convectiveBC :468-474) and the macroscopic moments (without the IBM
 // correction, which support sites receive afterwards).
-template <bool CM, class T>
-__device__ __forceinline__ void site_state(const T* __restrict__ P, const LatDev& L, int t, int i, int j, double f[9],
-                                           double& rho, double& ux, double& uy) {
-    gather(P, L, i, j, f);
+template <bool CM, class S>
+__device__ __forceinline__ void site_state(const typename S::T* __restrict__ P, const LatDev& L, int t, int i, int j,
+                                           double f[9], double& rho, double& ux, double& uy) {
+    gather<S>(P, L, i, j, f);
     double Fx, Fy;
     force_xy_at(L, t, Fx, Fy);
     const int type = site_type(L, i, j);
@@ -246,8 +287,8 @@ __device__ __forceinline__ void site_state(const T* __restrict__ P, const LatDev
             } else if (type == LIFE_FREESLIP || type == LIFE_PRESSURE) {
                 // zeroGradient order 2 along the normal on the new velocity field
                 double q1, a1x, a1y, q2, a2x, a2y;
-                fluid_moments(P, L, i + nx, j + ny, Fx, Fy, q1, a1x, a1y);
-                fluid_moments(P, L, i + 2 * nx, j + 2 * ny, Fx, Fy, q2, a2x, a2y);
+                fluid_moments<S>(P, L, i + nx, j + ny, Fx, Fy, q1, a1x, a1y);
+                fluid_moments<S>(P, L, i + 2 * nx, j + 2 * ny, Fx, Fy, q2, a2x, a2y);
                 if (type == LIFE_FREESLIP) un[nd] = 0.0;
                 else rn = L.rho_in[j];
                 const int d = 1 - nd;
@@ -258,8 +299,8 @@ __device__ __forceinline__ void site_state(const T* __restrict__ P, const LatDev
             }
             if (corner && (type == LIFE_VELOCITY || type == LIFE_WALL)) {
                 double a, b;
-                fluid_moments(P, L, i + nx, j + ny, Fx, Fy, r1, a, b);
-                fluid_moments(P, L, i + 2 * nx, j + 2 * ny, Fx, Fy, r2, a, b);
+                fluid_moments<S>(P, L, i + nx, j + ny, Fx, Fy, r1, a, b);
+                fluid_moments<S>(P, L, i + 2 * nx, j + 2 * ny, Fx, Fy, r2, a, b);
             }
             regularised<CM>(f, type, nx, ny, nd, rn, un, L.cs, r1, r2);
         }

@@ -1,14 +1,18 @@
-// FP64 lattice kernels: the plain form that reproduces the reference's CPU
-// FP64 results. Compiled with --fmad=false (see the header of lbm_device.cuh).
+// Lattice kernels with FP64 arithmetic: the plain form that reproduces the
+// reference's CPU FP64 results, plus the FP64-arithmetic parts every storage
+// form shares (boundary sites, start-up, restart, export). Compiled with
+// --fmad=false (see the header of lbm_device.cuh).
 //
-//   k_init_f64      initial equilibrium state and the first collision
-//   k_step_f64      fused pull-stream + macroscopic + boundary conditions +
-//                   collision of the next step (one read and one write of the
-//                   nine populations per site)
+//   k_init          initial equilibrium state and the first collision
+//   k_interior_f64  fused pull-stream + macroscopic + collision of the next
+//                   step for fluid sites (one read and one write of the nine
+//                   populations per site)
+//   k_perimeter     the same for boundary-condition sites, with the
+//                   regularised / convective conditions applied
 //   k_outlet_f64    convective outlet speed (sequential mean, as the reference)
-//   k_state_f64     collision from an explicit state (restart read)
-//   k_export_f64    reference-layout fields of the current step
-//   k_maxvel_f64    max |u| and NaN scan
+//   k_state         collision from an explicit state (restart read)
+//   k_export        reference-layout fields of the current step
+//   k_maxvel        max |u| and NaN scan
 #include <cuda_runtime.h>
 
 #include "collide_cm.cuh"
@@ -34,22 +38,22 @@ __device__ __forceinline__ void outlet_outputs(const LatDev& L, int i, int j, co
     }
 }
 
-template <bool CM>
-__device__ __forceinline__ void store_collided(double* __restrict__ B, const LatDev& L, int t_next, int i, int j,
-                                               const double f[9], double rho, double ux, double uy, double Ix,
+template <bool CM, class S>
+__device__ __forceinline__ void store_collided(typename S::T* __restrict__ B, const LatDev& L, int t_next, int i,
+                                               int j, const double f[9], double rho, double ux, double uy, double Ix,
                                                double Iy) {
     double Fx, Fy, fs[9];
     force_xy_at(L, t_next, Fx, Fy);
     collide<CM>(f, rho, ux, uy, Fx + Ix, Fy + Iy, L.omega, L.cs, fs);
     const size_t s = (size_t)j * L.pitch + i;
 #pragma unroll
-    for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = fs[v];
+    for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = S::save(fs[v], v);
 }
 
 // GridClass::initialiseGrid (reference src/Grid.cpp:998-1061): rho = 1,
 // initial velocity, f = feq; then the collision of step t0+1.
-template <bool CM>
-__global__ void k_init_f64(double* __restrict__ B, LatDev L, int t0) {
+template <bool CM, class S>
+__global__ void k_init(typename S::T* __restrict__ B, LatDev L, int t0) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     if (i >= L.Nx) return;
     double ux, uy;
@@ -62,19 +66,51 @@ __global__ void k_init_f64(double* __restrict__ B, LatDev L, int t0) {
 #pragma unroll
     for (int v = 0; v < 9; v++) f[v] = equilibrium<CM>(v, rho, ux, uy);
     outlet_outputs(L, i, j, f, ux, uy);
-    store_collided<CM>(B, L, t0 + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
+    store_collided<CM, S>(B, L, t0 + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
 }
 
-// One time step: S_t from P_t (A), then P_{t+1} into B. IBM support sites are
-// collided again by the IBM fix-up kernel once the spread force is known.
+// One time step, interior sites, FP64: S_t from P_t (A), then P_{t+1} into B.
+// Sites on a boundary-condition wall are left to k_perimeter; IBM support
+// sites are collided again by the IBM fix-up kernel once the spread force is
+// known. Same arithmetic as site_state() for a fluid site.
 template <bool CM>
-__global__ void __launch_bounds__(128) k_step_f64(const double* __restrict__ A, double* __restrict__ B, LatDev L, int t) {
+__global__ void __launch_bounds__(128) k_interior_f64(const double* __restrict__ A, double* __restrict__ B, LatDev L,
+                                                      int t) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     if (i >= L.Nx) return;
-    double f[9], rho, ux, uy;
-    site_state<CM>(A, L, t, i, j, f, rho, ux, uy);
+    if (site_type(L, i, j) != LIFE_FLUID) return;
+    double f[9], rho, ux, uy, Fx, Fy;
+    const bool edge = (i == 0) | (i == L.Nx - 1) | (j == 0) | (j == L.Ny - 1);
+    if (edge) {
+        gather<StoreF64>(A, L, i, j, f);
+    } else {
+        const size_t base = (size_t)j * L.pitch + i;
+#pragma unroll
+        for (int v = 0; v < 9; v++) f[v] = A[(size_t)v * L.S + base - cx_of(v) - (long long)cy_of(v) * L.pitch];
+    }
+    force_xy_at(L, t, Fx, Fy);
+    macroscopic(f, Fx, Fy, rho, ux, uy);
     outlet_outputs(L, i, j, f, ux, uy);
-    store_collided<CM>(B, L, t + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
+    store_collided<CM, StoreF64>(B, L, t + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
+}
+
+// Boundary-condition sites of one step (any storage form, FP64 arithmetic):
+// the perimeter is enumerated bottom row, top row, left column, right column.
+template <bool CM, class S>
+__global__ void k_perimeter(const typename S::T* __restrict__ A, typename S::T* __restrict__ B, LatDev L, int t) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Nx = L.Nx, Ny = L.Ny;
+    int i, j;
+    if (q < Nx) { i = q; j = 0; }
+    else if (q < 2 * Nx) { i = q - Nx; j = Ny - 1; }
+    else if (q < 2 * Nx + (Ny - 2)) { i = 0; j = q - 2 * Nx + 1; }
+    else if (q < 2 * Nx + 2 * (Ny - 2)) { i = Nx - 1; j = q - 2 * Nx - (Ny - 2) + 1; }
+    else return;
+    if (site_type(L, i, j) == LIFE_FLUID) return;
+    double f[9], rho, ux, uy;
+    site_state<CM, S>(A, L, t, i, j, f, rho, ux, uy);
+    outlet_outputs(L, i, j, f, ux, uy);
+    store_collided<CM, S>(B, L, t + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
 }
 
 // GridClass::convectiveSpeed (src/Grid.cpp:477-495): the mean outlet speed is
@@ -100,8 +136,8 @@ __global__ void k_outlet_f64(LatDev L, double* __restrict__ delU) {
 
 // Collision from an explicit reference-layout state (GridClass::readRestart,
 // src/Grid.cpp:1072-1160, followed by the next step's collision).
-template <bool CM>
-__global__ void k_state_f64(double* __restrict__ B, LatDev L, int t, const double* __restrict__ rho_in,
+template <bool CM, class S>
+__global__ void k_state(typename S::T* __restrict__ B, LatDev L, int t, const double* __restrict__ rho_in,
                             const double* __restrict__ u_in, const double* __restrict__ f_in,
                             const double* __restrict__ fibm_in) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
@@ -112,18 +148,18 @@ __global__ void k_state_f64(double* __restrict__ B, LatDev L, int t, const doubl
     for (int v = 0; v < 9; v++) f[v] = f_in[id * 9 + v];
     const double rho = rho_in[id], ux = u_in[id * 2], uy = u_in[id * 2 + 1];
     outlet_outputs(L, i, j, f, ux, uy);
-    store_collided<CM>(B, L, t + 1, i, j, f, rho, ux, uy, fibm_in[id * 2], fibm_in[id * 2 + 1]);
+    store_collided<CM, S>(B, L, t + 1, i, j, f, rho, ux, uy, fibm_in[id * 2], fibm_in[id * 2 + 1]);
 }
 
 // Reference-layout export of the state after step t (what
 // GridClass::writeRestart dumps, src/Grid.cpp:1191-1222).
-template <bool CM>
-__global__ void k_export_f64(const double* __restrict__ P, LatDev L, int t, double* __restrict__ rho_out,
+template <bool CM, class S>
+__global__ void k_export(const typename S::T* __restrict__ P, LatDev L, int t, double* __restrict__ rho_out,
                              double* __restrict__ u_out, double* __restrict__ f_out, double* __restrict__ fibm_out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     if (i >= L.Nx) return;
     double f[9], rho, ux, uy;
-    site_state<CM>(P, L, t, i, j, f, rho, ux, uy);
+    site_state<CM, S>(P, L, t, i, j, f, rho, ux, uy);
     double Ix = 0.0, Iy = 0.0;
     if (L.force_ibm) {
         const size_t s = (size_t)j * L.pitch + i;
@@ -145,7 +181,7 @@ __global__ void k_export_f64(const double* __restrict__ P, LatDev L, int t, doub
 
 // Initial state (before any step) in reference layout.
 template <bool CM>
-__global__ void k_export_init_f64(LatDev L, double* __restrict__ rho_out, double* __restrict__ u_out,
+__global__ void k_export_init(LatDev L, double* __restrict__ rho_out, double* __restrict__ u_out,
                                   double* __restrict__ f_out, double* __restrict__ fibm_out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     if (i >= L.Nx) return;
@@ -164,14 +200,14 @@ __global__ void k_export_init_f64(LatDev L, double* __restrict__ rho_out, double
 
 // max |u| and NaN flag over the current state (GridClass::writeInfo,
 // src/Grid.cpp:562-588). out[0] = max as ordered bits, out[1] = NaN count.
-template <bool CM>
-__global__ void k_maxvel_f64(const double* __restrict__ P, LatDev L, int t, unsigned long long* out) {
+template <bool CM, class S>
+__global__ void k_maxvel(const typename S::T* __restrict__ P, LatDev L, int t, unsigned long long* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     double vel = 0.0;
     bool nan = false;
     if (i < L.Nx) {
         double f[9], rho, ux, uy;
-        site_state<CM>(P, L, t, i, j, f, rho, ux, uy);
+        site_state<CM, S>(P, L, t, i, j, f, rho, ux, uy);
         if (L.force_ibm) {
             const size_t s = (size_t)j * L.pitch + i;
             double Ix = L.force_ibm[s], Iy = L.force_ibm[L.S + s];
@@ -198,45 +234,73 @@ __global__ void k_maxvel_f64(const double* __restrict__ P, LatDev L, int t, unsi
 // ------------------------------------------------------------ launchers
 static inline dim3 grid_of(const LatDev& L) { return dim3((L.Nx + 127) / 128, L.Ny); }
 
-cudaError_t launch_init_f64(double* B, const LatDev& L, int t0, cudaStream_t s) {
-    if (L.cm) k_init_f64<true><<<grid_of(L), 128, 0, s>>>(B, L, t0);
-    else k_init_f64<false><<<grid_of(L), 128, 0, s>>>(B, L, t0);
+// Instantiates KERNEL for the case's storage form and collision; PTR is the
+// population buffer (cast to the storage type), the rest are passed through.
+#define LIFE_DISPATCH(KERNEL, CONSTQ, PTR, ...)                                                         \
+    do {                                                                                                \
+        if (L.prec == LIFE_PREC_F64) {                                                                  \
+            if (L.cm) KERNEL<true, StoreF64><<<grid_of(L), 128, 0, s>>>((CONSTQ double*)(PTR), __VA_ARGS__); \
+            else KERNEL<false, StoreF64><<<grid_of(L), 128, 0, s>>>((CONSTQ double*)(PTR), __VA_ARGS__);    \
+        } else if (L.prec == LIFE_PREC_F32) {                                                           \
+            if (L.cm) KERNEL<true, StoreF32><<<grid_of(L), 128, 0, s>>>((CONSTQ float*)(PTR), __VA_ARGS__);  \
+            else KERNEL<false, StoreF32><<<grid_of(L), 128, 0, s>>>((CONSTQ float*)(PTR), __VA_ARGS__);     \
+        } else {                                                                                        \
+            if (L.cm) KERNEL<true, StoreF16><<<grid_of(L), 128, 0, s>>>((CONSTQ __half*)(PTR), __VA_ARGS__); \
+            else KERNEL<false, StoreF16><<<grid_of(L), 128, 0, s>>>((CONSTQ __half*)(PTR), __VA_ARGS__);    \
+        }                                                                                               \
+    } while (0)
+
+cudaError_t launch_init(void* B, const LatDev& L, int t0, cudaStream_t s) {
+    LIFE_DISPATCH(k_init, , B, L, t0);
     return cudaGetLastError();
 }
 
-cudaError_t launch_step_f64(const double* A, double* B, const LatDev& L, int t, cudaStream_t s) {
-    if (L.cm) k_step_f64<true><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
-    else k_step_f64<false><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
+cudaError_t launch_interior_f64(const double* A, double* B, const LatDev& L, int t, cudaStream_t s) {
+    if (L.cm) k_interior_f64<true><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
+    else k_interior_f64<false><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
     return cudaGetLastError();
 }
 
-cudaError_t launch_outlet_f64(const LatDev& L, double* delU, cudaStream_t s) {
-    k_outlet_f64<<<1, 256, 0, s>>>(L, delU);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_state_f64(double* B, const LatDev& L, int t, const double* rho, const double* u,
-                             const double* f, const double* fibm, cudaStream_t s) {
-    if (L.cm) k_state_f64<true><<<grid_of(L), 128, 0, s>>>(B, L, t, rho, u, f, fibm);
-    else k_state_f64<false><<<grid_of(L), 128, 0, s>>>(B, L, t, rho, u, f, fibm);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_export_f64(const double* P, const LatDev& L, int t, bool initial, double* rho, double* u,
-                              double* f, double* fibm, cudaStream_t s) {
-    if (initial) {
-        if (L.cm) k_export_init_f64<true><<<grid_of(L), 128, 0, s>>>(L, rho, u, f, fibm);
-        else k_export_init_f64<false><<<grid_of(L), 128, 0, s>>>(L, rho, u, f, fibm);
+cudaError_t launch_perimeter(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
+    const int n = 2 * L.Nx + 2 * (L.Ny - 2);
+    const dim3 grid((n + 127) / 128);
+    if (L.prec == LIFE_PREC_F64) {
+        if (L.cm) k_perimeter<true, StoreF64><<<grid, 128, 0, s>>>((const double*)A, (double*)B, L, t);
+        else k_perimeter<false, StoreF64><<<grid, 128, 0, s>>>((const double*)A, (double*)B, L, t);
+    } else if (L.prec == LIFE_PREC_F32) {
+        if (L.cm) k_perimeter<true, StoreF32><<<grid, 128, 0, s>>>((const float*)A, (float*)B, L, t);
+        else k_perimeter<false, StoreF32><<<grid, 128, 0, s>>>((const float*)A, (float*)B, L, t);
     } else {
-        if (L.cm) k_export_f64<true><<<grid_of(L), 128, 0, s>>>(P, L, t, rho, u, f, fibm);
-        else k_export_f64<false><<<grid_of(L), 128, 0, s>>>(P, L, t, rho, u, f, fibm);
+        if (L.cm) k_perimeter<true, StoreF16><<<grid, 128, 0, s>>>((const __half*)A, (__half*)B, L, t);
+        else k_perimeter<false, StoreF16><<<grid, 128, 0, s>>>((const __half*)A, (__half*)B, L, t);
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_maxvel_f64(const double* P, const LatDev& L, int t, unsigned long long* out, cudaStream_t s) {
-    if (L.cm) k_maxvel_f64<true><<<grid_of(L), 128, 0, s>>>(P, L, t, out);
-    else k_maxvel_f64<false><<<grid_of(L), 128, 0, s>>>(P, L, t, out);
+cudaError_t launch_outlet(const LatDev& L, double* delU, cudaStream_t s) {
+    k_outlet_f64<<<1, 256, 0, s>>>(L, delU);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_state(void* B, const LatDev& L, int t, const double* rho, const double* u, const double* f,
+                         const double* fibm, cudaStream_t s) {
+    LIFE_DISPATCH(k_state, , B, L, t, rho, u, f, fibm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export(const void* P, const LatDev& L, int t, bool initial, double* rho, double* u, double* f,
+                          double* fibm, cudaStream_t s) {
+    if (initial) {
+        if (L.cm) k_export_init<true><<<grid_of(L), 128, 0, s>>>(L, rho, u, f, fibm);
+        else k_export_init<false><<<grid_of(L), 128, 0, s>>>(L, rho, u, f, fibm);
+    } else {
+        LIFE_DISPATCH(k_export, const, P, L, t, rho, u, f, fibm);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_maxvel(const void* P, const LatDev& L, int t, unsigned long long* out, cudaStream_t s) {
+    LIFE_DISPATCH(k_maxvel, const, P, L, t, out);
     return cudaGetLastError();
 }
 

@@ -6,13 +6,26 @@
 
 namespace life {
 
-cudaError_t launch_init_f64(double* B, const LatDev& L, int t0, cudaStream_t s);
-cudaError_t launch_step_f64(const double* A, double* B, const LatDev& L, int t, cudaStream_t s);
-cudaError_t launch_outlet_f64(const LatDev& L, double* delU, cudaStream_t s);
-cudaError_t launch_state_f64(double* B, const LatDev& L, int t, const double* rho, const double* u,
-                             const double* f, const double* fibm, cudaStream_t s);
-cudaError_t launch_export_f64(const double* P, const LatDev& L, int t, bool initial, double* rho, double* u,
-                              double* f, double* fibm, cudaStream_t s);
-cudaError_t launch_maxvel_f64(const double* P, const LatDev& L, int t, unsigned long long* out, cudaStream_t s);
+// All launchers take the population buffers as untyped pointers; their
+// element type follows L.prec (double / float / __half).
+cudaError_t launch_init(void* B, const LatDev& L, int t0, cudaStream_t s);
+cudaError_t launch_interior_f64(const double* A, double* B, const LatDev& L, int t, cudaStream_t s);
+cudaError_t launch_interior_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s);
+cudaError_t launch_perimeter(const void* A, void* B, const LatDev& L, int t, cudaStream_t s);
+cudaError_t launch_outlet(const LatDev& L, double* delU, cudaStream_t s);
+cudaError_t launch_state(void* B, const LatDev& L, int t, const double* rho, const double* u, const double* f,
+                         const double* fibm, cudaStream_t s);
+cudaError_t launch_export(const void* P, const LatDev& L, int t, bool initial, double* rho, double* u, double* f,
+                          double* fibm, cudaStream_t s);
+cudaError_t launch_maxvel(const void* P, const LatDev& L, int t, unsigned long long* out, cudaStream_t s);
+
+// One lattice step: interior sites, then the boundary-condition perimeter.
+// Both read A and write disjoint sites of B.
+inline cudaError_t launch_step(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
+    cudaError_t e = L.prec == LIFE_PREC_F64 ? launch_interior_f64((const double*)A, (double*)B, L, t, s)
+                                            : launch_interior_lowp(A, B, L, t, s);
+    if (e != cudaSuccess) return e;
+    return launch_perimeter(A, B, L, t, s);
+}
 
 }  // namespace life

@@ -1,0 +1,167 @@
+// Reduced-precision lattice kernels: FP32 shifted populations and FP16
+// storage, both collided in FP32 (compiled with FMA contraction).
+//
+// Interior (fluid) sites take this fast path. It holds only the deviations
+// g_v = f_v - w_v in registers:
+//   drho = sum g_v,  rho = 1 + drho,  rho*u = sum c_v g_v + F/2,
+// and writes post-collision deviations, so no term of size w_v ever enters an
+// FP32 sum. Boundary-condition sites go to the perimeter kernel and IBM
+// support sites to the IBM fix-up kernel; both convert to FP64 and reuse the
+// reference-order code (lbm_device.cuh).
+//
+// BGK (GridClass::streamCollide BGK branch, reference src/Grid.cpp:236-244):
+//   g*_v = g_v + omega (geq_v - g_v) + (1 - omega/2) F_v
+//   geq_v = w_v [drho + rho (3 c.u + 4.5 (c.u)^2 - 1.5 u.u)]
+//   F_v   = 3 w_v [(c - u).F + 3 (c.u)(c.F)]
+// Central moments (src/Grid.cpp:106-233, De Rosis 2019): the inverse transform
+// is linear in the moments k; its rest-state part factorises per axis,
+//   E_v(u) = e(cx,ux) e(cy,uy),  e(0,u) = 2/3 - u^2,  e(+-1,u) = 1/6 +- u/2 + u^2/2,
+// so g*_v = drho E_v + (E_v - w_v) + sum_m T_vm(u) k_m over the force and
+// stress moments, with E_v - w_v = w_x d_y + d_x w_y + d_x d_y free of
+// cancellation (d = e - e|_{u=0}).
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "lbm_device.cuh"
+#include "lbm_kernels.h"
+
+namespace life {
+
+__device__ __forceinline__ void e1d(float u, float e[3], float w[3], float d[3]) {
+    // index 0: c = 0, 1: c = +1, 2: c = -1
+    const float u2 = u * u;
+    w[0] = 2.0f / 3.0f;
+    w[1] = w[2] = 1.0f / 6.0f;
+    d[0] = -u2;
+    d[1] = 0.5f * u + 0.5f * u2;
+    d[2] = -0.5f * u + 0.5f * u2;
+    e[0] = w[0] + d[0];
+    e[1] = w[1] + d[1];
+    e[2] = w[2] + d[2];
+}
+
+__device__ __forceinline__ int ax(int c) { return c == 0 ? 0 : (c > 0 ? 1 : 2); }
+
+template <bool CM>
+__device__ __forceinline__ void collide_dev32(const float g[9], float dr, float rho, float mx, float my, float ux,
+                                              float uy, float Gx, float Gy, float omega, float gs[9]) {
+    if (!CM) {
+        const float usq15 = 1.5f * (ux * ux + uy * uy);
+        const float uF = ux * Gx + uy * Gy;
+        const float fo = 1.0f - 0.5f * omega;
+#pragma unroll
+        for (int v = 0; v < 9; v++) {
+            const float cx = (float)cx_of(v), cy = (float)cy_of(v), w = wgt_f(v);
+            const float cu = cx * ux + cy * uy;
+            const float cF = cx * Gx + cy * Gy;
+            const float geq = w * (dr + rho * (3.0f * cu + 4.5f * cu * cu - usq15));
+            const float Fv = 3.0f * w * ((cF - uF) + 3.0f * cu * cF);
+            gs[v] = g[v] + omega * (geq - g[v]) + fo * Fv;
+        }
+    } else {
+        // raw second moments of the deviations
+        const float dxxyy = (g[1] + g[2]) - (g[3] + g[4]);
+        const float gxy = (g[5] + g[6]) - (g[7] + g[8]);
+        const float k4 = (1.0f - omega) * (dxxyy - 2.0f * ux * mx + 2.0f * uy * my + (ux * ux - uy * uy) * rho);
+        const float k5 = (1.0f - omega) * (gxy - uy * mx - ux * my + ux * uy * rho);
+        const float k1 = 0.5f * Gx, k2 = 0.5f * Gy, k7 = Gx * (1.0f / 6.0f), k6 = Gy * (1.0f / 6.0f);
+        float ex[3], wx[3], dx[3], ey[3], wy[3], dy[3];
+        e1d(ux, ex, wx, dx);
+        e1d(uy, ey, wy, dy);
+        const float X2 = ux * ux, Y2 = uy * uy, XY = ux * uy;
+        // T_v1..T_v7 (force/stress columns of the inverse transform)
+        float T1[9], T2[9], T4[9], T5[9], T6[9], T7[9];
+        T1[0] = 2.0f * ux * (Y2 - 1.0f);          T2[0] = 2.0f * uy * (X2 - 1.0f);
+        T4[0] = -0.5f * (X2 - Y2);                T5[0] = 4.0f * XY;
+        T6[0] = 2.0f * uy;                        T7[0] = 2.0f * ux;
+        T1[1] = -0.5f * (2.0f * ux + 1.0f) * (Y2 - 1.0f);  T2[1] = -XY * (ux + 1.0f);
+        T4[1] = 0.25f * (X2 + ux - Y2 + 1.0f);    T5[1] = -uy * (2.0f * ux + 1.0f);
+        T6[1] = -uy;                              T7[1] = -0.5f * (2.0f * ux + 1.0f);
+        T1[2] = -0.5f * (2.0f * ux - 1.0f) * (Y2 - 1.0f);  T2[2] = -XY * (ux - 1.0f);
+        T4[2] = 0.25f * (X2 - ux - Y2 + 1.0f);    T5[2] = -uy * (2.0f * ux - 1.0f);
+        T6[2] = -uy;                              T7[2] = -0.5f * (2.0f * ux - 1.0f);
+        T1[3] = -XY * (uy + 1.0f);                T2[3] = -0.5f * (X2 - 1.0f) * (2.0f * uy + 1.0f);
+        T4[3] = 0.25f * (X2 - Y2 - uy - 1.0f);    T5[3] = -ux * (2.0f * uy + 1.0f);
+        T6[3] = -0.5f * (2.0f * uy + 1.0f);       T7[3] = -ux;
+        T1[4] = -XY * (uy - 1.0f);                T2[4] = -0.5f * (X2 - 1.0f) * (2.0f * uy - 1.0f);
+        T4[4] = 0.25f * (X2 - Y2 + uy - 1.0f);    T5[4] = -ux * (2.0f * uy - 1.0f);
+        T6[4] = -0.5f * (2.0f * uy - 1.0f);       T7[4] = -ux;
+        T1[5] = 0.25f * uy * (2.0f * ux + 1.0f) * (uy + 1.0f);  T2[5] = 0.25f * ux * (ux + 1.0f) * (2.0f * uy + 1.0f);
+        T4[5] = -0.125f * (ux - uy) * (ux + uy + 1.0f);          T5[5] = 0.25f * (2.0f * ux + 1.0f) * (2.0f * uy + 1.0f);
+        T6[5] = 0.25f * (2.0f * uy + 1.0f);                      T7[5] = 0.25f * (2.0f * ux + 1.0f);
+        T1[6] = 0.25f * uy * (2.0f * ux - 1.0f) * (uy - 1.0f);  T2[6] = 0.25f * ux * (ux - 1.0f) * (2.0f * uy - 1.0f);
+        T4[6] = -0.125f * (ux - uy) * (ux + uy - 1.0f);          T5[6] = 0.25f * (2.0f * ux - 1.0f) * (2.0f * uy - 1.0f);
+        T6[6] = 0.25f * (2.0f * uy - 1.0f);                      T7[6] = 0.25f * (2.0f * ux - 1.0f);
+        T1[7] = 0.25f * uy * (2.0f * ux + 1.0f) * (uy - 1.0f);  T2[7] = 0.25f * ux * (ux + 1.0f) * (2.0f * uy - 1.0f);
+        T4[7] = -0.125f * (ux + uy) * (ux - uy + 1.0f);          T5[7] = 0.25f * (2.0f * ux + 1.0f) * (2.0f * uy - 1.0f);
+        T6[7] = 0.25f * (2.0f * uy - 1.0f);                      T7[7] = 0.25f * (2.0f * ux + 1.0f);
+        T1[8] = 0.25f * uy * (2.0f * ux - 1.0f) * (uy + 1.0f);  T2[8] = 0.25f * ux * (ux - 1.0f) * (2.0f * uy + 1.0f);
+        T4[8] = -0.125f * (ux + uy) * (ux - uy - 1.0f);          T5[8] = 0.25f * (2.0f * ux - 1.0f) * (2.0f * uy + 1.0f);
+        T6[8] = 0.25f * (2.0f * uy + 1.0f);                      T7[8] = 0.25f * (2.0f * ux - 1.0f);
+#pragma unroll
+        for (int v = 0; v < 9; v++) {
+            const int a = ax(cx_of(v)), b = ax(cy_of(v));
+            const float E = ex[a] * ey[b];
+            const float D = wx[a] * dy[b] + dx[a] * wy[b] + dx[a] * dy[b];
+            gs[v] = dr * E + D + T1[v] * k1 + T2[v] * k2 + T4[v] * k4 + T5[v] * k5 + T6[v] * k6 + T7[v] * k7;
+        }
+    }
+}
+
+// Interior sites, reduced-precision storage. Sites on a boundary-condition
+// wall are left to the perimeter kernel.
+template <bool CM, class S>
+__global__ void __launch_bounds__(256) k_interior_lowp(const typename S::T* __restrict__ A,
+                                                       typename S::T* __restrict__ B, LatDev L, int t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= L.Nx) return;
+    if (site_type(L, i, j) != LIFE_FLUID) return;
+    const bool edge = (i == 0) | (i == L.Nx - 1) | (j == 0) | (j == L.Ny - 1);
+    float g[9];
+    const size_t base = (size_t)j * L.pitch + i;
+    if (!edge) {
+#pragma unroll
+        for (int v = 0; v < 9; v++)
+            g[v] = S::dev(A[(size_t)v * L.S + base - cx_of(v) - (long long)cy_of(v) * L.pitch], v);
+    } else {
+#pragma unroll
+        for (int v = 0; v < 9; v++) {
+            int si = i - cx_of(v), sj = j - cy_of(v);
+            si = si < 0 ? si + L.Nx : (si >= L.Nx ? si - L.Nx : si);
+            sj = sj < 0 ? sj + L.Ny : (sj >= L.Ny ? sj - L.Ny : sj);
+            g[v] = S::dev(A[(size_t)v * L.S + (size_t)sj * L.pitch + si], v);
+        }
+    }
+    double Fxd, Fyd, Gxd, Gyd;
+    force_xy_at(L, t, Fxd, Fyd);
+    force_xy_at(L, t + 1, Gxd, Gyd);
+    const float dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
+    const float rho = 1.0f + dr;
+    const float mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
+    const float my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
+    const float inv = 1.0f / rho;
+    const float ux = (mx + 0.5f * (float)Fxd) * inv, uy = (my + 0.5f * (float)Fyd) * inv;
+    if (L.convective && i >= L.Nx - 3) {
+        const int c = i - (L.Nx - 3);
+        L.outlet_u[((size_t)c * L.Ny + j) * 2 + 0] = ux;
+        L.outlet_u[((size_t)c * L.Ny + j) * 2 + 1] = uy;
+    }
+    float gs[9];
+    collide_dev32<CM>(g, dr, rho, mx, my, ux, uy, (float)Gxd, (float)Gyd, (float)L.omega, gs);
+#pragma unroll
+    for (int v = 0; v < 9; v++) B[(size_t)v * L.S + base] = S::put(gs[v], v);
+}
+
+cudaError_t launch_interior_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
+    const dim3 grid((L.Nx + 255) / 256, L.Ny);
+    if (L.prec == LIFE_PREC_F32) {
+        if (L.cm) k_interior_lowp<true, StoreF32><<<grid, 256, 0, s>>>((const float*)A, (float*)B, L, t);
+        else k_interior_lowp<false, StoreF32><<<grid, 256, 0, s>>>((const float*)A, (float*)B, L, t);
+    } else {
+        if (L.cm) k_interior_lowp<true, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t);
+        else k_interior_lowp<false, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace life

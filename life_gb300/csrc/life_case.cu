@@ -110,6 +110,7 @@ LatDev life::lattice_view(const LifeCase* c, int t) {
     L.wall[2] = c->p.wall_bottom;
     L.wall[3] = c->p.wall_top;
     L.cm = c->p.central_moments;
+    L.prec = c->p.precision;
     L.womersley = c->p.has_womersley;
     L.convective = c->p.wall_right == LIFE_CONVECTIVE;
     L.has_ibm = c->obj.hasIBM;
@@ -173,7 +174,7 @@ static void free_case(LifeCase* c) {
 
 int upload_markers(LifeCase* c);
 int setup_fem(LifeCase* c);
-int ibm_step(LifeCase* c, int t, const double* A, double* B);
+int ibm_step(LifeCase* c, int t, const void* A, void* B);
 
 extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc* bodies, int32_t n_bodies,
                                 LifeCase** out) {
@@ -187,7 +188,8 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
     cudaGetDevice(&c->device);
     c->Nx = p.Nx;
     c->Ny = p.Ny;
-    c->pitch = (p.Nx + 31) / 32 * 32;
+    // Rows start on 128-byte boundaries for every storage form.
+    c->pitch = (p.Nx + 63) / 64 * 64;
     c->S = (long long)c->pitch * p.Ny;
     // GridClass::GridClass (src/Grid.cpp:1243-1260)
     const double rho0 = 1.0;
@@ -204,10 +206,7 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
     c->u0x = p.ux0_p * c->Dt / c->Dx;
     c->u0y = p.uy0_p * c->Dt / c->Dx;
     c->init_mode = p.has_inlet_ramp ? 0 : (p.profile >= 0 ? 1 : 2);
-    if (p.precision != LIFE_PREC_F64) {
-        delete c;
-        return set_error(LIFE_ERR_INVALID, "only the FP64 form is built into this library version");
-    }
+    c->elem = p.precision == LIFE_PREC_F64 ? 8 : (p.precision == LIFE_PREC_F32 ? 4 : 2);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete c;
@@ -248,7 +247,7 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
     }
     // Device buffers
     const size_t plane = (size_t)c->S;
-    if ((rc = dev_alloc_t(c, &c->P[0], plane * 9)) || (rc = dev_alloc_t(c, &c->P[1], plane * 9)) ||
+    if ((rc = dev_alloc(c, &c->P[0], plane * 9 * c->elem)) || (rc = dev_alloc(c, &c->P[1], plane * 9 * c->elem)) ||
         (rc = dev_alloc_t(c, &c->d_u_in, (size_t)p.Ny * 2)) || (rc = dev_alloc_t(c, &c->d_rho_in, (size_t)p.Ny)) ||
         (rc = dev_alloc_t(c, &c->d_outlet_u, (size_t)3 * p.Ny * 2)) ||
         (rc = dev_alloc_t(c, &c->d_outlet_f[0], (size_t)p.Ny * 3)) ||
@@ -277,7 +276,7 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
         return rc;
     }
     LatDev L = lattice_view(c, 0);
-    e = launch_init_f64(c->P[0], L, 0, c->stream);
+    e = launch_init(c->P[0], L, 0, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) {
         free_case(c);
@@ -305,6 +304,58 @@ static int check_device_status(LifeCase* c) {
     return LIFE_OK;
 }
 
+// Runs nsteps time steps on the case's stream. With `timing`, CUDA events are
+// recorded around every interior-lattice launch and around the whole range,
+// and the launches of the library's kernels are counted.
+struct StepTiming {
+    std::vector<cudaEvent_t> ev;   // 2 per step: before/after the interior kernel
+    cudaEvent_t start = nullptr, stop = nullptr;
+    int launches = 0;
+};
+
+static int run_steps(LifeCase* c, int nsteps, StepTiming* tm) {
+    int rc = ensure_steps(c, c->t, nsteps + 2);
+    if (rc) return rc;
+    const bool conv = c->p.wall_right == LIFE_CONVECTIVE;
+    if (tm) cudaEventRecord(tm->start, c->stream);
+    for (int k = 0; k < nsteps; k++) {
+        const int tt = c->t + 1;
+        LatDev L = lattice_view(c, tt);
+        const void* A = c->P[c->cur];
+        void* B = c->P[c->cur ^ 1];
+        cudaError_t e;
+        if (conv) {
+            e = launch_outlet(L, c->d_delU, c->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "outlet");
+            if (tm) tm->launches++;
+        }
+        if (tm) cudaEventRecord(tm->ev[2 * k], c->stream);
+        e = L.prec == LIFE_PREC_F64 ? launch_interior_f64((const double*)A, (double*)B, L, tt, c->stream)
+                                    : launch_interior_lowp(A, B, L, tt, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "interior step");
+        if (tm) cudaEventRecord(tm->ev[2 * k + 1], c->stream);
+        e = launch_perimeter(A, B, L, tt, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "perimeter step");
+        if (tm) tm->launches += 2;
+        if (c->obj.hasIBM) {
+            int before = c->ibm_launches;
+            if ((rc = ibm_step(c, tt, A, B))) return rc;
+            if (tm) tm->launches += c->ibm_launches - before;
+        }
+        c->cur ^= 1;
+        c->t = tt;
+    }
+    if (tm) cudaEventRecord(tm->stop, c->stream);
+    if (c->obj.hasFlex) {
+        if ((rc = check_device_status(c))) return rc;
+        if (c->status_code) {
+            c->status_msg = "Subiteration scheme hit 20 iterations...exiting";
+            return set_error(c->status_code, c->status_msg);
+        }
+    }
+    return LIFE_OK;
+}
+
 extern "C" int life_case_step(LifeCase* c, int32_t nsteps) {
     if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
     if (nsteps < 0) return set_error(LIFE_ERR_INVALID, "negative step count");
@@ -313,34 +364,41 @@ extern "C" int life_case_step(LifeCase* c, int32_t nsteps) {
     int prev = -1;
     cudaGetDevice(&prev);
     if (prev != c->device) cudaSetDevice(c->device);
-    int rc = ensure_steps(c, c->t, nsteps + 2);
-    if (rc) return rc;
-    const bool conv = c->p.wall_right == LIFE_CONVECTIVE;
-    for (int k = 0; k < nsteps; k++) {
-        const int tt = c->t + 1;
-        LatDev L = lattice_view(c, tt);
-        const double* A = c->P[c->cur];
-        double* B = c->P[c->cur ^ 1];
-        if (conv) {
-            cudaError_t e = launch_outlet_f64(L, c->d_delU, c->stream);
-            if (e != cudaSuccess) return cuda_fail(e, "outlet");
-        }
-        cudaError_t e = launch_step_f64(A, B, L, tt, c->stream);
-        if (e != cudaSuccess) return cuda_fail(e, "step");
-        if (c->obj.hasIBM) {
-            if ((rc = ibm_step(c, tt, A, B))) return rc;
-        }
-        c->cur ^= 1;
-        c->t = tt;
-    }
-    if (c->obj.hasFlex) {
-        if ((rc = check_device_status(c))) return rc;
-        if (c->status_code) {
-            c->status_msg = "Subiteration scheme hit 20 iterations...exiting";
-            return set_error(c->status_code, c->status_msg);
-        }
-    }
+    int rc = run_steps(c, nsteps, nullptr);
     if (prev >= 0 && prev != c->device) cudaSetDevice(prev);
+    return rc;
+}
+
+extern "C" int life_case_bench_steps(LifeCase* c, int32_t nsteps, double* total_ms, double* interior_ms,
+                                     int32_t* launches) {
+    if (!c || nsteps <= 0) return set_error(LIFE_ERR_INVALID, "bad arguments");
+    if (c->status_code) return set_error(c->status_code, c->status_msg);
+    StepTiming tm;
+    tm.ev.resize(2 * (size_t)nsteps);
+    for (auto& e : tm.ev) CK(cudaEventCreate(&e));
+    CK(cudaEventCreate(&tm.start));
+    CK(cudaEventCreate(&tm.stop));
+    CK(cudaStreamSynchronize(c->stream));
+    int rc = run_steps(c, nsteps, &tm);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    double tot = 0.0, inner = 0.0;
+    if (rc == LIFE_OK && e == cudaSuccess) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, tm.start, tm.stop);
+        tot = ms;
+        for (int k = 0; k < nsteps; k++) {
+            cudaEventElapsedTime(&ms, tm.ev[2 * k], tm.ev[2 * k + 1]);
+            inner += ms;
+        }
+    }
+    for (auto& ev : tm.ev) cudaEventDestroy(ev);
+    cudaEventDestroy(tm.start);
+    cudaEventDestroy(tm.stop);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "bench_steps");
+    if (total_ms) *total_ms = tot;
+    if (interior_ms) *interior_ms = inner / nsteps;
+    if (launches) *launches = tm.launches;
     return LIFE_OK;
 }
 
@@ -418,7 +476,7 @@ extern "C" int life_case_get_fields(LifeCase* c, double* rho, double* u, double*
     }
     LatDev L = lattice_view(c, c->t);
     const bool initial = (c->t == c->t_set);
-    cudaError_t e = launch_export_f64(c->P[c->cur ^ 1], L, c->t, initial, d_rho, d_u, d_f, d_fi, c->stream);
+    cudaError_t e = launch_export(c->P[c->cur ^ 1], L, c->t, initial, d_rho, d_u, d_f, d_fi, c->stream);
     if (e == cudaSuccess && rho) e = cudaMemcpyAsync(rho, d_rho, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess && u) e = cudaMemcpyAsync(u, d_u, n * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess && f) e = cudaMemcpyAsync(f, d_f, n * 9 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
@@ -464,7 +522,7 @@ extern "C" int life_case_set_fields(LifeCase* c, int32_t t, const double* rho, c
         return rc;
     }
     LatDev L = lattice_view(c, t);
-    cudaError_t e = launch_state_f64(c->P[0], L, t, d_rho, d_u, d_f, d_fi, c->stream);
+    cudaError_t e = launch_state(c->P[0], L, t, d_rho, d_u, d_f, d_fi, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     cleanup();
     if (e != cudaSuccess) return cuda_fail(e, "set_fields");
@@ -493,7 +551,7 @@ extern "C" int life_case_max_velocity(LifeCase* c, double* max_vel, int32_t* has
         if (has_nan) *has_nan = nan;
         return LIFE_OK;
     }
-    CK(launch_maxvel_f64(c->P[c->cur ^ 1], L, c->t, c->d_red, c->stream));
+    CK(launch_maxvel(c->P[c->cur ^ 1], L, c->t, c->d_red, c->stream));
     CK(cudaMemcpyAsync(h, c->d_red, sizeof h, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     double m;

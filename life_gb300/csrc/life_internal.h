@@ -41,7 +41,8 @@ struct LifeCase {
     bool host_state = false;  // state loaded from host arrays (kept for export)
     std::vector<double> h_rho, h_u, h_f, h_fibm;
     // device lattice state
-    double* P[2] = {nullptr, nullptr};
+    void* P[2] = {nullptr, nullptr};  // element type per p.precision
+    int elem = 8;     // bytes per stored population
     int cur = 0;      // P[cur] holds P_{t+1}
     double* d_u_in = nullptr;
     double* d_rho_in = nullptr;
@@ -63,6 +64,7 @@ struct LifeCase {
     life::FsiScalars* d_fsi = nullptr;
     int* d_status = nullptr;  // [code, t, ...]
     int status_code = 0, status_t = 0;
+    int ibm_launches = 0;     // kernels launched by the IBM/FEM sequence so far
     std::string status_msg;
 };
 

@@ -24,6 +24,7 @@ struct LatDev {
     int wall[4];          // left, right, bottom, top (LIFE_* lattice types)
     long long S;          // sites per population plane (pitch * Ny)
     int cm;               // central moments collision
+    int prec;             // population storage form (LIFE_PREC_*)
     int womersley;        // force_xy(t) from steps[]; else the constant Fx0/Fy0
     int convective;       // right wall is a convective outlet
     int has_ibm;

@@ -46,6 +46,7 @@ SIGNATURES = {
     "life_case_max_velocity": (C.c_int, [C.c_void_p, _dp, _ip]),
     "life_case_total_force": (C.c_int, [C.c_void_p, _dp, _dp]),
     "life_parse_geometry": (C.c_int, [C.c_char_p, C.c_void_p, C.c_int32, _ip]),
+    "life_case_bench_steps": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _ip]),
 }
 
 
@@ -190,6 +191,13 @@ class Case:
         m, nan = C.c_double(), C.c_int32()
         _check(lib().life_case_max_velocity(self._h, C.byref(m), C.byref(nan)))
         return m.value, bool(nan.value)
+
+    def bench_steps(self, n: int):
+        """Run n steps; return (total_ms, mean interior-kernel ms, kernel launches),
+        all measured with CUDA events on the case's stream."""
+        tot, inner, launches = C.c_double(), C.c_double(), C.c_int32()
+        _check(lib().life_case_bench_steps(self._h, int(n), C.byref(tot), C.byref(inner), C.byref(launches)))
+        return tot.value, inner.value, launches.value
 
     def total_force(self):
         fx, fy = C.c_double(), C.c_double()

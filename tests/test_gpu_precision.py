@@ -1,0 +1,62 @@
+"""Reduced-precision storage forms against the FP64 reference dumps.
+
+The FP32 form stores shifted populations f - w and collides in FP32; the
+FP16 form stores (f - w)/s_v with power-of-two per-direction scales. Both must
+stay within a stated velocity error of the reference's FP64 result after the
+full golden run (hundreds of steps). Tolerances (relative to max |u|):
+FP32 <= 1e-5, FP16 <= 5e-3.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from cases import golden_cases
+from life_gb300.case import PREC_F16, PREC_F32
+
+pytestmark = pytest.mark.gpu
+CASES = golden_cases()
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TOL = {PREC_F32: 1e-5, PREC_F16: 5e-3}
+NAMES = [k for k, (_, b) in CASES.items() if not any(getattr(x, "flexible", False) for x in b)]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from life_gb300.build import build
+    build()
+
+
+@pytest.mark.parametrize("prec", [PREC_F32, PREC_F16], ids=["f32", "f16"])
+@pytest.mark.parametrize("name", NAMES)
+def test_velocity_error_vs_reference(name, prec):
+    from life_gb300.lib import Case
+    p, b = CASES[name]
+    g = np.load(os.path.join(GOLD, f"{name}.npz"))
+    with Case(p.replace(precision=prec), b) as c:
+        c.step(p.nSteps)
+        fl = c.fields(("rho", "u"))
+    scale = np.abs(g["u"]).max()
+    err = np.abs(fl["u"] - g["u"]).max() / scale
+    assert err <= TOL[prec], err
+    assert np.abs(fl["rho"] - g["rho"]).max() < 50 * TOL[prec]
+
+
+def test_fp32_interior_matches_fp64_one_step_from_same_state():
+    """One step from an identical (FP32-representable) state: the FP32 fast
+    path and the FP64 path agree to FP32 rounding."""
+    from life_gb300.lib import Case
+    p, b = CASES["cavity_cm"]
+    with Case(p, b) as c64:
+        c64.step(50)
+        st = c64.fields()
+    f = st["f"]
+    w = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
+    f32 = (f - w).astype(np.float32).astype(np.float64) + w
+    with Case(p, b) as a, Case(p.replace(precision=PREC_F32), b) as q:
+        a.set_fields(50, st["rho"], st["u"], f32, st["force_ibm"])
+        q.set_fields(50, st["rho"], st["u"], f32, st["force_ibm"])
+        a.step(1)
+        q.step(1)
+        ua, uq = a.fields(("u",))["u"], q.fields(("u",))["u"]
+    assert np.abs(ua - uq).max() / np.abs(ua).max() < 2e-6
