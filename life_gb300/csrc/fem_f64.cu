@@ -1,0 +1,694 @@
+// Flexible-body kernels (FP64, --fmad=false, reference operation order).
+//
+// One CTA per flexible body runs the FEM work of that body:
+//   k_fsi_predict   predictor (first subiteration) or Aitken relaxation,
+//                   then updateFEMValues / finishNewmark / updateIBMValues
+//                   (FEMBodyClass::predictor, src/FEMBody.cpp:259-289;
+//                   ObjectsClass::recomputeObjectVals, src/Objects.cpp:152-232)
+//   k_fem_dynamic   FEMBodyClass::dynamicFEM (src/FEMBody.cpp:26-68): load
+//                   vector, Newton-Raphson with Newmark and the dense LU solve,
+//                   marker update, subiteration residual
+// and
+//   k_fsi_support   findSupport + computeDs of flexible markers
+//   k_fsi_epsilon   epsilon systems (per flexible body or all markers)
+//   k_fsi_residual  femKernel's ordered residual sums, the loop condition and
+//                   the next Aitken factor (src/Objects.cpp:63-99, 179-190)
+//
+// Element matrices are computed in parallel and assembled entry by entry in
+// element order, the order of the reference's sequential assembly. Products
+// with the element rotation T skip its structural zeros; a skipped term is an
+// exact zero, so results are unchanged.
+#include <cuda_runtime.h>
+
+#include "band_lu.h"
+#include "fem_kernels.h"
+
+namespace life {
+
+#define DSQ(x) ((x) * (x))
+#define DTH(x) ((x) * (x) * (x))
+__device__ constexpr double kPI = 3.14159265358979323846;
+
+__device__ __forceinline__ double* vec(FemBodyDev& B, int name) { return B.pool + (size_t)B.slots[name] * B.n; }
+
+__device__ __forceinline__ double shift_angle_d(double a) {
+    a = fmod(a + kPI, 2.0 * kPI);
+    if (a < 0.0) a += 2.0 * kPI;
+    return a - kPI;
+}
+
+__device__ __forceinline__ double dirac_d(double dist) {
+    double a = fabs(dist);
+    if (a > 1.5) return 0.0;
+    if (a > 0.5) return (5.0 - 3.0 * a - sqrt(-3.0 * DSQ(1.0 - a) + 1.0)) / 6.0;
+    return (1.0 + sqrt(1.0 - 3.0 * DSQ(a))) / 3.0;
+}
+
+// Element rotation T = diag(R, R), R = [[c, s, 0], [-s, c, 0], [0, 0, 1]]
+// (FEMElementClass::setElementTransform, src/FEMElement.cpp:255-262).
+__host__ __device__ constexpr bool tnz(int i, int j) {
+    return (i < 2 && j < 2) || (i == 2 && j == 2) || (i >= 3 && i < 5 && j >= 3 && j < 5) || (i == 5 && j == 5);
+}
+__device__ __forceinline__ double tval(int i, int j, double c, double s) {
+    const int a = i % 3, b = j % 3;
+    if (a == 2) return 1.0;
+    if (a == 0) return b == 0 ? c : s;
+    return b == 0 ? -s : c;
+}
+
+// out = T^T A T with the reference's summation order over non-zero terms.
+__device__ __forceinline__ void tt_a_t(const double* A, double c, double s, double* out) {
+    double R1[36];
+#pragma unroll
+    for (int i = 0; i < 6; i++)
+#pragma unroll
+        for (int j = 0; j < 6; j++) {
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if (tnz(k, i)) acc += tval(k, i, c, s) * A[k * 6 + j];
+            R1[i * 6 + j] = acc;
+        }
+#pragma unroll
+    for (int i = 0; i < 6; i++)
+#pragma unroll
+        for (int j = 0; j < 6; j++) {
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if (tnz(k, j)) acc += R1[i * 6 + k] * tval(k, j, c, s);
+            out[i * 6 + j] = acc;
+        }
+}
+
+// FEMBodyClass::updateFEMValues (src/FEMBody.cpp:198-223)
+__device__ void update_fem_values(FemBodyDev& B) {
+    const double* U = vec(B, V_U);
+    for (int n = threadIdx.x; n < B.nNodes; n += blockDim.x) {
+        double* nd = B.node + n * 6;
+        nd[2] = nd[0] + U[n * 3 + 0];
+        nd[3] = nd[1] + U[n * 3 + 1];
+        nd[5] = nd[4] + U[n * 3 + 2];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < B.nEl; e += blockDim.x) {
+        const double* n0 = B.node + e * 6;
+        const double* n1 = B.node + (e + 1) * 6;
+        const double ev0 = n1[2] - n0[2], ev1 = n1[3] - n0[3];
+        double* el = B.el + (size_t)e * EL_STRIDE;
+        const double ang = atan2(ev1, ev0);
+        double dd = 0.0;
+        dd += ev0 * ev0;
+        dd += ev1 * ev1;
+        el[EL_ANG] = ang;
+        el[EL_L] = sqrt(dd);
+        el[EL_COS] = cos(ang);
+        el[EL_SIN] = sin(ang);
+    }
+    __syncthreads();
+}
+
+// FEMBodyClass::finishNewmark (src/FEMBody.cpp:129-144)
+__device__ void finish_newmark(FemBodyDev& B, const FsiDev& F) {
+    const double Dt = F.Dt, al = F.alpha, de = F.delta;
+    const double a6 = 1.0 / (al * DSQ(Dt)), a7 = -1.0 / (al * Dt), a8 = -(1.0 / (2.0 * al) - 1.0);
+    const double a9 = Dt * (1.0 - de), a10 = de * Dt;
+    double* U = vec(B, V_U);
+    double* Un = vec(B, V_Un);
+    double* Ud = vec(B, V_Udot);
+    double* Udd = vec(B, V_Udotdot);
+    double* Udn = vec(B, V_Udotn);
+    double* Uddn = vec(B, V_Udotdotn);
+    for (int i = threadIdx.x; i < B.n; i += blockDim.x) {
+        const double udd = a6 * (U[i] - Un[i]) + a7 * Udn[i] + a8 * Uddn[i];
+        Udd[i] = udd;
+        Ud[i] = Udn[i] + a9 * Uddn[i] + a10 * udd;
+    }
+    __syncthreads();
+}
+
+// FEMElementClass::shapeFuns (src/FEMElement.cpp:141-160)
+__device__ __forceinline__ void shape_funs_d(double res[2], const double v[6], double zeta, double L) {
+    const double N0 = 1.0 - (zeta + 1.0) / 2.0;
+    const double N1 = 1.0 - 3.0 * DSQ((zeta + 1.0) / 2.0) + 2.0 * DTH((zeta + 1.0) / 2.0);
+    const double N2 = ((zeta + 1.0) / 2.0 - 2.0 * DSQ((zeta + 1.0) / 2.0) + DTH((zeta + 1.0) / 2.0)) * L;
+    const double N3 = (zeta + 1.0) / 2.0;
+    const double N4 = 3.0 * DSQ((zeta + 1.0) / 2.0) - 2.0 * DTH((zeta + 1.0) / 2.0);
+    const double N5 = (-DSQ((zeta + 1.0) / 2.0) + DTH((zeta + 1.0) / 2.0)) * L;
+    res[0] = v[0] * N0 + v[3] * N3;
+    res[1] = v[1] * N1 + v[2] * N2 + v[4] * N4 + v[5] * N5;
+}
+
+// T * v over non-zero entries of T.
+__device__ __forceinline__ void t_vec(const double v[6], double c, double s, double out[6]) {
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+        double acc = 0.0;
+#pragma unroll
+        for (int j = 0; j < 6; j++)
+            if (tnz(i, j)) acc += tval(i, j, c, s) * v[j];
+        out[i] = acc;
+    }
+}
+// T^T * v over non-zero entries of T.
+__device__ __forceinline__ void tt_vec(const double v[6], double c, double s, double out[6]) {
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+        double acc = 0.0;
+#pragma unroll
+        for (int j = 0; j < 6; j++)
+            if (tnz(j, i)) acc += tval(j, i, c, s) * v[j];
+        out[i] = acc;
+    }
+}
+
+// FEMBodyClass::updateIBMValues (src/FEMBody.cpp:147-195)
+__device__ void update_ibm(FemBodyDev& B, const MarkerDev& M) {
+    const double* U = vec(B, V_U);
+    const double* Ud = vec(B, V_Udot);
+    for (int i = threadIdx.x; i < B.nMark; i += blockDim.x) {
+        const int e = B.mapEl[i];
+        const double zeta = B.mapZeta[i];
+        const double* el = B.el + (size_t)e * EL_STRIDE;
+        const double c = el[EL_COS], s = el[EL_SIN], ang = el[EL_ANG], L = el[EL_L];
+        double dU[6], dUd[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            dU[k] = U[3 * e + k];
+            dUd[k] = Ud[3 * e + k];
+        }
+        const double* nd0 = B.node + e * 6;
+#pragma unroll
+        for (int n = 0; n < 2; n++) {
+            const double* nd = B.node + (e + n) * 6;
+            dU[n * 3 + 0] += nd[0] - nd0[2];
+            dU[n * 3 + 1] += nd[1] - nd0[3];
+            dU[n * 3 + 2] += nd[4] - ang;
+            dU[n * 3 + 2] = shift_angle_d(dU[n * 3 + 2]);
+        }
+        double lU[6], lUd[6], sU[2], sUd[2];
+        t_vec(dU, c, s, lU);
+        t_vec(dUd, c, s, lUd);
+        shape_funs_d(sU, lU, zeta, L);
+        shape_funs_d(sUd, lUd, zeta, L);
+        const double gU0 = (0.0 + c * sU[0]) + (-s) * sU[1];
+        const double gU1 = (0.0 + s * sU[0]) + c * sU[1];
+        const double gV0 = (0.0 + c * sUd[0]) + (-s) * sUd[1];
+        const double gV1 = (0.0 + s * sUd[0]) + c * sUd[1];
+        const int k = B.mbase + i;
+        M.pos[k * 2 + 0] = nd0[2] + gU0;
+        M.pos[k * 2 + 1] = nd0[3] + gU1;
+        M.vel[k * 2 + 0] = gV0;
+        M.vel[k * 2 + 1] = gV1;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void swap_slots(FemBodyDev& B, int a, int b) {
+    const int t = B.slots[a];
+    B.slots[a] = B.slots[b];
+    B.slots[b] = t;
+}
+
+// Predictor (subiteration 0) or relaxation (later subiterations).
+__global__ void __launch_bounds__(256) k_fsi_predict(FsiDev F, MarkerDev M) {
+    FemBodyDev& B = F.bodies[blockIdx.x];
+    const int subIt = F.s->subIt;
+    const int t = F.s->t;
+    if (subIt == 0) {
+        if (threadIdx.x == 0) {
+            // FEMBodyClass::resetValues (src/FEMBody.cpp:341-349)
+            swap_slots(B, V_Unm2, V_Unm1);
+            swap_slots(B, V_Unm1, V_Un);
+            swap_slots(B, V_Un, V_U);
+            swap_slots(B, V_Udotn, V_Udot);
+            swap_slots(B, V_Udotdotn, V_Udotdot);
+        }
+        __syncthreads();
+        double* U = vec(B, V_U);
+        const double* Un = vec(B, V_Un);
+        const double* Unm1 = vec(B, V_Unm1);
+        const double* Unm2 = vec(B, V_Unm2);
+        for (int i = threadIdx.x; i < B.n; i += blockDim.x) {
+            if (t > 2) U[i] = 2.5 * Un[i] - 2.0 * Unm1[i] + 0.5 * Unm2[i];
+            else if (t == 2) U[i] = 2.0 * Un[i] - Unm1[i];
+            else if (t == 1) U[i] = Un[i];
+        }
+    } else {
+        const double relax = F.s->relax;
+        double* U = vec(B, V_U);
+        const double* Uk = vec(B, V_Ukm1);
+        for (int i = threadIdx.x; i < B.n; i += blockDim.x) U[i] = Uk[i] + relax * (U[i] - Uk[i]);
+    }
+    __syncthreads();
+    update_fem_values(B);
+    finish_newmark(B, F);
+    update_ibm(B, M);
+    if (threadIdx.x == 0) swap_slots(B, V_Ukm1, V_U);
+}
+
+// IBMNodeClass::findSupport + computeDs (src/IBMNode.cpp:139-204) for the
+// markers of flexible bodies.
+__global__ void k_fsi_support(FsiDev F, MarkerDev M) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= F.nFlexMarkers) return;
+    const int k = F.flexMarkers[q];
+    const double Dx = F.Dx;
+    const double px = M.pos[k * 2], py = M.pos[k * 2 + 1];
+    const int inear = (int)round(px / Dx), jnear = (int)round(py / Dx);
+    int ns = 0;
+    for (int s = 0; s < 9; s++) {
+        M.si[k * 9 + s] = 0;
+        M.sj[k * 9 + s] = 0;
+        M.sd[k * 9 + s] = 0.0;
+    }
+    for (int i = inear - 2; i <= inear + 2; i++) {
+        const double dX = fabs(px / Dx - i);
+        for (int j = jnear - 2; j <= jnear + 2; j++) {
+            const double dY = fabs(py / Dx - j);
+            if (dX < 1.5 && dY < 1.5 && i >= 0 && i <= F.Nx - 1 && j >= 0 && j <= F.Ny - 1) {
+                if (ns == 9) {
+                    atomicCAS(&F.status[0], 0, LIFE_ERR_SUPPORT);
+                    continue;
+                }
+                M.si[k * 9 + ns] = i;
+                M.sj[k * 9 + ns] = j;
+                M.sd[k * 9 + ns] = dirac_d(dX) * dirac_d(dY);
+                ns++;
+            }
+        }
+    }
+    M.nsupp[k] = ns;
+    const int b = F.markerBody[k];
+    const int b0 = F.bodyStart[b], bn = F.bodyCount[b];
+    double cur = 10.0;
+    for (int n = 0; n < bn; n++) {
+        const int o = b0 + n;
+        if (o != k) {
+            const double d0 = px - M.pos[o * 2], d1 = py - M.pos[o * 2 + 1];
+            double dd = 0.0;
+            dd += d0 * d0;
+            dd += d1 * d1;
+            const double mag = sqrt(dd) / Dx;
+            if (mag < cur) cur = mag;
+        }
+    }
+    M.ds[k] = cur;
+}
+
+// Dense LU with band-limited loops (band_lu.h semantics) by one warp.
+// M(i,j) = A[(bc+j)*dim + bc+i]. lmax[c] tracks the last row that can hold a
+// multiplier of column c after row interchanges.
+__device__ void warp_lu_factor(double* A, int dim, int bc, int kl, int ku, int* piv, int* lmax) {
+    const int lane = threadIdx.x & 31;
+    const int n = dim - bc;
+    for (int c = lane; c < n; c += 32) lmax[c] = c;
+    __syncwarp();
+    for (int j = 0; j < n; j++) {
+        const int imax = j + kl < n - 1 ? j + kl : n - 1;
+        // first maximal |M(i,j)|, i in [j, imax] (LAPACK idamax semantics)
+        int best = j;
+        double bval = -1.0;
+        for (int i0 = j; i0 <= imax; i0 += 32) {
+            const int i = i0 + lane;
+            double va = -1.0;
+            int vi = i;
+            if (i <= imax) va = fabs(lu_m(A, dim, bc, i, j));
+            for (int o = 16; o > 0; o >>= 1) {
+                const double oa = __shfl_down_sync(0xffffffffu, va, o);
+                const int oi = __shfl_down_sync(0xffffffffu, vi, o);
+                if (oa > va || (oa == va && oi < vi)) { va = oa; vi = oi; }
+            }
+            va = __shfl_sync(0xffffffffu, va, 0);
+            vi = __shfl_sync(0xffffffffu, vi, 0);
+            if (va > bval) { bval = va; best = vi; }
+        }
+        const int jp = best;
+        if (lane == 0) piv[j] = jp;
+        const double pv = lu_m(A, dim, bc, jp, j);
+        if (pv != 0.0) {
+            if (jp != j) {
+                for (int k = lane; k < n; k += 32) {
+                    const double tj = lu_m(A, dim, bc, j, k), tp = lu_m(A, dim, bc, jp, k);
+                    if (k < j && tj != 0.0 && lmax[k] < jp) lmax[k] = jp;
+                    lu_m(A, dim, bc, j, k) = tp;
+                    lu_m(A, dim, bc, jp, k) = tj;
+                }
+                __syncwarp();
+            }
+            const double r = 1.0 / lu_m(A, dim, bc, j, j);
+            for (int i = j + 1 + lane; i <= imax; i += 32) lu_m(A, dim, bc, i, j) *= r;
+        }
+        if (lane == 0 && lmax[j] < imax) lmax[j] = imax;
+        __syncwarp();
+        const int kmax = j + kl + ku < n - 1 ? j + kl + ku : n - 1;
+        const int rows = imax - j, cols = kmax - j;
+        for (int q = lane; q < rows * cols; q += 32) {
+            const int i = j + 1 + q % rows, k = j + 1 + q / rows;
+            const double t = -lu_m(A, dim, bc, j, k);
+            lu_m(A, dim, bc, i, k) += lu_m(A, dim, bc, i, j) * t;
+        }
+        __syncwarp();
+    }
+}
+
+// Transposed solve (lane 0); x has dim entries, the first bc zeroed.
+__device__ void warp_lu_solve(const double* A_, int dim, int bc, int kl, int ku, const int* piv, const int* lmax,
+                              const double* b, double* x) {
+    const int lane = threadIdx.x & 31;
+    double* A = const_cast<double*>(A_);
+    const int n = dim - bc;
+    for (int i = lane; i < bc; i += 32) x[i] = 0.0;
+    for (int i = lane; i < n; i += 32) x[bc + i] = b[bc + i];
+    __syncwarp();
+    if (lane == 0) {
+        double* y = x + bc;
+        const int w = kl + ku;
+        for (int i = 0; i < n; i++) {
+            double t = y[i];
+            for (int k = (i - w > 0 ? i - w : 0); k < i; k++) t -= lu_m(A, dim, bc, k, i) * y[k];
+            y[i] = t / lu_m(A, dim, bc, i, i);
+        }
+        for (int i = n - 1; i >= 0; i--) {
+            double t = y[i];
+            const int kend = lmax[i];
+            for (int k = i + 1; k <= kend; k++) t -= lu_m(A, dim, bc, k, i) * y[k];
+            y[i] = t;
+        }
+        for (int i = n - 1; i >= 0; i--)
+            if (piv[i] != i) {
+                const double t = y[i];
+                y[i] = y[piv[i]];
+                y[piv[i]] = t;
+            }
+    }
+    __syncwarp();
+}
+
+// Epsilon system of a contiguous marker range [m0, m0+dim) (ObjectsClass::
+// computeEpsilon, src/Objects.cpp:264-311).
+__device__ void epsilon_range(const FsiDev& F, const MarkerDev& M, int m0, int dim, double* A, double* bx, int* piv,
+                              int* lmax) {
+    __shared__ int s_kl, s_ku;
+    if (threadIdx.x == 0) { s_kl = 0; s_ku = 0; }
+    for (long long p = threadIdx.x; p < (long long)dim * dim; p += blockDim.x) A[p] = 0.0;
+    __syncthreads();
+    const double Dx = F.Dx;
+    for (long long p = threadIdx.x; p < (long long)dim * dim; p += blockDim.x) {
+        const int i = (int)(p / dim), j = (int)(p % dim);
+        const int ki = m0 + i, kj = m0 + j;
+        const double xj = M.pos[kj * 2], yj = M.pos[kj * 2 + 1];
+        if (fabs(M.pos[ki * 2] - xj) / Dx < 3.0 && fabs(M.pos[ki * 2 + 1] - yj) / Dx < 3.0) {
+            double acc = 0.0;
+            const int ns = M.nsupp[ki];
+            for (int s = 0; s < ns; s++) {
+                const double dvi = M.sd[ki * 9 + s];
+                const double dX = fabs(xj / Dx - M.si[ki * 9 + s]);
+                const double dY = fabs(yj / Dx - M.sj[ki * 9 + s]);
+                acc += dvi * (dirac_d(dX) * dirac_d(dY));
+            }
+            const double a = acc * (1.0 * 1.0 * M.ds[kj]);
+            A[p] = a;
+            if (a != 0.0) {
+                // M = A^T: entry A[i][j] is M(j, i)
+                if (j - i > 0) atomicMax(&s_kl, j - i);
+                if (i - j > 0) atomicMax(&s_ku, i - j);
+            }
+        }
+    }
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) bx[i] = 1.0;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        warp_lu_factor(A, dim, 0, s_kl, s_ku, piv, lmax);
+        warp_lu_solve(A, dim, 0, s_kl, s_ku, piv, lmax, bx, bx);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) M.eps[m0 + i] = bx[i];
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_fsi_epsilon_body(FsiDev F, MarkerDev M) {
+    FemBodyDev& B = F.bodies[blockIdx.x];
+    epsilon_range(F, M, B.mbase, B.nMark, B.epsA, B.epsB, B.piv, B.lmax);
+}
+
+__global__ void __launch_bounds__(256) k_fsi_epsilon_uni(FsiDev F, MarkerDev M) {
+    epsilon_range(F, M, 0, M.n, F.uniA, F.uniB, F.uniPiv, F.uniLmax);
+}
+
+// FEMBodyClass::dynamicFEM (src/FEMBody.cpp:26-68) for one body per CTA.
+__global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
+    FemBodyDev& B = F.bodies[blockIdx.x];
+    __shared__ double s_res;
+    __shared__ int s_it;
+    const int n = B.n;
+    {
+        double* U = vec(B, V_U);
+        double* Ud = vec(B, V_Udot);
+        double* Udd = vec(B, V_Udotdot);
+        const double* Un = vec(B, V_Un);
+        const double* Udn = vec(B, V_Udotn);
+        const double* Uddn = vec(B, V_Udotdotn);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            U[i] = Un[i];
+            Ud[i] = Udn[i];
+            Udd[i] = Uddn[i];
+        }
+    }
+    __syncthreads();
+    update_fem_values(B);
+    // constructRVector (src/FEMBody.cpp:226-234; FEMElementClass::loadVector,
+    // src/FEMElement.cpp:27-69): contributions per force-map entry, then an
+    // ordered assembly.
+    {
+        const double forceScale = F.Dm / DSQ(F.Dt);
+        for (int q = threadIdx.x; q < B.nfmap; q += blockDim.x) {
+            const int e = B.fmapEl[q];
+            const double* el = B.el + (size_t)e * EL_STRIDE;
+            const double c = el[EL_COS], s = el[EL_SIN], L = el[EL_L];
+            const double wgt0 = el[EL_RHO] * el[EL_A] * F.gravityX, wgt1 = el[EL_RHO] * el[EL_A] * F.gravityY;
+            const int k = B.mbase + B.fmapNode[q];
+            const double a = B.fmapZ[q * 2], b = B.fmapZ[q * 2 + 1];
+            const double sc = -M.eps[k] * 1.0 * forceScale;
+            const double g0 = sc * M.force[k * 2] + wgt0, g1 = sc * M.force[k * 2 + 1] + wgt1;
+            const double F0 = (0.0 + c * g0) + s * g1;
+            const double F1 = (0.0 + (-s) * g0) + c * g1;
+            double R[6], RG[6];
+            R[0] = F0 * 0.5 * L * (0.5 * b - 0.5 * a + 0.25 * DSQ(a) - 0.25 * DSQ(b));
+            R[1] = F1 * 0.5 * L * (0.5 * b - 0.5 * a - DSQ(a) * DSQ(a) / 16.0 + DSQ(b) * DSQ(b) / 16.0 + 3.0 * DSQ(a) / 8.0 - 3.0 * DSQ(b) / 8.0);
+            R[2] = F1 * 0.5 * L * (L * (-DSQ(a) * DSQ(a) + DSQ(b) * DSQ(b)) / 32.0 - L * (-DTH(a) + DTH(b)) / 24.0 - L * (-DSQ(a) + DSQ(b)) / 16.0 + L * (b - a) / 8.0);
+            R[3] = F0 * 0.5 * L * (-0.25 * DSQ(a) + 0.25 * DSQ(b) + 0.5 * b - 0.5 * a);
+            R[4] = F1 * 0.5 * L * (0.5 * b - 0.5 * a + DSQ(a) * DSQ(a) / 16.0 - DSQ(b) * DSQ(b) / 16.0 - 3.0 * DSQ(a) / 8.0 + 3.0 * DSQ(b) / 8.0);
+            R[5] = F1 * 0.5 * L * (L * (-DSQ(a) * DSQ(a) + DSQ(b) * DSQ(b)) / 32.0 + L * (-DTH(a) + DTH(b)) / 24.0 - L * (-DSQ(a) + DSQ(b)) / 16.0 - L * (b - a) / 8.0);
+            tt_vec(R, c, s, RG);
+            for (int r = 0; r < 6; r++) B.rgscr[q * 6 + r] = RG[r];
+        }
+        __syncthreads();
+        double* Rv = vec(B, V_R);
+        for (int r = threadIdx.x; r < n; r += blockDim.x) {
+            double acc = 0.0;
+            const int e1 = r / 3 - 1, e2 = r / 3;
+            for (int e = (e1 < 0 ? 0 : e1); e <= e2 && e < B.nEl; e++)
+                for (int q = B.fmapStart[e]; q < B.fmapStart[e + 1]; q++) acc += B.rgscr[q * 6 + (r - 3 * e)];
+            Rv[r] = acc;
+        }
+        __syncthreads();
+    }
+    const double Dt = F.Dt, al = F.alpha;
+    const double a0 = 1.0 / (al * DSQ(Dt)), a2 = 1.0 / (al * Dt), a3 = 1.0 / (2.0 * al) - 1.0;
+    if (threadIdx.x == 0) s_it = 0;
+    __syncthreads();
+    do {
+        // buildGlobalMatrices (src/FEMBody.cpp:90-109)
+        for (long long p = threadIdx.x; p < (long long)n * n; p += blockDim.x) B.K[p] = 0.0;
+        for (int e = threadIdx.x; e < B.nEl; e += blockDim.x) {
+            const double* el = B.el + (size_t)e * EL_STRIDE;
+            const double L = el[EL_L], L0 = el[EL_L0], E = el[EL_E], A = el[EL_A], I = el[EL_I];
+            const double c = el[EL_COS], s = el[EL_SIN], ang = el[EL_ANG];
+            const double u = (DSQ(L) - DSQ(L0)) / (L + L0);
+            const double th1 = shift_angle_d(B.node[e * 6 + 5] - ang);
+            const double th2 = shift_angle_d(B.node[(e + 1) * 6 + 5] - ang);
+            const double F0 = (E * A / L0) * u;
+            const double M1 = (2 * E * I / L0) * (2.0 * th1 + th2);
+            const double M2 = (2 * E * I / L0) * (th1 + 2.0 * th2);
+            double Fl[6];
+            Fl[0] = -F0;
+            Fl[1] = (1.0 / L0) * (M1 + M2);
+            Fl[2] = M1;
+            Fl[3] = F0;
+            Fl[4] = -(1.0 / L0) * (M1 + M2);
+            Fl[5] = M2;
+            double* sc = B.elscr + (size_t)e * ES_STRIDE;
+            tt_vec(Fl, c, s, sc + ES_F);
+            tt_a_t(el + EL_M, c, s, sc + ES_M);
+            double G[36], G2[36], KNL[36];
+            tt_a_t(el + EL_KL, c, s, G);
+            const double Fa = -Fl[0], V0 = Fl[4];
+#pragma unroll
+            for (int q = 0; q < 36; q++) KNL[q] = 0.0;
+            KNL[0 * 6 + 1] = -V0 / L0;
+            KNL[0 * 6 + 4] = V0 / L0;
+            KNL[1 * 6 + 0] = -V0 / L0;
+            KNL[1 * 6 + 1] = Fa / L0;
+            KNL[1 * 6 + 3] = V0 / L0;
+            KNL[1 * 6 + 4] = -Fa / L0;
+            KNL[3 * 6 + 1] = V0 / L0;
+            KNL[3 * 6 + 4] = -V0 / L0;
+            KNL[4 * 6 + 0] = V0 / L0;
+            KNL[4 * 6 + 1] = -Fa / L0;
+            KNL[4 * 6 + 3] = -V0 / L0;
+            KNL[4 * 6 + 4] = Fa / L0;
+            tt_a_t(KNL, c, s, G2);
+#pragma unroll
+            for (int q = 0; q < 36; q++) sc[ES_K + q] = G[q] + G2[q];
+        }
+        __syncthreads();
+        // ordered assembly of M, K (band |r-c| <= 5) and F
+        {
+            double* Fv = vec(B, V_F);
+            for (int p = threadIdx.x; p < n * 11; p += blockDim.x) {
+                const int r = p / 11, cc = r - 5 + p % 11;
+                if (cc < 0 || cc >= n) continue;
+                double am = 0.0, ak = 0.0;
+                const int lo = (r > cc ? r : cc), hi = (r < cc ? r : cc);
+                for (int e = (lo / 3 - 1 < 0 ? 0 : lo / 3 - 1); e <= hi / 3 && e < B.nEl; e++) {
+                    const int li = r - 3 * e, lj = cc - 3 * e;
+                    if (li < 0 || li > 5 || lj < 0 || lj > 5) continue;
+                    const double* sc = B.elscr + (size_t)e * ES_STRIDE;
+                    am += sc[ES_M + li * 6 + lj];
+                    ak += sc[ES_K + li * 6 + lj];
+                }
+                B.M[(size_t)r * n + cc] = am;
+                B.K[(size_t)r * n + cc] = ak;
+            }
+            for (int r = threadIdx.x; r < n; r += blockDim.x) {
+                double af = 0.0;
+                for (int e = (r / 3 - 1 < 0 ? 0 : r / 3 - 1); e <= r / 3 && e < B.nEl; e++)
+                    af += B.elscr[(size_t)e * ES_STRIDE + ES_F + (r - 3 * e)];
+                Fv[r] = af;
+            }
+        }
+        __syncthreads();
+        // setNewmark (src/FEMBody.cpp:112-126)
+        {
+            const double* U = vec(B, V_U);
+            const double* Un = vec(B, V_Un);
+            const double* Ud = vec(B, V_Udot);
+            const double* Udd = vec(B, V_Udotdot);
+            double* v = vec(B, V_delU);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) v[i] = a0 * (Un[i] - U[i]) + a2 * Ud[i] + a3 * Udd[i];
+            __syncthreads();
+            double* Fv = vec(B, V_F);
+            const double* Rv = vec(B, V_R);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                double mv = 0.0;
+                for (int j = (i - 5 < 0 ? 0 : i - 5); j <= i + 5 && j < n; j++) mv += B.M[(size_t)i * n + j] * v[j];
+                Fv[i] = Rv[i] - Fv[i] + mv;
+            }
+            for (int p = threadIdx.x; p < n * 11; p += blockDim.x) {
+                const int r = p / 11, cc = r - 5 + p % 11;
+                if (cc < 0 || cc >= n) continue;
+                B.K[(size_t)r * n + cc] = B.K[(size_t)r * n + cc] + a0 * B.M[(size_t)r * n + cc];
+            }
+        }
+        __syncthreads();
+        // delU = solveLAPACK(K, F, bcDOFs) (src/Utils.cpp:288-311)
+        if (threadIdx.x < 32) {
+            warp_lu_factor(B.K, n, B.bc, 5, 5, B.piv, B.lmax);
+            warp_lu_solve(B.K, n, B.bc, 5, 5, B.piv, B.lmax, vec(B, V_F), vec(B, V_delU));
+        }
+        __syncthreads();
+        {
+            double* U = vec(B, V_U);
+            const double* dU = vec(B, V_delU);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) U[i] = U[i] + dU[i];
+        }
+        __syncthreads();
+        update_fem_values(B);
+        if (threadIdx.x == 0) {
+            const double* dU = vec(B, V_delU);
+            double dd = 0.0;
+            for (int i = 0; i < n; i++) dd += dU[i] * dU[i];
+            s_res = sqrt(dd) / (F.ref_L * sqrt((double)n));
+            s_it++;
+        }
+        __syncthreads();
+    } while (s_res > 1e-10 && s_it < 20);
+    finish_newmark(B, F);
+    update_ibm(B, M);
+    if (threadIdx.x == 0) {
+        B.itNR = s_it;
+        B.resNR = s_res;
+        // FEMBodyClass::subResidual (src/FEMBody.cpp:244-256)
+        swap_slots(B, V_Rkm1, V_Rk);
+        double* Rk = vec(B, V_Rk);
+        const double* Rkm1 = vec(B, V_Rkm1);
+        const double* U = vec(B, V_U);
+        const double* Uk = vec(B, V_Ukm1);
+        for (int i = 0; i < n; i++) Rk[i] = U[i] - Uk[i];
+        double res = 0.0, num = 0.0, den = 0.0;
+        for (int i = 0; i < n; i++) res += Rk[i] * Rk[i];
+        for (int i = 0; i < n; i++) num += Rkm1[i] * (Rk[i] - Rkm1[i]);
+        for (int i = 0; i < n; i++) den += (Rk[i] - Rkm1[i]) * (Rk[i] - Rkm1[i]);
+        B.subRes = res;
+        B.subNum = num;
+        B.subDen = den;
+    }
+}
+
+// ObjectsClass::femKernel sums + loop condition + next relaxation factor.
+__global__ void k_fsi_residual(FsiDev F) {
+    if (threadIdx.x != 0) return;
+    FsiScalars& S = *F.s;
+    double res = 0.0, num = 0.0, den = 0.0;
+    for (int b = 0; b < F.nFlex; b++) {
+        res += F.bodies[b].subRes;
+        num += F.bodies[b].subNum;
+        den += F.bodies[b].subDen;
+    }
+    S.subRes = sqrt(res) / (F.ref_L * sqrt((double)F.simDOFs));
+    S.subNum = num;
+    S.subDen = den;
+    S.subIt += 1;
+    S.lastNR = F.nFlex > 0 ? F.bodies[0].itNR : 0;
+    const int cont = (S.subIt < 20 && S.subRes > F.subTol) ? 1 : 0;
+    if (cont) {
+        if (S.subIt == 1) {
+            const double a = fabs(S.relax);
+            const int sg = (0.0 < S.relax) - (S.relax < 0.0);
+            S.relax = (double)(sg * (a < F.relaxMax ? a : F.relaxMax));
+        } else {
+            S.relax = -S.relax * S.subNum / S.subDen;
+        }
+    } else if (S.subIt == 20) {
+        if (atomicCAS(&F.status[0], 0, LIFE_ERR_SUBITER) == 0) F.status[1] = S.t;
+    }
+    *F.cont = cont;
+}
+
+__global__ void k_fsi_begin(FsiDev F, int t) {
+    F.s->t = t;
+    F.s->subIt = 0;
+    *F.cont = 1;
+}
+
+cudaError_t launch_fsi_begin(const FsiDev& F, int t, cudaStream_t s) {
+    k_fsi_begin<<<1, 1, 0, s>>>(F, t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fsi_subiteration(const FsiDev& F, const MarkerDev& M, const void* P, const LatDev& L, int t,
+                                    double velScale, cudaStream_t s, int* launches) {
+    k_fsi_predict<<<F.nFlex, 256, 0, s>>>(F, M);
+    k_fsi_support<<<(F.nFlexMarkers + 127) / 128, 128, 0, s>>>(F, M);
+    if (F.uni) k_fsi_epsilon_uni<<<1, 256, 0, s>>>(F, M);
+    else k_fsi_epsilon_body<<<F.nFlex, 256, 0, s>>>(F, M);
+    cudaError_t e = launch_ibm_interp(P, L, t, M, velScale, s);
+    if (e != cudaSuccess) return e;
+    k_fem_dynamic<<<F.nFlex, 256, 0, s>>>(F, M);
+    k_fsi_residual<<<1, 32, 0, s>>>(F);
+    if (launches) *launches += 6;
+    return cudaGetLastError();
+}
+
+}  // namespace life

@@ -1,27 +1,254 @@
+// Host side of the flexible bodies: upload of the FEM state built at start-up
+// (objects.cpp), the per-step block Gauss-Seidel loop (ObjectsClass::
+// objectKernel, reference src/Objects.cpp:26-60) and the FEM accessors.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
 #include "fem_kernels.h"
 
 using namespace life;
 
-int setup_fem(LifeCase* c) {
-    (void)c;
-    return set_error(LIFE_ERR_INVALID, "flexible bodies are not built into this library version");
+namespace life {
+struct FemHost {
+    FsiDev F{};
+    std::vector<FemBodyDev> bodies;   // host copies of the device records
+    std::vector<int> hostBody;        // host body index of each flexible body
+    int* h_cont = nullptr;            // pinned flag
+};
+}  // namespace life
+
+#define CK(call)                                              \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+    } while (0)
+
+static int falloc(LifeCase* c, void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 8);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return set_error(LIFE_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    c->allocs.push_back(*p);
+    c->dev_bytes += bytes;
+    return LIFE_OK;
+}
+template <class T>
+static int fallocT(LifeCase* c, T** p, size_t n) {
+    return falloc(c, (void**)p, sizeof(T) * n);
+}
+template <class T>
+static int upload(LifeCase* c, T** p, const std::vector<T>& h) {
+    int rc = fallocT(c, p, h.size());
+    if (rc) return rc;
+    if (!h.empty()) {
+        cudaError_t e = cudaMemcpy(*p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(e, "upload");
+    }
+    return LIFE_OK;
 }
 
+static FemHost* fem_of(LifeCase* c) { return c->fem; }
+
+int setup_fem(LifeCase* c) {
+    FemHost* H = new FemHost();
+    c->fem = H;
+    HObjects& o = c->obj;
+    FsiDev& F = H->F;
+    int rc;
+    // body marker ranges (contiguous after de-overlap)
+    std::vector<int> start(o.b.size()), count(o.b.size()), flexMarkers;
+    for (size_t b = 0; b < o.b.size(); b++) {
+        const auto& nodes = o.b[b].nodes;
+        start[b] = nodes.empty() ? 0 : nodes[0];
+        count[b] = (int)nodes.size();
+        for (size_t k = 0; k < nodes.size(); k++)
+            if (nodes[k] != start[b] + (int)k) return set_error(LIFE_ERR_GEOMETRY, "body markers are not contiguous");
+        if (o.b[b].flex)
+            for (int k : nodes) flexMarkers.push_back(k);
+    }
+    std::vector<int> markerBody(o.m.size());
+    for (size_t k = 0; k < o.m.size(); k++) markerBody[k] = o.m[k].body;
+    if ((rc = upload(c, &F.flexMarkers, flexMarkers)) || (rc = upload(c, &F.markerBody, markerBody)) ||
+        (rc = upload(c, &F.bodyStart, start)) || (rc = upload(c, &F.bodyCount, count)))
+        return rc;
+    F.nFlexMarkers = (int)flexMarkers.size();
+    F.uni = c->p.uni_epsilon;
+    F.simDOFs = o.simDOFs;
+    const int N = (int)o.m.size();
+    if (F.uni) {
+        if ((rc = fallocT(c, &F.uniA, (size_t)N * N)) || (rc = fallocT(c, &F.uniB, (size_t)N)) ||
+            (rc = fallocT(c, &F.uniPiv, (size_t)N)) || (rc = fallocT(c, &F.uniLmax, (size_t)N)))
+            return rc;
+    }
+    // FEM bodies
+    for (size_t b = 0; b < o.b.size(); b++) {
+        if (!o.b[b].flex) continue;
+        const HFem& f = *o.b[b].fem;
+        FemBodyDev D{};
+        D.n = f.dofs;
+        D.nNodes = f.nNodes;
+        D.nEl = f.nEl;
+        D.bc = f.bc;
+        D.nMark = count[b];
+        D.mbase = start[b];
+        D.body = (int)b;
+        D.L0 = f.L0;
+        D.angle0 = f.angle0;
+        const int n = f.dofs;
+        std::vector<double> pool((size_t)NVEC * n, 0.0);
+        const std::vector<double>* src[NVEC] = {&f.U, &f.Udot, &f.Udotdot, &f.U_n, &f.U_nm1, &f.U_nm2, &f.Udot_n,
+                                                &f.Udotdot_n, &f.U_km1, &f.R_k, &f.R_km1, &f.R, &f.F, &f.delU};
+        for (int v = 0; v < NVEC; v++) {
+            for (int i = 0; i < n; i++) pool[(size_t)v * n + i] = (*src[v])[i];
+            D.slots[v] = v;
+        }
+        std::vector<double> node((size_t)f.nNodes * 6);
+        for (int k = 0; k < f.nNodes; k++) {
+            node[k * 6 + 0] = f.pos0[k * 2];
+            node[k * 6 + 1] = f.pos0[k * 2 + 1];
+            node[k * 6 + 2] = f.pos[k * 2];
+            node[k * 6 + 3] = f.pos[k * 2 + 1];
+            node[k * 6 + 4] = f.angle0n[k];
+            node[k * 6 + 5] = f.anglen[k];
+        }
+        std::vector<double> el((size_t)f.nEl * EL_STRIDE, 0.0);
+        std::vector<int> fStart(f.nEl + 1, 0), fNode, fEl;
+        std::vector<double> fZ;
+        for (int e = 0; e < f.nEl; e++) {
+            const HElement& h = f.el[e];
+            double* r = &el[(size_t)e * EL_STRIDE];
+            r[EL_L0] = h.L0;
+            r[EL_L] = h.L;
+            r[EL_ANG] = h.angle;
+            r[EL_A] = h.A;
+            r[EL_I] = h.I;
+            r[EL_E] = h.E;
+            r[EL_RHO] = h.rho;
+            r[EL_COS] = h.T[0][0];
+            r[EL_SIN] = h.T[0][1];
+            for (int q = 0; q < 36; q++) {
+                r[EL_M + q] = h.M[q / 6][q % 6];
+                r[EL_KL + q] = h.KL[q / 6][q % 6];
+            }
+            fStart[e] = (int)fNode.size();
+            for (const auto& m : h.fmap) {
+                fNode.push_back(m.node);
+                fEl.push_back(e);
+                fZ.push_back(m.z1);
+                fZ.push_back(m.z2);
+            }
+        }
+        fStart[f.nEl] = (int)fNode.size();
+        D.nfmap = (int)fNode.size();
+        if ((rc = upload(c, &D.pool, pool)) || (rc = fallocT(c, &D.K, (size_t)n * n)) ||
+            (rc = fallocT(c, &D.M, (size_t)n * n)) || (rc = upload(c, &D.node, node)) || (rc = upload(c, &D.el, el)) ||
+            (rc = fallocT(c, &D.elscr, (size_t)f.nEl * ES_STRIDE)) || (rc = upload(c, &D.fmapStart, fStart)) ||
+            (rc = upload(c, &D.fmapEl, fEl)) || (rc = upload(c, &D.fmapNode, fNode)) || (rc = upload(c, &D.fmapZ, fZ)) ||
+            (rc = fallocT(c, &D.rgscr, (size_t)D.nfmap * 6)) || (rc = upload(c, &D.mapEl, f.mapEl)) ||
+            (rc = upload(c, &D.mapZeta, f.mapZeta)) || (rc = fallocT(c, &D.piv, (size_t)n)) ||
+            (rc = fallocT(c, &D.lmax, (size_t)n)) || (rc = fallocT(c, &D.epsA, (size_t)D.nMark * D.nMark)) ||
+            (rc = fallocT(c, &D.epsB, (size_t)D.nMark)))
+            return rc;
+        CK(cudaMemset(D.M, 0, sizeof(double) * n * n));
+        H->bodies.push_back(D);
+        H->hostBody.push_back((int)b);
+    }
+    F.nFlex = (int)H->bodies.size();
+    if ((rc = upload(c, &F.bodies, H->bodies))) return rc;
+    F.s = c->d_fsi;
+    F.status = c->d_status;
+    if ((rc = fallocT(c, &F.cont, 1))) return rc;
+    CK(cudaMallocHost(&H->h_cont, sizeof(int)));
+    F.Dx = c->Dx;
+    F.Dt = c->Dt;
+    F.Dm = c->Dm;
+    F.gravityX = c->p.gravityX;
+    F.gravityY = c->p.gravityY;
+    F.ref_L = c->p.ref_L;
+    F.alpha = c->p.alpha;
+    F.delta = c->p.delta;
+    F.relaxMax = c->p.relaxMax;
+    F.subTol = c->p.subTol;
+    F.Nx = c->Nx;
+    F.Ny = c->Ny;
+    return LIFE_OK;
+}
+
+void life::free_fem(LifeCase* c) {
+    FemHost* H = fem_of(c);
+    if (!H) return;
+    if (H->h_cont) cudaFreeHost(H->h_cont);
+    delete H;
+    c->fem = nullptr;
+}
+
+// The subiteration loop of one step; the spread follows in ibm_step().
 int fem_fsi_loop(LifeCase* c, int t, const void* A, const LatDev& L) {
-    (void)c; (void)t; (void)A; (void)L;
-    return set_error(LIFE_ERR_INVALID, "flexible bodies are not built into this library version");
+    FemHost* H = fem_of(c);
+    cudaError_t e = launch_fsi_begin(H->F, t, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "fsi_begin");
+    c->ibm_launches += 1;
+    for (int it = 0; it < 20; it++) {
+        e = launch_fsi_subiteration(H->F, c->M, A, L, t, c->Dt / c->Dx, c->stream, &c->ibm_launches);
+        if (e != cudaSuccess) return cuda_fail(e, "fsi_subiteration");
+        e = cudaMemcpyAsync(H->h_cont, H->F.cont, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "fsi_loop");
+        if (!*H->h_cont) break;
+    }
+    return LIFE_OK;
 }
 
 extern "C" int life_case_get_fem(LifeCase* c, int32_t k, double* U, double* Udot, double* Udotdot, double* U_n,
                                  double* U_nm1, double* R_k, double* el_L, double* el_angle, double* node_pos,
                                  double* node_angle) {
-    (void)c; (void)k; (void)U; (void)Udot; (void)Udotdot; (void)U_n; (void)U_nm1; (void)R_k; (void)el_L;
-    (void)el_angle; (void)node_pos; (void)node_angle;
-    return set_error(LIFE_ERR_INVALID, "no flexible bodies");
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    FemHost* H = fem_of(c);
+    if (!H || k < 0 || k >= (int)H->bodies.size()) return set_error(LIFE_ERR_INVALID, "no such flexible body");
+    FemBodyDev D;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(&D, H->F.bodies + k, sizeof D, cudaMemcpyDeviceToHost));
+    const int n = D.n;
+    auto vecout = [&](int name, double* dst) -> cudaError_t {
+        if (!dst) return cudaSuccess;
+        return cudaMemcpy(dst, D.pool + (size_t)D.slots[name] * n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    };
+    CK(vecout(V_U, U));
+    CK(vecout(V_Udot, Udot));
+    CK(vecout(V_Udotdot, Udotdot));
+    CK(vecout(V_Un, U_n));
+    CK(vecout(V_Unm1, U_nm1));
+    CK(vecout(V_Rk, R_k));
+    std::vector<double> el((size_t)D.nEl * EL_STRIDE), node((size_t)D.nNodes * 6);
+    CK(cudaMemcpy(el.data(), D.el, sizeof(double) * el.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(node.data(), D.node, sizeof(double) * node.size(), cudaMemcpyDeviceToHost));
+    for (int e = 0; e < D.nEl; e++) {
+        if (el_L) el_L[e] = el[(size_t)e * EL_STRIDE + EL_L];
+        if (el_angle) el_angle[e] = el[(size_t)e * EL_STRIDE + EL_ANG];
+    }
+    for (int q = 0; q < D.nNodes; q++) {
+        if (node_pos) {
+            node_pos[q * 2] = node[q * 6 + 2];
+            node_pos[q * 2 + 1] = node[q * 6 + 3];
+        }
+        if (node_angle) node_angle[q] = node[q * 6 + 5];
+    }
+    return LIFE_OK;
 }
 
 extern "C" int life_case_get_relax(LifeCase* c, double* relax) {
-    (void)c;
-    if (relax) *relax = 0.0;
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    if (!c->d_fsi) {
+        if (relax) *relax = c->p.relaxMax;
+        return LIFE_OK;
+    }
+    FsiScalars h{};
+    CK(cudaMemcpyAsync(&h, c->d_fsi, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (relax) *relax = h.relax;
     return LIFE_OK;
 }

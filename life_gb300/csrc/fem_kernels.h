@@ -1,14 +1,79 @@
 // Flexible bodies on the device: corotational FEM with Newmark integration,
-// the block Gauss-Seidel FSI subiterations and Aitken relaxation.
+// the block Gauss-Seidel FSI subiterations and Aitken relaxation
+// (reference src/FEMBody.cpp, src/FEMElement.cpp, src/Objects.cpp:26-232).
 #pragma once
 #include <cuda_runtime.h>
 
+#include "ibm_kernels.h"
 #include "life_internal.h"
 
 namespace life {
-struct FemDev {
-    int placeholder;
+
+// Vectors of one FEM body (FEMBodyClass members, reference inc/FEMBody.h:80-107).
+// The reference swaps whole vectors (resetValues, predictor, relaxation); the
+// device keeps them in a pool and swaps slot indices instead.
+enum { V_U, V_Udot, V_Udotdot, V_Un, V_Unm1, V_Unm2, V_Udotn, V_Udotdotn, V_Ukm1, V_Rk, V_Rkm1, V_R, V_F, V_delU,
+       NVEC };
+
+// Element record: L0, L, angle, A, I, E, rho, cos(angle), sin(angle), local
+// mass matrix (6x6), local linear stiffness (6x6).
+enum { EL_L0, EL_L, EL_ANG, EL_A, EL_I, EL_E, EL_RHO, EL_COS, EL_SIN, EL_M = 9, EL_KL = 45, EL_STRIDE = 84 };
+// Per-element scratch: global mass (6x6), global stiffness (6x6), global
+// internal force (6).
+enum { ES_M = 0, ES_K = 36, ES_F = 72, ES_STRIDE = 78 };
+
+struct FemBodyDev {
+    int n, nNodes, nEl, bc;      // DOFs, nodes, elements, constrained DOFs
+    int nMark, mbase, nfmap, body;
+    double L0, angle0;
+    double* pool;      // [NVEC][n]
+    double* K;         // [n][n] row-major (reference layout)
+    double* M;         // [n][n]
+    double* node;      // [nNodes][6]: pos0x, pos0y, posx, posy, angle0, angle
+    double* el;        // [nEl][EL_STRIDE]
+    double* elscr;     // [nEl][ES_STRIDE]
+    int* fmapStart;    // [nEl+1]
+    int* fmapEl;       // [nfmap] element of each force-map entry
+    int* fmapNode;     // [nfmap] IBM marker index within the body
+    double* fmapZ;     // [nfmap][2]
+    double* rgscr;     // [nfmap][6] element load contributions
+    int* mapEl;        // [nMark]
+    double* mapZeta;   // [nMark]
+    int* piv;          // [n]
+    int* lmax;         // [n] last row that can hold a multiplier of column c
+    double* epsA;      // [nMark][nMark] epsilon system scratch
+    double* epsB;      // [nMark] right-hand side / solution
+    int slots[NVEC];
+    int itNR;
+    double resNR, subRes, subNum, subDen;
 };
+
+// Everything the FSI kernels need besides the bodies.
+struct FsiDev {
+    FemBodyDev* bodies;   // [nFlex] device array
+    int nFlex;
+    int uni;              // UNI_EPSILON: one system over all markers
+    int simDOFs;
+    int nFlexMarkers;
+    int* flexMarkers;     // [nFlexMarkers] global indices of flexible markers
+    int* markerBody;      // [nMarkers] owning body index (host body numbering)
+    int* bodyStart;       // [nBodies] first marker of each body
+    int* bodyCount;       // [nBodies] marker count of each body
+    double* uniA;         // [N][N] UNI epsilon scratch
+    double* uniB;         // [N]
+    int* uniPiv;          // [N]
+    int* uniLmax;         // [N]
+    FsiScalars* s;        // subIt, relax, residuals
+    int* status;          // [code, t]
+    int* cont;            // continue flag for the host loop
+    double Dx, Dt, Dm, gravityX, gravityY, ref_L, alpha, delta, relaxMax, subTol;
+    int Nx, Ny;
+};
+
+cudaError_t launch_fsi_subiteration(const FsiDev& F, const MarkerDev& M, const void* P, const LatDev& L, int t,
+                                    double velScale, cudaStream_t s, int* launches);
+cudaError_t launch_fsi_begin(const FsiDev& F, int t, cudaStream_t s);
+
 }  // namespace life
 
 int setup_fem(LifeCase* c);

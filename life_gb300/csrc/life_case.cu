@@ -165,8 +165,13 @@ static void free_case(LifeCase* c) {
     cudaGetDevice(&prev);
     if (c->device >= 0) cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    free_fem(c);
     for (void* p : c->allocs)
         if (p) cudaFree(p);
+    if (c->side) cudaStreamSynchronize(c->side);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (prev >= 0) cudaSetDevice(prev);
     delete c;
@@ -208,8 +213,11 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
     c->init_mode = p.has_inlet_ramp ? 0 : (p.profile >= 0 ? 1 : 2);
     c->elem = p.precision == LIFE_PREC_F64 ? 8 : (p.precision == LIFE_PREC_F32 ? 4 : 2);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
-        delete c;
+        free_case(c);
         return cuda_fail(e, "cudaStreamCreate");
     }
     // Immersed bodies on the host (geometryReadIn + initialiseObjects).
@@ -329,13 +337,20 @@ static int run_steps(LifeCase* c, int nsteps, StepTiming* tm) {
             if (e != cudaSuccess) return cuda_fail(e, "outlet");
             if (tm) tm->launches++;
         }
+        // The boundary-condition perimeter runs on a side stream, overlapped
+        // with the interior kernel: both read only A and write disjoint sites
+        // of B. The main stream waits for it before anything reads B.
+        cudaEventRecord(c->ev_fork, c->stream);
+        cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+        e = launch_perimeter(A, B, L, tt, c->side);
+        if (e != cudaSuccess) return cuda_fail(e, "perimeter step");
+        cudaEventRecord(c->ev_join, c->side);
         if (tm) cudaEventRecord(tm->ev[2 * k], c->stream);
         e = L.prec == LIFE_PREC_F64 ? launch_interior_f64((const double*)A, (double*)B, L, tt, c->stream)
                                     : launch_interior_lowp(A, B, L, tt, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "interior step");
         if (tm) cudaEventRecord(tm->ev[2 * k + 1], c->stream);
-        e = launch_perimeter(A, B, L, tt, c->stream);
-        if (e != cudaSuccess) return cuda_fail(e, "perimeter step");
+        cudaStreamWaitEvent(c->stream, c->ev_join, 0);
         if (tm) tm->launches += 2;
         if (c->obj.hasIBM) {
             int before = c->ibm_launches;

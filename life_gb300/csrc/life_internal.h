@@ -17,11 +17,12 @@ namespace life {
 struct FsiScalars {
     int subIt;
     int lastNR;
-    int pad[2];
+    int t;          // time step being solved
+    int pad;
     double relax, subRes, subNum, subDen;
 };
 
-struct FemDev;  // fem_kernels.h
+struct FemHost;  // fem_host.cu
 
 int set_error(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* where);
@@ -52,7 +53,9 @@ struct LifeCase {
     double* d_outlet_f[2] = {nullptr, nullptr};
     double* d_delU = nullptr;
     unsigned long long* d_red = nullptr;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;   // every kernel of the case is ordered on this stream
+    cudaStream_t side = nullptr;     // perimeter kernel, forked from and joined to `stream`
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     size_t dev_bytes = 0;
     std::vector<void*> allocs;
     // immersed bodies
@@ -60,7 +63,7 @@ struct LifeCase {
     life::HObjects obj;
     life::MarkerDev M{};
     life::IbmScratch W{};
-    life::FemDev* fem = nullptr;
+    life::FemHost* fem = nullptr;
     life::FsiScalars* d_fsi = nullptr;
     int* d_status = nullptr;  // [code, t, ...]
     int status_code = 0, status_t = 0;
@@ -70,5 +73,6 @@ struct LifeCase {
 
 namespace life {
 LatDev lattice_view(const LifeCase* c, int t);
+void free_fem(LifeCase* c);
 int ensure_steps(LifeCase* c, int t0, int n);
 }  // namespace life
