@@ -170,6 +170,21 @@ int life_case_get_markers(LifeCase* c, double* pos, double* vel, double* force,
 int life_case_get_bodies(LifeCase* c, int32_t* ids, int32_t* flexible, int32_t* n_markers,
                          int32_t* n_fem_nodes);
 
+/* Support table of every marker (IBMNodeClass::supp, reference
+ * inc/IBMNode.h:69-70): count nsupp[n], lattice indices si/sj[n*9] and delta
+ * weights sd[n*9], as findSupport left them (src/IBMNode.cpp:139-179). */
+int life_case_get_support(LifeCase* c, int32_t* nsupp, int32_t* si, int32_t* sj, double* sd);
+
+/* Epsilon weights of the implicit IBM for one marker set, on device buffers
+ * the caller owns (ObjectsClass::computeEpsilon, src/Objects.cpp:264-311):
+ * solves A eps = 1 with A_ij = (sum_s d_i(s) delta(x_j - s)) ds_j. Inputs are
+ * device pointers pos[n*2], nsupp[n], si/sj/sd[n*9], ds[n] in lattice units
+ * (pos in physical units, Dx the lattice spacing); eps[n] is written. Runs on
+ * `stream` (a cudaStream_t, NULL for the default stream) and returns when the
+ * result is ready. Allocates the n x n system for the duration of the call. */
+int life_ibm_epsilon(const double* pos, const int32_t* nsupp, const int32_t* si, const int32_t* sj,
+                     const double* sd, const double* ds, int32_t n, double Dx, double* eps, void* stream);
+
 /* FEM state of flexible body k (in body order): each array has 3*n_fem_nodes
  * entries, or n_el / n_node entries for the element and node arrays.
  * The set mirrors FEM.restart (src/Objects.cpp:1289-1362). */

@@ -637,6 +637,21 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
 }
 
 // ObjectsClass::femKernel sums + loop condition + next relaxation factor.
+// Standalone epsilon solve over n markers with caller-provided scratch
+// (A: n*n, b: n, piv, lmax: n).
+__global__ void __launch_bounds__(256) k_epsilon_markers(FsiDev F, MarkerDev M, int n, double* A, double* b, int* piv,
+                                                         int* lmax) {
+    epsilon_range(F, M, 0, n, A, b, piv, lmax);
+}
+
+cudaError_t launch_epsilon_markers(const MarkerDev& M, int n, double Dx, double* A, double* b, int* piv, int* lmax,
+                                   cudaStream_t s) {
+    FsiDev F{};
+    F.Dx = Dx;
+    k_epsilon_markers<<<1, 256, 0, s>>>(F, M, n, A, b, piv, lmax);
+    return cudaGetLastError();
+}
+
 __global__ void k_fsi_residual(FsiDev F) {
     if (threadIdx.x != 0) return;
     FsiScalars& S = *F.s;

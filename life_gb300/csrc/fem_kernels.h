@@ -73,6 +73,9 @@ struct FsiDev {
 cudaError_t launch_fsi_subiteration(const FsiDev& F, const MarkerDev& M, const void* P, const LatDev& L, int t,
                                     double velScale, cudaStream_t s, int* launches);
 cudaError_t launch_fsi_begin(const FsiDev& F, int t, cudaStream_t s);
+// Epsilon system of markers [0, n) of M into M.eps, with caller-provided scratch.
+cudaError_t launch_epsilon_markers(const MarkerDev& M, int n, double Dx, double* A, double* b, int* piv, int* lmax,
+                                   cudaStream_t s);
 
 }  // namespace life
 

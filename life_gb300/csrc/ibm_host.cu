@@ -242,3 +242,53 @@ extern "C" int life_parse_geometry(const char* text, LifeBodyDesc* out, int32_t 
     *n = count;
     return LIFE_OK;
 }
+
+extern "C" int life_case_get_support(LifeCase* c, int32_t* nsupp, int32_t* si, int32_t* sj, double* sd) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    const int n = c->M.n;
+    if (n == 0) return LIFE_OK;
+    cudaStream_t s = c->stream;
+    if (nsupp) CK(cudaMemcpyAsync(nsupp, c->M.nsupp, 4 * n, cudaMemcpyDeviceToHost, s));
+    if (si) CK(cudaMemcpyAsync(si, c->M.si, 36 * n, cudaMemcpyDeviceToHost, s));
+    if (sj) CK(cudaMemcpyAsync(sj, c->M.sj, 36 * n, cudaMemcpyDeviceToHost, s));
+    if (sd) CK(cudaMemcpyAsync(sd, c->M.sd, 72 * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return LIFE_OK;
+}
+
+// ObjectsClass::computeEpsilon for one marker set on caller-provided device
+// buffers; the n x n system and pivots live in memory allocated per call.
+extern "C" int life_ibm_epsilon(const double* pos, const int32_t* nsupp, const int32_t* si, const int32_t* sj,
+                                const double* sd, const double* ds, int32_t n, double Dx, double* eps,
+                                void* stream) {
+    if (n < 0 || (n > 0 && (!pos || !nsupp || !si || !sj || !sd || !ds || !eps)))
+        return set_error(LIFE_ERR_INVALID, "bad arguments");
+    if (n == 0) return LIFE_OK;
+    if (!(Dx > 0.0)) return set_error(LIFE_ERR_INVALID, "Dx must be positive");
+    cudaStream_t s = (cudaStream_t)stream;
+    double *A = nullptr, *b = nullptr;
+    int *piv = nullptr, *lmax = nullptr;
+    cudaError_t e = cudaMalloc(&A, sizeof(double) * (size_t)n * n);
+    if (e == cudaSuccess) e = cudaMalloc(&b, sizeof(double) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&piv, sizeof(int) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&lmax, sizeof(int) * n);
+    if (e == cudaSuccess) {
+        MarkerDev M{};
+        M.n = n;
+        M.pos = const_cast<double*>(pos);
+        M.nsupp = const_cast<int*>(nsupp);
+        M.si = const_cast<int*>(si);
+        M.sj = const_cast<int*>(sj);
+        M.sd = const_cast<double*>(sd);
+        M.ds = const_cast<double*>(ds);
+        M.eps = eps;
+        e = launch_epsilon_markers(M, n, Dx, A, b, piv, lmax, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    cudaFree(A);
+    cudaFree(b);
+    cudaFree(piv);
+    cudaFree(lmax);
+    if (e != cudaSuccess) return cuda_fail(e, "life_ibm_epsilon");
+    return LIFE_OK;
+}

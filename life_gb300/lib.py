@@ -47,6 +47,9 @@ SIGNATURES = {
     "life_case_total_force": (C.c_int, [C.c_void_p, _dp, _dp]),
     "life_parse_geometry": (C.c_int, [C.c_char_p, C.c_void_p, C.c_int32, _ip]),
     "life_case_bench_steps": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _ip]),
+    "life_case_get_support": (C.c_int, [C.c_void_p, _ip, _ip, _ip, _dp]),
+    "life_ibm_epsilon": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_int32, C.c_double, C.c_void_p, C.c_void_p]),
 }
 
 
@@ -162,6 +165,14 @@ class Case:
         body = np.empty(n, dtype=np.int32)
         _check(lib().life_case_get_markers(self._h, _p(pos), _p(vel), _p(force), _p(eps), _p(ds), _p(body)))
         return dict(pos=pos, vel=vel, force=force, epsilon=eps, ds=ds, body=body)
+
+    def support(self) -> Dict[str, np.ndarray]:
+        n = self.n_markers
+        ns = np.empty(n, dtype=np.int32)
+        si, sj = np.empty((n, 9), dtype=np.int32), np.empty((n, 9), dtype=np.int32)
+        sd = np.empty((n, 9))
+        _check(lib().life_case_get_support(self._h, _p(ns), _p(si), _p(sj), _p(sd)))
+        return dict(nsupp=ns, si=si, sj=sj, sd=sd)
 
     def bodies(self) -> Dict[str, np.ndarray]:
         nb = self.n_bodies

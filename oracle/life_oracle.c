@@ -490,6 +490,31 @@ static void convective_speed(OracleCase* c) {
 
 #define SWAPP(a, b) do { double* _t = (a); (a) = (b); (b) = _t; } while (0)
 
+/* BGK stream-collide for one site with loop invariants hoisted into locals
+ * (same arithmetic as stream_collide's BGK branch). */
+static inline void stream_collide_bgk(int i, int j, int Nx, int Ny, double omega, const double* w,
+                                      const double* restrict fn, const double* restrict rn,
+                                      const double* restrict un, const double* restrict fxy,
+                                      const double* restrict fib, double* restrict f) {
+    const int id = i * Ny + j;
+    const double ux = un[id * 2 + 0], uy = un[id * 2 + 1], rho = rn[id];
+    const double Fx = fxy[id * 2 + 0] + fib[id * 2 + 0];
+    const double Fy = fxy[id * 2 + 1] + fib[id * 2 + 1];
+    for (int v = 0; v < NV; v++) {
+        const int cx = CX[v], cy = CY[v];
+        const double feq = rho * w[v] *
+                           (1.0 + 3.0 * (cx * ux + cy * uy) +
+                            4.5 * (SQ(ux) * (SQ(cx) - 1.0 / 3.0) + SQ(uy) * (SQ(cy) - 1.0 / 3.0)) +
+                            9.0 * cx * cy * ux * uy);
+        const double F = 3.0 * w[v] *
+                         (Fx * (cx - ux + cx * 3.0 * (cx * ux + cy * uy)) +
+                          (Fy * (cy - uy + cy * 3.0 * (cx * ux + cy * uy))));
+        const double fv = fn[id * NV + v];
+        const int recv = ((i + cx + Nx) % Nx) * Ny + ((j + cy + Ny) % Ny);
+        f[recv * NV + v] = fv + omega * (feq - fv) + (1.0 - 0.5 * omega) * F;
+    }
+}
+
 /* GridClass::lbmKernel (src/Grid.cpp:36-100) */
 static void lbm_kernel(OracleCase* c) {
     const int Nx = c->Nx, Ny = c->Ny;
@@ -508,11 +533,23 @@ static void lbm_kernel(OracleCase* c) {
             c->force_xy[id * 2 + 1] = (c->rho_n[id] * c->Drho * p->gravityY + p->dpdy * ph) * sc / c->Dm;
         }
     }
+    const int bgk = !c->p.central_moments;
+    const double omega = c->omega;
+    const double* w = c->w;
+    const double* restrict fn = c->f_n;
+    const double* restrict rn = c->rho_n;
+    const double* restrict un = c->u_n;
+    const double* restrict fxy = c->force_xy;
+    const double* restrict fib = c->force_ibm;
+    double* restrict fo = c->f;
 #pragma omp parallel
     {
 #pragma omp for schedule(guided) collapse(2)
         for (int i = 0; i < Nx; i++)
-            for (int j = 0; j < Ny; j++) stream_collide(c, i, j, i * Ny + j);
+            for (int j = 0; j < Ny; j++) {
+                if (bgk) stream_collide_bgk(i, j, Nx, Ny, omega, w, fn, rn, un, fxy, fib, fo);
+                else stream_collide(c, i, j, i * Ny + j);
+            }
 #pragma omp for schedule(guided)
         for (int id = 0; id < Nx * Ny; id++)
             if (c->type[id] == LIFE_FLUID) macroscopic(c, id);
