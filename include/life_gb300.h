@@ -185,6 +185,21 @@ int life_case_get_support(LifeCase* c, int32_t* nsupp, int32_t* si, int32_t* sj,
 int life_ibm_epsilon(const double* pos, const int32_t* nsupp, const int32_t* si, const int32_t* sj,
                      const double* sd, const double* ds, int32_t n, double Dx, double* eps, void* stream);
 
+/* life_ibm_epsilon without any device allocation. No counterpart in the
+ * reference (which has no GPU memory to manage): it exists for callers that
+ * cannot call cudaMalloc, because their device memory all comes from another
+ * allocator's pool or because cudaMalloc/cudaFree's implicit device
+ * synchronisation is not allowed where they run. The n x n system lives in a
+ * library-owned static device array sized for at most 256 markers (516 KiB,
+ * held on every GPU that loads the library until exit); larger n is rejected
+ * with LIFE_ERR_INVALID. All calls share that array, so calls that overlap on
+ * the GPU race; the caller must order them. The first call on each device
+ * looks up the array's device address, and should come before any stream
+ * capture on that device. Same arguments and result as life_ibm_epsilon. */
+int life_ibm_epsilon_noalloc(const double* pos, const int32_t* nsupp, const int32_t* si, const int32_t* sj,
+                             const double* sd, const double* ds, int32_t n, double Dx, double* eps,
+                             void* stream);
+
 /* FEM state of flexible body k (in body order): each array has 3*n_fem_nodes
  * entries, or n_el / n_node entries for the element and node arrays.
  * The set mirrors FEM.restart (src/Objects.cpp:1289-1362). */

@@ -44,6 +44,7 @@ UNITS: List[Tuple[str, List[str]]] = [
     ("life_case.cu", ["--fmad=false"]),
     ("ibm_host.cu", ["--fmad=false"]),
     ("fem_host.cu", ["--fmad=false"]),
+    ("ibm_noalloc.cu", ["--fmad=false"]),
     ("objects.cpp", []),
 ]
 

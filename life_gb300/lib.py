@@ -50,6 +50,8 @@ SIGNATURES = {
     "life_case_get_support": (C.c_int, [C.c_void_p, _ip, _ip, _ip, _dp]),
     "life_ibm_epsilon": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_int32, C.c_double, C.c_void_p, C.c_void_p]),
+    "life_ibm_epsilon_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_int32, C.c_double, C.c_void_p, C.c_void_p]),
 }
 
 
