@@ -59,6 +59,22 @@ def cylinder_params(precision: int):
     return p, [Circle(x=200.0, y=200.0, radius=20.0)]
 
 
+def filament_params(precision: int):
+    """Flexible filament channel: 1200 x 400 BGK, inlet 0.05, convective outlet,
+    one filament L = 80 clamped at (300, 200), 80 corotational elements,
+    EI/(rho U^2 L^3) = 0.2 (E = 3072 with H = 1), mass ratio 0.5 (rho_s = 40),
+    Re = 100 on L (tau = 0.62), initial tip deflection 0.03 L."""
+    from life_gb300.case import CONVECTIVE, VELOCITY, WALL, CaseParams, Filament
+    omega = 1.0 / 0.62
+    cs = 1.0 / (3.0 ** 0.5)
+    nu = (1.0 / omega - 0.5) * (cs * cs)
+    p = CaseParams(Nx=1200, Ny=400, height_p=399.0, rho_p=1.0, nu_p=nu, omega=omega,
+                   wall_left=VELOCITY, wall_right=CONVECTIVE, wall_bottom=WALL, wall_top=WALL,
+                   uxInlet_p=0.05, precision=precision, ref_L=80.0, initial_deflect=0.03, subTol=1e-8)
+    return p, [Filament(x=300.0, y=200.0, length=80.0, height=1.0, angle_deg=0.0, flexible=True,
+                        n_elements=80, clamped=True, rho=40.0, E=3072.0)]
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -243,7 +259,8 @@ def run_gb300(args, world, rank, local):
             extras[f"{name}_velocity_rel_err"] = float(np.abs(u - u64).max() / umax)
         extras["error_after_steps"] = done
         del c64, c16, u64
-        # ---- rigid cylinder channel (1000 x 400, CM, IBM), FP64 and FP32
+        # ---- rigid cylinder channel (1000 x 400, CM, IBM) and flexible
+        # filament channel (1200 x 400, BGK, FEM), FP64 and FP32
         for prec, tag in ((PREC_F64, "fp64"), (PREC_F32, "fp32")):
             p, b = cylinder_params(prec)
             cc = Case(p, b)
@@ -251,6 +268,15 @@ def run_gb300(args, world, rank, local):
             tt, _, _ = cc.bench_steps(200)
             extras[f"cylinder_1000x400_cm_{tag}_mlups"] = round(1000 * 400 * 200 / (tt * 1e-3) / 1e6, 1)
             del cc
+            p, b = filament_params(prec)
+            cf = Case(p, b)
+            cf.step(args.warmup)
+            tt, _, _ = cf.bench_steps(50)
+            st = cf.status()
+            extras[f"filament_1200x400_bgk_{tag}_mlups"] = round(1200 * 400 * 50 / (tt * 1e-3) / 1e6, 1)
+            extras[f"filament_1200x400_bgk_{tag}_ms_per_step"] = round(tt / 50, 3)
+            extras["filament_subiterations_last_step"] = st.last_subits
+            del cf
 
     # ---- end to end through the C-ABI: create from params (host), K steps,
     # read the velocity field back to host memory

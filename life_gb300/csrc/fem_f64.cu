@@ -636,7 +636,6 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
     }
 }
 
-// ObjectsClass::femKernel sums + loop condition + next relaxation factor.
 // Standalone epsilon solve over n markers with caller-provided scratch
 // (A: n*n, b: n, piv, lmax: n).
 __global__ void __launch_bounds__(256) k_epsilon_markers(FsiDev F, MarkerDev M, int n, double* A, double* b, int* piv,
@@ -652,7 +651,9 @@ cudaError_t launch_epsilon_markers(const MarkerDev& M, int n, double Dx, double*
     return cudaGetLastError();
 }
 
-__global__ void k_fsi_residual(FsiDev F) {
+// ObjectsClass::femKernel sums + loop condition + next relaxation factor.
+// Inside the captured loop graph the condition also drives the WHILE node.
+__global__ void k_fsi_residual(FsiDev F, cudaGraphConditionalHandle cond, int use_cond) {
     if (threadIdx.x != 0) return;
     FsiScalars& S = *F.s;
     double res = 0.0, num = 0.0, den = 0.0;
@@ -679,6 +680,7 @@ __global__ void k_fsi_residual(FsiDev F) {
         if (atomicCAS(&F.status[0], 0, LIFE_ERR_SUBITER) == 0) F.status[1] = S.t;
     }
     *F.cont = cont;
+    if (use_cond) cudaGraphSetConditional(cond, cont ? 1u : 0u);
 }
 
 __global__ void k_fsi_begin(FsiDev F, int t) {
@@ -693,15 +695,16 @@ cudaError_t launch_fsi_begin(const FsiDev& F, int t, cudaStream_t s) {
 }
 
 cudaError_t launch_fsi_subiteration(const FsiDev& F, const MarkerDev& M, const void* P, const LatDev& L, int t,
-                                    double velScale, cudaStream_t s, int* launches) {
+                                    double velScale, cudaStream_t s, int* launches,
+                                    const cudaGraphConditionalHandle* cond) {
     k_fsi_predict<<<F.nFlex, 256, 0, s>>>(F, M);
     k_fsi_support<<<(F.nFlexMarkers + 127) / 128, 128, 0, s>>>(F, M);
     if (F.uni) k_fsi_epsilon_uni<<<1, 256, 0, s>>>(F, M);
     else k_fsi_epsilon_body<<<F.nFlex, 256, 0, s>>>(F, M);
-    cudaError_t e = launch_ibm_interp(P, L, t, M, velScale, s);
+    cudaError_t e = launch_ibm_interp(P, L, t, M, velScale, s, cond ? &F.s->t : nullptr);
     if (e != cudaSuccess) return e;
     k_fem_dynamic<<<F.nFlex, 256, 0, s>>>(F, M);
-    k_fsi_residual<<<1, 32, 0, s>>>(F);
+    k_fsi_residual<<<1, 32, 0, s>>>(F, cond ? *cond : cudaGraphConditionalHandle{}, cond ? 1 : 0);
     if (launches) *launches += 6;
     return cudaGetLastError();
 }

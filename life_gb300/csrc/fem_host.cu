@@ -3,6 +3,7 @@
 // objectKernel, reference src/Objects.cpp:26-60) and the FEM accessors.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -12,11 +13,21 @@
 using namespace life;
 
 namespace life {
+// The subiteration loop of one step captured as a graph: a WHILE node whose
+// body is one subiteration's kernels; the residual kernel sets the condition.
+// Kernel arguments are fixed at capture, so one graph exists per
+// (population buffer, parity of t) combination the case uses.
+struct FsiGraph {
+    cudaGraphExec_t exec = nullptr;
+};
 struct FemHost {
     FsiDev F{};
     std::vector<FemBodyDev> bodies;   // host copies of the device records
     std::vector<int> hostBody;        // host body index of each flexible body
-    int* h_cont = nullptr;            // pinned flag
+    int* h_cont = nullptr;            // pinned flag (host-driven loop)
+    cudaStream_t cap = nullptr;       // capture stream
+    FsiGraph graph[4];
+    bool host_loop = false;           // LIFE_FSI_HOSTLOOP=1: read the flag on the host instead
 };
 }  // namespace life
 
@@ -163,6 +174,8 @@ int setup_fem(LifeCase* c) {
     F.status = c->d_status;
     if ((rc = fallocT(c, &F.cont, 1))) return rc;
     CK(cudaMallocHost(&H->h_cont, sizeof(int)));
+    CK(cudaStreamCreateWithFlags(&H->cap, cudaStreamNonBlocking));
+    if (const char* v = std::getenv("LIFE_FSI_HOSTLOOP")) H->host_loop = (v[0] == '1');
     F.Dx = c->Dx;
     F.Dt = c->Dt;
     F.Dm = c->Dm;
@@ -181,9 +194,39 @@ int setup_fem(LifeCase* c) {
 void life::free_fem(LifeCase* c) {
     FemHost* H = fem_of(c);
     if (!H) return;
+    for (auto& g : H->graph)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (H->cap) cudaStreamDestroy(H->cap);
     if (H->h_cont) cudaFreeHost(H->h_cont);
     delete H;
     c->fem = nullptr;
+}
+
+static int build_fsi_graph(LifeCase* c, FemHost* H, int key, int t, const void* A, const LatDev& L) {
+    cudaGraph_t graph = nullptr;
+    CK(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+    if (e == cudaSuccess) {
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(H->cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t el = launch_fsi_subiteration(H->F, c->M, A, L, t, c->Dt / c->Dx, H->cap, nullptr, &h);
+            e = cudaStreamEndCapture(H->cap, &body);
+            if (el != cudaSuccess) e = el;
+        }
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&H->graph[key].exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "FSI loop graph");
+    return LIFE_OK;
 }
 
 // The subiteration loop of one step; the spread follows in ibm_step().
@@ -192,6 +235,15 @@ int fem_fsi_loop(LifeCase* c, int t, const void* A, const LatDev& L) {
     cudaError_t e = launch_fsi_begin(H->F, t, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "fsi_begin");
     c->ibm_launches += 1;
+    if (!H->host_loop) {
+        const int key = (A == c->P[0] ? 0 : 2) + (t & 1);
+        if (!H->graph[key].exec)
+            if (int rc = build_fsi_graph(c, H, key, t, A, L)) return rc;
+        e = cudaGraphLaunch(H->graph[key].exec, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "FSI loop graph launch");
+        c->ibm_launches += 1;
+        return LIFE_OK;
+    }
     for (int it = 0; it < 20; it++) {
         e = launch_fsi_subiteration(H->F, c->M, A, L, t, c->Dt / c->Dx, c->stream, &c->ibm_launches);
         if (e != cudaSuccess) return cuda_fail(e, "fsi_subiteration");

@@ -70,8 +70,12 @@ struct FsiDev {
     int Nx, Ny;
 };
 
+// One subiteration's kernels. With `cond`, the launch is being captured into
+// the body of a WHILE graph node and the residual kernel sets its condition;
+// the step is then read from the device (F.s->t).
 cudaError_t launch_fsi_subiteration(const FsiDev& F, const MarkerDev& M, const void* P, const LatDev& L, int t,
-                                    double velScale, cudaStream_t s, int* launches);
+                                    double velScale, cudaStream_t s, int* launches,
+                                    const cudaGraphConditionalHandle* cond = nullptr);
 cudaError_t launch_fsi_begin(const FsiDev& F, int t, cudaStream_t s);
 // Epsilon system of markers [0, n) of M into M.eps, with caller-provided scratch.
 cudaError_t launch_epsilon_markers(const MarkerDev& M, int n, double Dx, double* A, double* b, int* piv, int* lmax,

@@ -24,9 +24,11 @@ namespace life {
 constexpr int TILE = 16;
 
 template <bool CM, class S>
-__global__ void k_ibm_interp(const typename S::T* __restrict__ P, LatDev L, int t, MarkerDev M, double velScale) {
+__global__ void k_ibm_interp(const typename S::T* __restrict__ P, LatDev L, int t, MarkerDev M, double velScale,
+                             const int* __restrict__ t_dev) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= M.n) return;
+    if (t_dev) t = *t_dev;  // inside a replayed graph the step comes from the device
     double iRho = 0.0, iMx = 0.0, iMy = 0.0;
     const int ns = M.nsupp[k];
     int imin = 1 << 30, imax = -(1 << 30), jmin = 1 << 30, jmax = -(1 << 30);
@@ -165,11 +167,11 @@ struct TypedPtr {
 };
 
 cudaError_t launch_ibm_interp(const void* P, const LatDev& L, int t, const MarkerDev& M, double velScale,
-                              cudaStream_t s) {
+                              cudaStream_t s, const int* t_dev) {
     if (M.n == 0) return cudaSuccess;
     const int nb = (M.n + 127) / 128;
     TypedPtr<void> Pp{P};
-    IBM_DISPATCH(k_ibm_interp, nb, 128, Pp, L, t, M, velScale);
+    IBM_DISPATCH(k_ibm_interp, nb, 128, Pp, L, t, M, velScale, t_dev);
     return cudaGetLastError();
 }
 

@@ -36,8 +36,9 @@ struct IbmScratch {
 };
 
 // Population buffers are untyped; their element type follows L.prec.
+// With t_dev, the step is read from device memory when the kernel runs.
 cudaError_t launch_ibm_interp(const void* P, const LatDev& L, int t, const MarkerDev& M, double velScale,
-                              cudaStream_t s);
+                              cudaStream_t s, const int* t_dev = nullptr);
 cudaError_t launch_ibm_spread(const void* A, void* B, const LatDev& L, int t, const MarkerDev& M,
                               const IbmScratch& W, cudaStream_t s);
 

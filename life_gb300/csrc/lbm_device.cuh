@@ -185,7 +185,7 @@ __device__ __forceinline__ void collide_cm(const double f[9], double rho, double
 // step t and the uniform pressure-gradient force of step t (Womersley).
 __device__ __forceinline__ void force_xy_at(const LatDev& L, int t, double& Fx, double& Fy) {
     if (L.womersley) {
-        const StepScalars& s = L.steps[t - L.t_base];
+        const StepScalars& s = L.steps[t % L.steps_cap];
         Fx = s.fx;
         Fy = s.fy;
     } else {
@@ -281,7 +281,7 @@ __device__ __forceinline__ void site_state(const typename S::T* __restrict__ P, 
             double r1 = 0.0, r2 = 0.0;
             const bool corner = (nx != 0 && ny != 0);
             if (type == LIFE_VELOCITY) {
-                const double ramp = L.steps[t - L.t_base].ramp;
+                const double ramp = L.steps[t % L.steps_cap].ramp;
                 un[0] = L.u_in[j * 2 + 0] * ramp;
                 un[1] = L.u_in[j * 2 + 1] * ramp;
             } else if (type == LIFE_FREESLIP || type == LIFE_PRESSURE) {

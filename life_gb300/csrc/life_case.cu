@@ -65,16 +65,13 @@ static int dev_alloc_t(LifeCase* c, T** p, size_t count) {
 // Per-step scalars for absolute steps [t0, t0+n): inlet ramp
 // (GridClass::getRampCoefficient, src/Grid.cpp:548-556) and the Womersley force
 // (src/Grid.cpp:52-62), both with the C library's cos() as in the reference.
+// The table is a ring of kStepRing entries (step t at t % kStepRing) with a
+// fixed address, so captured graphs stay valid; n must not exceed the ring.
 int life::ensure_steps(LifeCase* c, int t0, int n) {
-    if (n > c->steps_cap) {
-        if (c->d_steps) {
-            cudaFree(c->d_steps);
-            for (auto& p : c->allocs)
-                if (p == c->d_steps) p = nullptr;
-        }
-        int cap = n < 1024 ? 1024 : n;
-        if (int rc = dev_alloc_t(c, &c->d_steps, (size_t)cap)) return rc;
-        c->steps_cap = cap;
+    if (n > kStepRing) return set_error(LIFE_ERR_INVALID, "step table request larger than its ring");
+    if (!c->d_steps) {
+        if (int rc = dev_alloc_t(c, &c->d_steps, (size_t)kStepRing)) return rc;
+        c->steps_cap = kStepRing;
     }
     const LifeCaseParams& p = c->p;
     std::vector<StepScalars> h(n);
@@ -92,9 +89,14 @@ int life::ensure_steps(LifeCase* c, int t0, int n) {
         }
         h[k] = s;
     }
-    CK(cudaMemcpyAsync(c->d_steps, h.data(), sizeof(StepScalars) * n, cudaMemcpyHostToDevice, c->stream));
+    // copy in at most two contiguous pieces of the ring
+    const int first = t0 % kStepRing;
+    const int n1 = n < kStepRing - first ? n : kStepRing - first;
+    CK(cudaMemcpyAsync(c->d_steps + first, h.data(), sizeof(StepScalars) * n1, cudaMemcpyHostToDevice, c->stream));
+    if (n1 < n)
+        CK(cudaMemcpyAsync(c->d_steps, h.data() + n1, sizeof(StepScalars) * (n - n1), cudaMemcpyHostToDevice,
+                           c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    c->t_base = t0;
     c->steps_n = n;
     return LIFE_OK;
 }
@@ -121,7 +123,7 @@ LatDev life::lattice_view(const LifeCase* c, int t) {
     L.u0x = c->u0x;
     L.u0y = c->u0y;
     L.init_mode = c->init_mode;
-    L.t_base = c->t_base;
+    L.steps_cap = kStepRing;
     L.steps = c->d_steps;
     L.u_in = c->d_u_in;
     L.rho_in = c->d_rho_in;
@@ -322,11 +324,15 @@ struct StepTiming {
 };
 
 static int run_steps(LifeCase* c, int nsteps, StepTiming* tm) {
-    int rc = ensure_steps(c, c->t, nsteps + 2);
+    int rc = ensure_steps(c, c->t, (nsteps < kStepChunk ? nsteps : kStepChunk) + 2);
     if (rc) return rc;
     const bool conv = c->p.wall_right == LIFE_CONVECTIVE;
     if (tm) cudaEventRecord(tm->start, c->stream);
     for (int k = 0; k < nsteps; k++) {
+        if (k > 0 && k % kStepChunk == 0) {
+            const int left = nsteps - k;
+            if ((rc = ensure_steps(c, c->t, (left < kStepChunk ? left : kStepChunk) + 2))) return rc;
+        }
         const int tt = c->t + 1;
         LatDev L = lattice_view(c, tt);
         const void* A = c->P[c->cur];

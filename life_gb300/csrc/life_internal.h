@@ -12,6 +12,9 @@
 
 namespace life {
 
+constexpr int kStepRing = 4096;   // entries of the per-step scalar ring
+constexpr int kStepChunk = 2048;  // steps per table refill (< kStepRing - 2)
+
 // FSI loop scalars kept on the device (ObjectsClass members subIt, relax,
 // subRes, subNum, subDen; reference inc/Objects.h:66-71).
 struct FsiScalars {
@@ -48,7 +51,7 @@ struct LifeCase {
     double* d_u_in = nullptr;
     double* d_rho_in = nullptr;
     life::StepScalars* d_steps = nullptr;
-    int steps_cap = 0, steps_n = 0, t_base = 0;
+    int steps_cap = 0, steps_n = 0;
     double* d_outlet_u = nullptr;
     double* d_outlet_f[2] = {nullptr, nullptr};
     double* d_delU = nullptr;

@@ -32,7 +32,7 @@ struct LatDev {
     double Fx0, Fy0;      // constant force_xy (reference src/Grid.cpp:1035-1045)
     double u0x, u0y;      // initial uniform velocity (ux0_p*Dt/Dx, uy0_p*Dt/Dx)
     int init_mode;        // 0: zero velocity (ramp), 1: inlet profile, 2: uniform u0
-    int t_base;           // steps[t - t_base]
+    int steps_cap;        // steps[] is a ring: time step t lives at t % steps_cap
     const StepScalars* steps;
     const double* u_in;   // [Ny][2] inlet profile
     const double* rho_in; // [Ny]

@@ -82,3 +82,25 @@ def test_fsi_run_matches_oracle_and_reference(name):
         assert np.abs(fem[k]["pos"] - femo[k]["pos"]).max() < 1e-11
     assert st.code == 0
     print(name, {f"{a}:{b}": f"{v:.2e}" for (a, b), v in report.items()}, "subits", st.last_subits)
+
+
+def test_graph_loop_equals_host_driven_loop():
+    """The FSI loop replayed as a CUDA graph (WHILE node set from the device)
+    gives the same bits as the host-driven loop that reads the flag each
+    subiteration."""
+    import subprocess
+    import sys
+    code = ("import sys, numpy as np; sys.path.insert(0, 'tests/golden'); sys.path.insert(0, '.');"
+            "from cases import golden_cases; from life_gb300.lib import Case;"
+            "p, b = golden_cases()['honami_like_cm']; c = Case(p, b); c.step(60);"
+            "f = c.fields(); m = c.markers();"
+            "np.save(sys.argv[1], np.concatenate([f['f'].ravel(), m['pos'].ravel(), m['force'].ravel()]))")
+    import os
+    import tempfile
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    with tempfile.TemporaryDirectory() as td:
+        a, h = os.path.join(td, "graph.npy"), os.path.join(td, "host.npy")
+        subprocess.run([sys.executable, "-c", code, a], cwd=root, check=True)
+        subprocess.run([sys.executable, "-c", code, h], cwd=root, check=True,
+                       env=dict(os.environ, LIFE_FSI_HOSTLOOP="1"))
+        assert np.array_equal(np.load(a), np.load(h))
