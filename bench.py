@@ -208,6 +208,33 @@ def run_reference(args, world, rank):
     return 0
 
 
+def run_workload(args, world, rank):
+    """Single-workload timing (--workload cylinder|filament): FP64 and FP32
+    MLUPS of one IBM case, used for profiling the immersed-body path."""
+    from life_gb300.build import build
+    from life_gb300.case import PREC_F32, PREC_F64
+    build()
+    from life_gb300.lib import Case
+    make = cylinder_params if args.workload == "cylinder" else filament_params
+    out = {"workload": args.workload}
+    for prec, tag in ((PREC_F64, "fp64"), (PREC_F32, "fp32")):
+        p, b = make(prec)
+        c = Case(p, b)
+        c.step(args.warmup)
+        tt, inner, launches = c.bench_steps(args.steps)
+        st = c.status()
+        out[f"{tag}_mlups"] = round(p.Nx * p.Ny * args.steps / (tt * 1e-3) / 1e6, 1)
+        out[f"{tag}_ms_per_step"] = round(tt / args.steps, 4)
+        out[f"{tag}_lattice_ms"] = round(inner, 4)
+        out[f"{tag}_launches_per_step"] = launches / args.steps
+        out["last_subiterations"] = st.last_subits
+        out["last_nr_iterations"] = st.last_nr_its
+        del c
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_gb300(args, world, rank, local):
     import numpy as np
     from life_gb300.build import build
@@ -337,6 +364,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nx", type=int, default=4096)
     ap.add_argument("--quick", action="store_true", help="headline measurement only")
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "cylinder", "filament"],
+                    help="cavity: the headline line; cylinder/filament: timing of one IBM case")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -344,6 +373,8 @@ def main():
     try:
         if args.impl == "reference":
             return run_reference(args, world, rank)
+        if args.workload != "cavity":
+            return run_workload(args, world, rank)
         return run_gb300(args, world, rank, local)
     finally:
         if world > 1:

@@ -385,55 +385,201 @@ __device__ void warp_lu_solve(const double* A_, int dim, int bc, int kl, int ku,
     __syncwarp();
 }
 
+
+// ---------------------------------------------------------------------------
+// Band LU in shared memory with the dense textbook arithmetic.
+//
+// M is nn x nn with kl sub- and ku super-diagonals; row i of Bd holds M(i, c)
+// for c in [i-kl, i+kl+ku] at Bd[i*W + c - i + kl], W = 2*kl + ku + 1. The
+// factorisation performs exactly the operations of the dense unblocked LU
+// (first maximal pivot, reciprocal scaling, rank-1 update; band_lu.h), but
+// like LAPACK's banded routine it does not move the multipliers of earlier
+// columns when it swaps rows. The dense transposed solve reads each
+// multiplier from the row where the later swaps would have carried it; the
+// solve below follows each multiplier to that final row (Fp, updated swap by
+// swap from the last step back), so it forms the same products and sums
+// them in the same order as the dense solve. Results are bit-identical.
+__device__ __forceinline__ double& bd(double* Bd, int W, int kl, int i, int c) { return Bd[i * W + c - i + kl]; }
+
+__device__ void band_factor_smem(double* Bd, int nn, int kl, int ku, int W, int* piv) {
+    const int lane = threadIdx.x & 31;
+    for (int j = 0; j < nn; j++) {
+        const int imax = j + kl < nn - 1 ? j + kl : nn - 1;
+        const int kmax = j + kl + ku < nn - 1 ? j + kl + ku : nn - 1;
+        int best = j;
+        double bval = -1.0;
+        for (int i0 = j; i0 <= imax; i0 += 32) {
+            const int i = i0 + lane;
+            double va = -1.0;
+            int vi = i;
+            if (i <= imax) va = fabs(bd(Bd, W, kl, i, j));
+            for (int o = 16; o > 0; o >>= 1) {
+                const double oa = __shfl_down_sync(0xffffffffu, va, o);
+                const int oi = __shfl_down_sync(0xffffffffu, vi, o);
+                if (oa > va || (oa == va && oi < vi)) { va = oa; vi = oi; }
+            }
+            va = __shfl_sync(0xffffffffu, va, 0);
+            vi = __shfl_sync(0xffffffffu, vi, 0);
+            if (va > bval) { bval = va; best = vi; }
+        }
+        const int jp = best;
+        if (lane == 0) piv[j] = jp;
+        if (bd(Bd, W, kl, jp, j) != 0.0) {
+            if (jp != j)
+                for (int c = j + lane; c <= kmax; c += 32) {
+                    const double t = bd(Bd, W, kl, j, c);
+                    bd(Bd, W, kl, j, c) = bd(Bd, W, kl, jp, c);
+                    bd(Bd, W, kl, jp, c) = t;
+                }
+            __syncwarp();
+            const double r = 1.0 / bd(Bd, W, kl, j, j);
+            for (int i = j + 1 + lane; i <= imax; i += 32) bd(Bd, W, kl, i, j) *= r;
+        }
+        __syncwarp();
+        const int rows = imax - j, cols = kmax - j;
+        for (int q = lane; q < rows * cols; q += 32) {
+            const int i = j + 1 + q % rows, k = j + 1 + q / rows;
+            const double t = -bd(Bd, W, kl, j, k);
+            bd(Bd, W, kl, i, k) += bd(Bd, W, kl, i, j) * t;
+        }
+        __syncwarp();
+    }
+}
+
+// Transposed solve M^T x = y in place (one lane); Fp is nn ints of scratch.
+__device__ void band_solve_smem(double* Bd, int nn, int kl, int ku, int W, const int* piv, int* Fp, double* y) {
+    const int w = kl + ku;
+    for (int i = 0; i < nn; i++) {
+        double t = y[i];
+        for (int k = (i - w > 0 ? i - w : 0); k < i; k++) t -= bd(Bd, W, kl, k, i) * y[k];
+        y[i] = t / bd(Bd, W, kl, i, i);
+    }
+    for (int r = 0; r < nn; r++) Fp[r] = r;
+    int fk[32];
+    double fv[32];
+    for (int i = nn - 1; i >= 0; i--) {
+        const int rmax = i + kl < nn - 1 ? i + kl : nn - 1;
+        int m = 0;
+        for (int r = i + 1; r <= rmax; r++) {
+            const int k = Fp[r];
+            const double v = bd(Bd, W, kl, r, i);
+            int q = m++;
+            while (q > 0 && fk[q - 1] > k) {
+                fk[q] = fk[q - 1];
+                fv[q] = fv[q - 1];
+                q--;
+            }
+            fk[q] = k;
+            fv[q] = v;
+        }
+        double t = y[i];
+        for (int q = 0; q < m; q++) t -= fv[q] * y[fk[q]];
+        y[i] = t;
+        const int p = piv[i];
+        const int tmp = Fp[i];
+        Fp[i] = Fp[p];
+        Fp[p] = tmp;
+    }
+    for (int i = nn - 1; i >= 0; i--)
+        if (piv[i] != i) {
+            const double t = y[i];
+            y[i] = y[piv[i]];
+            y[piv[i]] = t;
+        }
+}
+
 // Epsilon system of a contiguous marker range [m0, m0+dim) (ObjectsClass::
-// computeEpsilon, src/Objects.cpp:264-311).
+// computeEpsilon, src/Objects.cpp:264-311). Markers interact only when both
+// coordinates are within 3 lattice units (the support is +-1.5); those pairs
+// set the band of the system. If that band fits in `smem` (smem_doubles
+// entries) the system is assembled and solved there; otherwise it is built
+// densely in A (global) and solved with band-limited loops.
+__device__ __forceinline__ bool eps_near(const MarkerDev& M, int ki, int kj, double Dx) {
+    return fabs(M.pos[ki * 2] - M.pos[kj * 2]) / Dx < 3.0 && fabs(M.pos[ki * 2 + 1] - M.pos[kj * 2 + 1]) / Dx < 3.0;
+}
+
+__device__ __forceinline__ double eps_entry(const MarkerDev& M, int ki, int kj, double Dx) {
+    const double xj = M.pos[kj * 2], yj = M.pos[kj * 2 + 1];
+    double acc = 0.0;
+    const int ns = M.nsupp[ki];
+    for (int s = 0; s < ns; s++) {
+        const double dvi = M.sd[ki * 9 + s];
+        const double dX = fabs(xj / Dx - M.si[ki * 9 + s]);
+        const double dY = fabs(yj / Dx - M.sj[ki * 9 + s]);
+        acc += dvi * (dirac_d(dX) * dirac_d(dY));
+    }
+    return acc * (1.0 * 1.0 * M.ds[kj]);
+}
+
 __device__ void epsilon_range(const FsiDev& F, const MarkerDev& M, int m0, int dim, double* A, double* bx, int* piv,
-                              int* lmax) {
+                              int* lmax, double* smem = nullptr, int smem_doubles = 0) {
     __shared__ int s_kl, s_ku;
     if (threadIdx.x == 0) { s_kl = 0; s_ku = 0; }
-    for (long long p = threadIdx.x; p < (long long)dim * dim; p += blockDim.x) A[p] = 0.0;
     __syncthreads();
     const double Dx = F.Dx;
+    // bandwidths of the LU's view M = A^T: A[i][j] sits at M(j, i)
     for (long long p = threadIdx.x; p < (long long)dim * dim; p += blockDim.x) {
         const int i = (int)(p / dim), j = (int)(p % dim);
-        const int ki = m0 + i, kj = m0 + j;
-        const double xj = M.pos[kj * 2], yj = M.pos[kj * 2 + 1];
-        if (fabs(M.pos[ki * 2] - xj) / Dx < 3.0 && fabs(M.pos[ki * 2 + 1] - yj) / Dx < 3.0) {
-            double acc = 0.0;
-            const int ns = M.nsupp[ki];
-            for (int s = 0; s < ns; s++) {
-                const double dvi = M.sd[ki * 9 + s];
-                const double dX = fabs(xj / Dx - M.si[ki * 9 + s]);
-                const double dY = fabs(yj / Dx - M.sj[ki * 9 + s]);
-                acc += dvi * (dirac_d(dX) * dirac_d(dY));
-            }
-            const double a = acc * (1.0 * 1.0 * M.ds[kj]);
-            A[p] = a;
-            if (a != 0.0) {
-                // M = A^T: entry A[i][j] is M(j, i)
-                if (j - i > 0) atomicMax(&s_kl, j - i);
-                if (i - j > 0) atomicMax(&s_ku, i - j);
-            }
+        if (i != j && eps_near(M, m0 + i, m0 + j, Dx)) {
+            if (j > i) atomicMax(&s_kl, j - i);
+            else atomicMax(&s_ku, i - j);
         }
+    }
+    __syncthreads();
+    const int kl = s_kl, ku = s_ku, W = 2 * kl + ku + 1;
+    const long long need = (long long)dim * W + dim + dim;  // band, y, two int arrays
+    if (smem && kl < 32 && need <= smem_doubles) {
+        double* Bd = smem;
+        double* y = Bd + (size_t)dim * W;
+        int* sp = reinterpret_cast<int*>(y + dim);
+        int* fp = sp + dim;
+        for (long long q = threadIdx.x; q < (long long)dim * W; q += blockDim.x) Bd[q] = 0.0;
+        for (int i = threadIdx.x; i < dim; i += blockDim.x) y[i] = 1.0;
+        __syncthreads();
+        const int bw = kl > ku ? kl : ku;
+        for (long long p = threadIdx.x; p < (long long)dim * dim; p += blockDim.x) {
+            const int i = (int)(p / dim), j = (int)(p % dim);
+            if (j - i > bw || i - j > bw) continue;
+            if (eps_near(M, m0 + i, m0 + j, Dx)) bd(Bd, W, kl, j, i) = eps_entry(M, m0 + i, m0 + j, Dx);
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            band_factor_smem(Bd, dim, kl, ku, W, sp);
+            if (threadIdx.x == 0) band_solve_smem(Bd, dim, kl, ku, W, sp, fp, y);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < dim; i += blockDim.x) M.eps[m0 + i] = y[i];
+        __syncthreads();
+        return;
+    }
+    for (long long p = threadIdx.x; p < (long long)dim * dim; p += blockDim.x) A[p] = 0.0;
+    __syncthreads();
+    for (long long p = threadIdx.x; p < (long long)dim * dim; p += blockDim.x) {
+        const int i = (int)(p / dim), j = (int)(p % dim);
+        if (eps_near(M, m0 + i, m0 + j, Dx)) A[p] = eps_entry(M, m0 + i, m0 + j, Dx);
     }
     for (int i = threadIdx.x; i < dim; i += blockDim.x) bx[i] = 1.0;
     __syncthreads();
     if (threadIdx.x < 32) {
-        warp_lu_factor(A, dim, 0, s_kl, s_ku, piv, lmax);
-        warp_lu_solve(A, dim, 0, s_kl, s_ku, piv, lmax, bx, bx);
+        warp_lu_factor(A, dim, 0, kl, ku, piv, lmax);
+        warp_lu_solve(A, dim, 0, kl, ku, piv, lmax, bx, bx);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < dim; i += blockDim.x) M.eps[m0 + i] = bx[i];
     __syncthreads();
 }
 
+constexpr int kEpsSmemDoubles = 6000;  // 48000 bytes of dynamic shared memory
+
 __global__ void __launch_bounds__(256) k_fsi_epsilon_body(FsiDev F, MarkerDev M) {
+    extern __shared__ double eps_smem[];
     FemBodyDev& B = F.bodies[blockIdx.x];
-    epsilon_range(F, M, B.mbase, B.nMark, B.epsA, B.epsB, B.piv, B.lmax);
+    epsilon_range(F, M, B.mbase, B.nMark, B.epsA, B.epsB, B.piv, B.lmax, eps_smem, kEpsSmemDoubles);
 }
 
 __global__ void __launch_bounds__(256) k_fsi_epsilon_uni(FsiDev F, MarkerDev M) {
-    epsilon_range(F, M, 0, M.n, F.uniA, F.uniB, F.uniPiv, F.uniLmax);
+    extern __shared__ double eps_smem[];
+    epsilon_range(F, M, 0, M.n, F.uniA, F.uniB, F.uniPiv, F.uniLmax, eps_smem, kEpsSmemDoubles);
 }
 
 // FEMBodyClass::dynamicFEM (src/FEMBody.cpp:26-68) for one body per CTA.
@@ -442,6 +588,16 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
     __shared__ double s_res;
     __shared__ int s_it;
     const int n = B.n;
+    const int nn = n - B.bc;
+    constexpr int KW = 2 * 5 + 5 + 1;  // band width of the LU (kl = ku = 5)
+    extern __shared__ double fem_smem[];
+    double* sBd = fem_smem;            // [nn][KW] LU band
+    double* sMb = sBd + nn * KW;       // [n][11] mass band
+    double* sKe = sMb + n * 11;        // [n][11] stiffness band
+    double* sV = sKe + n * 11;         // [n] Newmark vector
+    double* sY = sV + n;               // [nn] right-hand side / solution
+    int* sPiv = reinterpret_cast<int*>(sY + nn);
+    int* sFp = sPiv + nn;
     {
         double* U = vec(B, V_U);
         double* Ud = vec(B, V_Udot);
@@ -500,7 +656,6 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
     __syncthreads();
     do {
         // buildGlobalMatrices (src/FEMBody.cpp:90-109)
-        for (long long p = threadIdx.x; p < (long long)n * n; p += blockDim.x) B.K[p] = 0.0;
         for (int e = threadIdx.x; e < B.nEl; e += blockDim.x) {
             const double* el = B.el + (size_t)e * EL_STRIDE;
             const double L = el[EL_L], L0 = el[EL_L0], E = el[EL_E], A = el[EL_A], I = el[EL_I];
@@ -543,9 +698,12 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
             for (int q = 0; q < 36; q++) sc[ES_K + q] = G[q] + G2[q];
         }
         __syncthreads();
-        // ordered assembly of M, K (band |r-c| <= 5) and F
+        // Ordered assembly of M, K (band |r-c| <= 5) and F, then setNewmark
+        // (src/FEMBody.cpp:112-126): K_eff = K + a0*M goes straight into the
+        // shared-memory band of the LU's view M(i,j) = K_eff[bc+j][bc+i].
         {
             double* Fv = vec(B, V_F);
+            for (int q = threadIdx.x; q < nn * KW; q += blockDim.x) sBd[q] = 0.0;
             for (int p = threadIdx.x; p < n * 11; p += blockDim.x) {
                 const int r = p / 11, cc = r - 5 + p % 11;
                 if (cc < 0 || cc >= n) continue;
@@ -558,8 +716,8 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
                     am += sc[ES_M + li * 6 + lj];
                     ak += sc[ES_K + li * 6 + lj];
                 }
-                B.M[(size_t)r * n + cc] = am;
-                B.K[(size_t)r * n + cc] = ak;
+                sMb[p] = am;
+                sKe[p] = ak;
             }
             for (int r = threadIdx.x; r < n; r += blockDim.x) {
                 double af = 0.0;
@@ -567,35 +725,37 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
                     af += B.elscr[(size_t)e * ES_STRIDE + ES_F + (r - 3 * e)];
                 Fv[r] = af;
             }
-        }
-        __syncthreads();
-        // setNewmark (src/FEMBody.cpp:112-126)
-        {
             const double* U = vec(B, V_U);
             const double* Un = vec(B, V_Un);
             const double* Ud = vec(B, V_Udot);
             const double* Udd = vec(B, V_Udotdot);
-            double* v = vec(B, V_delU);
-            for (int i = threadIdx.x; i < n; i += blockDim.x) v[i] = a0 * (Un[i] - U[i]) + a2 * Ud[i] + a3 * Udd[i];
+            for (int i = threadIdx.x; i < n; i += blockDim.x) sV[i] = a0 * (Un[i] - U[i]) + a2 * Ud[i] + a3 * Udd[i];
             __syncthreads();
-            double* Fv = vec(B, V_F);
             const double* Rv = vec(B, V_R);
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 double mv = 0.0;
-                for (int j = (i - 5 < 0 ? 0 : i - 5); j <= i + 5 && j < n; j++) mv += B.M[(size_t)i * n + j] * v[j];
-                Fv[i] = Rv[i] - Fv[i] + mv;
+                for (int j = (i - 5 < 0 ? 0 : i - 5); j <= i + 5 && j < n; j++) mv += sMb[i * 11 + (j - i + 5)] * sV[j];
+                const double fe = Rv[i] - Fv[i] + mv;
+                Fv[i] = fe;
+                if (i >= B.bc) sY[i - B.bc] = fe;
             }
             for (int p = threadIdx.x; p < n * 11; p += blockDim.x) {
                 const int r = p / 11, cc = r - 5 + p % 11;
-                if (cc < 0 || cc >= n) continue;
-                B.K[(size_t)r * n + cc] = B.K[(size_t)r * n + cc] + a0 * B.M[(size_t)r * n + cc];
+                if (cc < B.bc || cc >= n || r < B.bc) continue;
+                const double keff = sKe[p] + a0 * sMb[p];
+                bd(sBd, KW, 5, cc - B.bc, r - B.bc) = keff;
             }
         }
         __syncthreads();
         // delU = solveLAPACK(K, F, bcDOFs) (src/Utils.cpp:288-311)
         if (threadIdx.x < 32) {
-            warp_lu_factor(B.K, n, B.bc, 5, 5, B.piv, B.lmax);
-            warp_lu_solve(B.K, n, B.bc, 5, 5, B.piv, B.lmax, vec(B, V_F), vec(B, V_delU));
+            band_factor_smem(sBd, nn, 5, 5, KW, sPiv);
+            if (threadIdx.x == 0) band_solve_smem(sBd, nn, 5, 5, KW, sPiv, sFp, sY);
+        }
+        __syncthreads();
+        {
+            double* dU = vec(B, V_delU);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) dU[i] = i < B.bc ? 0.0 : sY[i - B.bc];
         }
         __syncthreads();
         {
@@ -689,6 +849,15 @@ __global__ void k_fsi_begin(FsiDev F, int t) {
     *F.cont = 1;
 }
 
+size_t fem_dynamic_smem(int n, int bc) {
+    const int nn = n - bc;
+    return sizeof(double) * ((size_t)nn * 16 + (size_t)n * 22 + n + nn) + sizeof(int) * 2 * (size_t)nn;
+}
+
+cudaError_t fem_dynamic_configure(size_t smem) {
+    return cudaFuncSetAttribute(k_fem_dynamic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 cudaError_t launch_fsi_begin(const FsiDev& F, int t, cudaStream_t s) {
     k_fsi_begin<<<1, 1, 0, s>>>(F, t);
     return cudaGetLastError();
@@ -699,11 +868,11 @@ cudaError_t launch_fsi_subiteration(const FsiDev& F, const MarkerDev& M, const v
                                     const cudaGraphConditionalHandle* cond) {
     k_fsi_predict<<<F.nFlex, 256, 0, s>>>(F, M);
     k_fsi_support<<<(F.nFlexMarkers + 127) / 128, 128, 0, s>>>(F, M);
-    if (F.uni) k_fsi_epsilon_uni<<<1, 256, 0, s>>>(F, M);
-    else k_fsi_epsilon_body<<<F.nFlex, 256, 0, s>>>(F, M);
+    if (F.uni) k_fsi_epsilon_uni<<<1, 256, kEpsSmemDoubles * sizeof(double), s>>>(F, M);
+    else k_fsi_epsilon_body<<<F.nFlex, 256, kEpsSmemDoubles * sizeof(double), s>>>(F, M);
     cudaError_t e = launch_ibm_interp(P, L, t, M, velScale, s, cond ? &F.s->t : nullptr);
     if (e != cudaSuccess) return e;
-    k_fem_dynamic<<<F.nFlex, 256, 0, s>>>(F, M);
+    k_fem_dynamic<<<F.nFlex, 256, F.fem_smem, s>>>(F, M);
     k_fsi_residual<<<1, 32, 0, s>>>(F, cond ? *cond : cudaGraphConditionalHandle{}, cond ? 1 : 0);
     if (launches) *launches += 6;
     return cudaGetLastError();

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -170,6 +171,17 @@ int setup_fem(LifeCase* c) {
     }
     F.nFlex = (int)H->bodies.size();
     if ((rc = upload(c, &F.bodies, H->bodies))) return rc;
+    // Each FEM CTA holds its body's LU band and matrices in shared memory.
+    size_t smem = 0;
+    for (const auto& D : H->bodies) smem = std::max(smem, fem_dynamic_smem(D.n, D.bc));
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (smem > (size_t)optin)
+        return set_error(LIFE_ERR_INVALID, "a flexible body has too many elements for the shared-memory FEM solve (" +
+                                               std::to_string(smem) + " bytes needed)");
+    F.fem_smem = smem;
+    CK(fem_dynamic_configure(smem));
     F.s = c->d_fsi;
     F.status = c->d_status;
     if ((rc = fallocT(c, &F.cont, 1))) return rc;

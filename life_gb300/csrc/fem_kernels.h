@@ -68,7 +68,12 @@ struct FsiDev {
     int* cont;            // continue flag for the host loop
     double Dx, Dt, Dm, gravityX, gravityY, ref_L, alpha, delta, relaxMax, subTol;
     int Nx, Ny;
+    size_t fem_smem;      // dynamic shared memory of k_fem_dynamic (largest body)
 };
+
+// Shared memory k_fem_dynamic needs for a body of n DOFs, bc constrained.
+size_t fem_dynamic_smem(int n, int bc);
+cudaError_t fem_dynamic_configure(size_t smem);
 
 // One subiteration's kernels. With `cond`, the launch is being captured into
 // the body of a WHILE graph node and the residual kernel sets its condition;

@@ -77,6 +77,11 @@ __global__ void __launch_bounds__(256) k_ibm_spread(const typename S::T* __restr
                                                     LatDev L, int t, MarkerDev M, IbmScratch W) {
     __shared__ int list[256];
     __shared__ int warp_cnt[8];
+    // support tables and force factors of the compacted markers
+    __shared__ int s_ij[256][9];
+    __shared__ double s_d[256][9];
+    __shared__ double s_fx[256], s_fy[256];
+    __shared__ int s_ns[256];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ntiles = *W.ntiles;
     for (int q = blockIdx.x; q < ntiles; q += gridDim.x) {
@@ -100,18 +105,31 @@ __global__ void __launch_bounds__(256) k_ibm_spread(const typename S::T* __restr
                 if (w < warp) off += warp_cnt[w];
                 cnt += warp_cnt[w];
             }
-            if (hit) list[off + __popc(bal & ((1u << lane) - 1u))] = k;
+            if (hit) {
+                // stage this marker's support (site packed as j*65536 + i)
+                const int r = off + __popc(bal & ((1u << lane) - 1u));
+                list[r] = k;
+                const int ns = M.nsupp[k];
+                s_ns[r] = ns;
+                for (int s = 0; s < 9; s++) {
+                    s_ij[r][s] = s < ns ? (M.sj[k * 9 + s] << 16) | M.si[k * 9 + s] : -1;
+                    s_d[r][s] = M.sd[k * 9 + s];
+                }
+                s_fx[r] = M.force[k * 2 + 0];
+                s_fy[r] = M.force[k * 2 + 1];
+            }
             __syncthreads();
             // Marker order within the chunk is preserved by the ordered compaction.
+            const int me = (j << 16) | i;
             for (int r = 0; r < cnt; r++) {
-                const int m = list[r];
-                const int ns = M.nsupp[m];
+                const int ns = s_ns[r];
                 for (int s = 0; s < ns; s++)
-                    if (M.si[m * 9 + s] == i && M.sj[m * 9 + s] == j) {
-                        const double d = M.sd[m * 9 + s];
+                    if (s_ij[r][s] == me) {
+                        const int m = list[r];
+                        const double d = s_d[r][s];
                         const double e = M.eps[m], ds = M.ds[m];
-                        ax += M.force[m * 2 + 0] * e * ds * 1.0 * d;
-                        ay += M.force[m * 2 + 1] * e * ds * 1.0 * d;
+                        ax += s_fx[r] * e * ds * 1.0 * d;
+                        ay += s_fy[r] * e * ds * 1.0 * d;
                         touched = true;
                         break;
                     }

@@ -117,15 +117,25 @@ __global__ void k_perimeter(const typename S::T* __restrict__ A, typename S::T* 
 // a sequential sum over j, as in the reference.
 __global__ void k_outlet_f64(LatDev L, double* __restrict__ delU) {
     __shared__ double uOut_s;
+    __shared__ double col[1024];
     const int Ny = L.Ny;
     const double* u1 = L.outlet_u + (size_t)2 * Ny * 2;  // column Nx-1
     const double* u2 = L.outlet_u + (size_t)1 * Ny * 2;  // column Nx-2
     const double* u3 = L.outlet_u;                       // column Nx-3
+    // All threads stage the outlet column through shared memory; one thread
+    // then adds it up in j order.
+    double acc = 0.0;
+    for (int j0 = 0; j0 < Ny; j0 += 1024) {
+        const int m = Ny - j0 < 1024 ? Ny - j0 : 1024;
+        __syncthreads();
+        for (int j = threadIdx.x; j < m; j += blockDim.x) col[j] = u1[(j0 + j) * 2];
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int j = 0; j < m; j++) acc += col[j];
+    }
     if (threadIdx.x == 0) {
-        double uOut = 0.0;
-        for (int j = 0; j < Ny; j++) uOut += u1[j * 2];
-        uOut /= (double)Ny;
-        uOut_s = uOut;
+        acc /= (double)Ny;
+        uOut_s = acc;
     }
     __syncthreads();
     const double uOut = uOut_s;

@@ -1652,6 +1652,17 @@ int oracle_get_fem(const OracleCase* c, int k, double* U, double* Udot, double* 
     return fail(LIFE_ERR_INVALID, "oracle: no flexible body %d", k);
 }
 
+int oracle_get_nr(const OracleCase* c, int k, int* itNR, double* resNR) {
+    int q = -1;
+    for (int ib = 0; ib < c->nb; ib++)
+        if (c->b[ib].flex && ++q == k) {
+            if (itNR) *itNR = c->b[ib].fem->itNR;
+            if (resNR) *resNR = c->b[ib].fem->resNR;
+            return LIFE_OK;
+        }
+    return fail(LIFE_ERR_INVALID, "oracle: no flexible body %d", k);
+}
+
 int oracle_get_relax(const OracleCase* c, double* relax, int* subits, double* subres) {
     if (relax) *relax = c->relax;
     if (subits) *subits = c->subIt;

@@ -43,6 +43,8 @@ int oracle_get_fem(const OracleCase* c, int k, double* U, double* Udot, double* 
                    double* U_n, double* U_nm1, double* R_k, double* el_L, double* el_angle,
                    double* node_pos, double* node_angle);
 int oracle_get_relax(const OracleCase* c, double* relax, int* subits, double* subres);
+/* Newton-Raphson iterations and residual of flexible body k's last dynamicFEM. */
+int oracle_get_nr(const OracleCase* c, int k, int* itNR, double* resNR);
 /* Dense LU solve exactly as the oracle's FEM/epsilon paths use it (row-major A,
  * first bc rows/cols dropped); exposed for unit tests. */
 int oracle_solve(int dim, const double* A, const double* b, int bc, double* x);

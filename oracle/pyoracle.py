@@ -51,6 +51,7 @@ def lib() -> C.CDLL:
             L.oracle_get_fem.argtypes = [C.c_void_p, C.c_int] + [dp] * 10
             L.oracle_get_relax.argtypes = [C.c_void_p, dp, ip, dp]
             L.oracle_solve.argtypes = [C.c_int, dp, dp, C.c_int, dp]
+            L.oracle_get_nr.argtypes = [C.c_void_p, C.c_int, ip, dp]
             _lib = L
     return _lib
 
@@ -143,6 +144,11 @@ class Oracle:
         if rc:
             raise OracleError(rc, lib().oracle_last_error().decode())
         return out
+
+    def nr(self, k: int = 0):
+        it, res = C.c_int(), C.c_double()
+        lib().oracle_get_nr(self._h, k, C.byref(it), C.byref(res))
+        return it.value, res.value
 
     def relax(self):
         r, s, res = C.c_double(), C.c_int(), C.c_double()
