@@ -20,6 +20,8 @@
 // exact zero, so results are unchanged.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "band_lu.h"
 #include "fem_kernels.h"
 
@@ -248,52 +250,67 @@ __global__ void __launch_bounds__(256) k_fsi_predict(FsiDev F, MarkerDev M) {
 }
 
 // IBMNodeClass::findSupport + computeDs (src/IBMNode.cpp:139-204) for the
-// markers of flexible bodies.
-__global__ void k_fsi_support(FsiDev F, MarkerDev M) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= F.nFlexMarkers) return;
+// markers of flexible bodies, one warp per marker. Lanes 0..24 test the 5 x 5
+// lattice nodes around the nearest node, lane = 5*(i - inear + 2) + (j -
+// jnear + 2), so the ballot packs the supporting nodes in the reference's
+// loop order (i outer, j inner). The spacing ds is the minimum of sqrt(dd)/Dx
+// over the body's other markers; correctly rounded sqrt and division are
+// monotone, so it equals sqrt(min dd)/Dx, and the lanes only reduce dd.
+__global__ void __launch_bounds__(128) k_fsi_support(FsiDev F, MarkerDev M) {
+    const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (q >= F.nFlexMarkers) return;  // uniform per warp
     const int k = F.flexMarkers[q];
     const double Dx = F.Dx;
     const double px = M.pos[k * 2], py = M.pos[k * 2 + 1];
-    const int inear = (int)round(px / Dx), jnear = (int)round(py / Dx);
-    int ns = 0;
-    for (int s = 0; s < 9; s++) {
-        M.si[k * 9 + s] = 0;
-        M.sj[k * 9 + s] = 0;
-        M.sd[k * 9 + s] = 0.0;
+    const double sx = px / Dx, sy = py / Dx;
+    const int inear = (int)round(sx), jnear = (int)round(sy);
+    const int i = inear - 2 + lane / 5, j = jnear - 2 + lane % 5;
+    double dX = 0.0, dY = 0.0;
+    bool in = false;
+    if (lane < 25) {
+        dX = fabs(sx - i);
+        dY = fabs(sy - j);
+        in = dX < 1.5 && dY < 1.5 && i >= 0 && i <= F.Nx - 1 && j >= 0 && j <= F.Ny - 1;
     }
-    for (int i = inear - 2; i <= inear + 2; i++) {
-        const double dX = fabs(px / Dx - i);
-        for (int j = jnear - 2; j <= jnear + 2; j++) {
-            const double dY = fabs(py / Dx - j);
-            if (dX < 1.5 && dY < 1.5 && i >= 0 && i <= F.Nx - 1 && j >= 0 && j <= F.Ny - 1) {
-                if (ns == 9) {
-                    atomicCAS(&F.status[0], 0, LIFE_ERR_SUPPORT);
-                    continue;
-                }
-                M.si[k * 9 + ns] = i;
-                M.sj[k * 9 + ns] = j;
-                M.sd[k * 9 + ns] = dirac_d(dX) * dirac_d(dY);
-                ns++;
-            }
-        }
+    const unsigned bal = __ballot_sync(0xffffffffu, in);
+    const int slot = __popc(bal & ((1u << lane) - 1u));
+    const int total = __popc(bal);
+    if (lane < 9) {
+        M.si[k * 9 + lane] = 0;
+        M.sj[k * 9 + lane] = 0;
+        M.sd[k * 9 + lane] = 0.0;
     }
-    M.nsupp[k] = ns;
+    __syncwarp();
+    if (in && slot < 9) {
+        M.si[k * 9 + slot] = i;
+        M.sj[k * 9 + slot] = j;
+        M.sd[k * 9 + slot] = dirac_d(dX) * dirac_d(dY);
+    }
+    if (lane == 0) {
+        M.nsupp[k] = total < 9 ? total : 9;
+        if (total > 9) atomicCAS(&F.status[0], 0, LIFE_ERR_SUPPORT);
+    }
     const int b = F.markerBody[k];
     const int b0 = F.bodyStart[b], bn = F.bodyCount[b];
-    double cur = 10.0;
-    for (int n = 0; n < bn; n++) {
+    // non-negative doubles order like their bit patterns; NaN never passes dd < best
+    unsigned long long best = 0x7ff0000000000000ull;  // +inf
+    for (int n = lane; n < bn; n += 32) {
         const int o = b0 + n;
         if (o != k) {
             const double d0 = px - M.pos[o * 2], d1 = py - M.pos[o * 2 + 1];
             double dd = 0.0;
             dd += d0 * d0;
             dd += d1 * d1;
-            const double mag = sqrt(dd) / Dx;
-            if (mag < cur) cur = mag;
+            if (dd < __longlong_as_double((long long)best)) best = (unsigned long long)__double_as_longlong(dd);
         }
     }
-    M.ds[k] = cur;
+    const unsigned bh = __reduce_min_sync(0xffffffffu, (unsigned)(best >> 32));
+    const unsigned bl = __reduce_min_sync(0xffffffffu, (unsigned)(best >> 32) == bh ? (unsigned)best : 0xffffffffu);
+    if (lane == 0) {
+        const double mag = sqrt(__longlong_as_double((long long)(((unsigned long long)bh << 32) | bl))) / Dx;
+        M.ds[k] = mag < 10.0 ? mag : 10.0;
+    }
 }
 
 // Dense LU with band-limited loops (band_lu.h semantics) by one warp.
@@ -401,38 +418,40 @@ __device__ void warp_lu_solve(const double* A_, int dim, int bc, int kl, int ku,
 // them in the same order as the dense solve. Results are bit-identical.
 __device__ __forceinline__ double& bd(double* Bd, int W, int kl, int i, int c) { return Bd[i * W + c - i + kl]; }
 
+// One warp; kl <= 31. Lane l holds the candidate M(j+l, j) of column j. The
+// pivot is the first maximal magnitude (LAPACK idamax: a NaN in the first
+// place wins, later NaNs never do); magnitudes are compared as bit patterns,
+// which order like the values for non-negative doubles. Each candidate's
+// reciprocal is formed while the pivot is being chosen and the pivot's is
+// kept: the same correctly rounded 1/pivot as a division after the choice.
 __device__ void band_factor_smem(double* Bd, int nn, int kl, int ku, int W, int* piv) {
     const int lane = threadIdx.x & 31;
     for (int j = 0; j < nn; j++) {
         const int imax = j + kl < nn - 1 ? j + kl : nn - 1;
         const int kmax = j + kl + ku < nn - 1 ? j + kl + ku : nn - 1;
-        int best = j;
-        double bval = -1.0;
-        for (int i0 = j; i0 <= imax; i0 += 32) {
-            const int i = i0 + lane;
-            double va = -1.0;
-            int vi = i;
-            if (i <= imax) va = fabs(bd(Bd, W, kl, i, j));
-            for (int o = 16; o > 0; o >>= 1) {
-                const double oa = __shfl_down_sync(0xffffffffu, va, o);
-                const int oi = __shfl_down_sync(0xffffffffu, vi, o);
-                if (oa > va || (oa == va && oi < vi)) { va = oa; vi = oi; }
-            }
-            va = __shfl_sync(0xffffffffu, va, 0);
-            vi = __shfl_sync(0xffffffffu, vi, 0);
-            if (va > bval) { bval = va; best = vi; }
-        }
-        const int jp = best;
+        const bool valid = j + lane <= imax;
+        const double v = valid ? bd(Bd, W, kl, j + lane, j) : 0.0;
+        const double rc = 1.0 / v;
+        unsigned long long key = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+        if (key > 0x7ff0000000000000ull) key = lane == 0 ? ~0ull : 0ull;
+        const unsigned kh = (unsigned)(key >> 32), klo = (unsigned)key;
+        const unsigned mh = __reduce_max_sync(0xffffffffu, valid ? kh : 0u);
+        const bool c1 = valid && kh == mh;
+        const unsigned ml = __reduce_max_sync(0xffffffffu, c1 ? klo : 0u);
+        const int src = __ffs(__ballot_sync(0xffffffffu, c1 && klo == ml)) - 1;
+        const int jp = j + src;
+        const double pv = __shfl_sync(0xffffffffu, v, src);
+        const double r = __shfl_sync(0xffffffffu, rc, src);
         if (lane == 0) piv[j] = jp;
-        if (bd(Bd, W, kl, jp, j) != 0.0) {
-            if (jp != j)
+        if (pv != 0.0) {
+            if (jp != j) {
                 for (int c = j + lane; c <= kmax; c += 32) {
                     const double t = bd(Bd, W, kl, j, c);
                     bd(Bd, W, kl, j, c) = bd(Bd, W, kl, jp, c);
                     bd(Bd, W, kl, jp, c) = t;
                 }
-            __syncwarp();
-            const double r = 1.0 / bd(Bd, W, kl, j, j);
+                __syncwarp();
+            }
             for (int i = j + 1 + lane; i <= imax; i += 32) bd(Bd, W, kl, i, j) *= r;
         }
         __syncwarp();
@@ -446,7 +465,67 @@ __device__ void band_factor_smem(double* Bd, int nn, int kl, int ku, int W, int*
     }
 }
 
-// Transposed solve M^T x = y in place (one lane); Fp is nn ints of scratch.
+// Transposed solve M^T x = y in place by one warp; kl + ku <= 31, kl <= 31.
+// Forward (U^T): column-oriented. Lane r % 32 keeps the partial sum of row r;
+// when y[k] is final every row r in (k, k + kl + ku] subtracts U(k, r) y[k].
+// Each row still subtracts its terms in ascending k, as the row-oriented
+// loop does, so every sum is formed in the same order.
+// Backward (L^T): lane l forms the product of the multiplier stored in band
+// row i+1+l with y at its final row Fp[i+1+l]; the products are subtracted
+// in ascending final row, the order of the dense solve.
+__device__ void band_solve_warp(const double* Bd_, int nn, int kl, int ku, int W, const int* piv, int* Fp, double* y) {
+    double* Bd = const_cast<double*>(Bd_);
+    const int lane = threadIdx.x & 31;
+    const int w = kl + ku;
+    double t = lane < nn ? y[lane] : 0.0;
+    for (int k = 0; k < nn; k++) {
+        const int owner = k & 31;
+        const double tk = __shfl_sync(0xffffffffu, t, owner);
+        const double yk = tk / bd(Bd, W, kl, k, k);
+        if (lane == owner) {
+            y[k] = yk;
+            t = k + 32 < nn ? y[k + 32] : 0.0;
+        }
+        const int r = k + 1 + ((lane - k - 1) & 31);
+        if (r <= k + w && r < nn) t = t - bd(Bd, W, kl, k, r) * yk;
+    }
+    for (int r = lane; r < nn; r += 32) Fp[r] = r;
+    __syncwarp();
+    for (int i = nn - 1; i >= 0; i--) {
+        const int rmax = i + kl < nn - 1 ? i + kl : nn - 1;
+        const int m = rmax - i;
+        const bool act = lane < m;
+        const int fk = act ? Fp[i + 1 + lane] : 0x7fffffff;
+        const double pr = act ? bd(Bd, W, kl, i + 1 + lane, i) * y[fk] : 0.0;
+        int rank = 0;
+        for (int q = 0; q < m; q++) rank += __shfl_sync(0xffffffffu, fk, q) < fk ? 1 : 0;
+        double ti = y[i];
+        for (int q = 0; q < m; q++) {
+            const int src = __ffs(__ballot_sync(0xffffffffu, act && rank == q)) - 1;
+            ti = ti - __shfl_sync(0xffffffffu, pr, src);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            y[i] = ti;
+            const int p = piv[i];
+            const int tmp = Fp[i];
+            Fp[i] = Fp[p];
+            Fp[p] = tmp;
+        }
+        __syncwarp();
+    }
+    for (int i = nn - 1; i >= 0; i--) {
+        if (lane == 0 && piv[i] != i) {
+            const double tt = y[i];
+            y[i] = y[piv[i]];
+            y[piv[i]] = tt;
+        }
+    }
+    __syncwarp();
+}
+
+// Transposed solve M^T x = y in place (one lane, any band); Fp is nn ints of
+// scratch.
 __device__ void band_solve_smem(double* Bd, int nn, int kl, int ku, int W, const int* piv, int* Fp, double* y) {
     const int w = kl + ku;
     for (int i = 0; i < nn; i++) {
@@ -491,9 +570,7 @@ __device__ void band_solve_smem(double* Bd, int nn, int kl, int ku, int W, const
 // Epsilon system of a contiguous marker range [m0, m0+dim) (ObjectsClass::
 // computeEpsilon, src/Objects.cpp:264-311). Markers interact only when both
 // coordinates are within 3 lattice units (the support is +-1.5); those pairs
-// set the band of the system. If that band fits in `smem` (smem_doubles
-// entries) the system is assembled and solved there; otherwise it is built
-// densely in A (global) and solved with band-limited loops.
+// set the band of the system.
 __device__ __forceinline__ bool eps_near(const MarkerDev& M, int ki, int kj, double Dx) {
     return fabs(M.pos[ki * 2] - M.pos[kj * 2]) / Dx < 3.0 && fabs(M.pos[ki * 2 + 1] - M.pos[kj * 2 + 1]) / Dx < 3.0;
 }
@@ -511,8 +588,138 @@ __device__ __forceinline__ double eps_entry(const MarkerDev& M, int ki, int kj, 
     return acc * (1.0 * 1.0 * M.ds[kj]);
 }
 
+// Fast path of the epsilon system, all in shared memory (`sm`, `sm_doubles`):
+//   xy[2*dim]    marker positions
+//   ph[10*dim]   kernel tables: for marker k and axis a, s = pos/Dx and
+//                ph[k*10 + 5a + o] = dirac(|s - c|) at lattice line
+//                c = c0[2k+a] + o, c0 = floor(s) - 2, o = 0..4. The kernel is
+//                zero beyond 1.5, so every line outside the table gives the
+//                exact 0.0 the direct evaluation gives.
+//   c0[2*dim]    (ints)
+//   cand[cap]    pairs that pass a conservative prefilter (|dx| and |dy|
+//                below 3*Dx*(1 + 2^-40)), then their matrix entries
+//   band / y / pivots / final rows of the banded LU
+// Entries use the same operations and operands as eps_entry, so they are
+// identical. Returns false (uniformly) when the marker set does not fit; the
+// caller then runs the direct path.
+__device__ __forceinline__ double eps_entry_tab(const MarkerDev& M, int ki, int jl, const double* ph, const int* c0,
+                                                double dsj) {
+    double acc = 0.0;
+    const int ns = M.nsupp[ki];
+    for (int s = 0; s < ns; s++) {
+        const double dvi = M.sd[ki * 9 + s];
+        const int ox = M.si[ki * 9 + s] - c0[jl * 2], oy = M.sj[ki * 9 + s] - c0[jl * 2 + 1];
+        const double px = (ox >= 0 && ox < 5) ? ph[jl * 10 + ox] : 0.0;
+        const double py = (oy >= 0 && oy < 5) ? ph[jl * 10 + 5 + oy] : 0.0;
+        acc += dvi * (px * py);
+    }
+    return acc * (1.0 * 1.0 * dsj);
+}
+
+__device__ bool epsilon_fast(const FsiDev& F, const MarkerDev& M, int m0, int dim, double* A, double* bx, int* piv,
+                             int* lmax, double* sm, int sm_doubles) {
+    __shared__ int s_kl, s_ku, s_nc;
+    const long long fixed = 13LL * dim + 64;
+    if (!sm || dim > 4096 || fixed >= sm_doubles) return false;
+    const int cap = (int)((sm_doubles - fixed) / 3);
+    double* xy = sm;
+    double* ph = xy + 2 * dim;
+    int* c0 = reinterpret_cast<int*>(ph + 10 * dim);
+    double* cval = ph + 11 * dim + 1;
+    int* ckey = reinterpret_cast<int*>(cval + cap);
+    double* band = cval + cap + (cap + 1) / 2 + 1;
+    const long long band_doubles = sm_doubles - (band - sm);
+    const double Dx = F.Dx;
+    if (threadIdx.x == 0) { s_kl = 0; s_ku = 0; s_nc = 0; }
+    for (int q = threadIdx.x; q < 2 * dim; q += blockDim.x) xy[q] = M.pos[m0 * 2 + q];
+    __syncthreads();
+    for (int q = threadIdx.x; q < 10 * dim; q += blockDim.x) {
+        const int k = q / 10, a = (q % 10) / 5, o = q % 5;
+        const double sc = xy[2 * k + a] / Dx;
+        const int base = (int)floor(sc) - 2;
+        if (o == 0) c0[2 * k + a] = base;
+        ph[q] = dirac_d(fabs(sc - (base + o)));
+    }
+    // prefilter + compaction, whole warps per iteration
+    const double lim = 3.0 * Dx * (1.0 + 0x1p-40);
+    const int lane = threadIdx.x & 31;
+    const int total = dim * dim;
+    for (int p0 = threadIdx.x & ~31; p0 < total; p0 += blockDim.x) {
+        const int pp = p0 + lane;
+        bool c = false;
+        if (pp < total) {
+            const int i = pp / dim, j = pp % dim;
+            c = fabs(xy[2 * i] - xy[2 * j]) < lim && fabs(xy[2 * i + 1] - xy[2 * j + 1]) < lim;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, c);
+        int base = 0;
+        if (lane == 0 && bal) base = atomicAdd(&s_nc, __popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const int slot = base + __popc(bal & ((1u << lane) - 1u));
+        if (c && slot < cap) ckey[slot] = pp;
+    }
+    __syncthreads();
+    const int nc = s_nc;
+    if (nc > cap) return false;
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        const int pp = ckey[c];
+        const int i = pp / dim, j = pp % dim;
+        if (fabs(xy[2 * i] - xy[2 * j]) / Dx < 3.0 && fabs(xy[2 * i + 1] - xy[2 * j + 1]) / Dx < 3.0) {
+            cval[c] = eps_entry_tab(M, m0 + i, j, ph, c0, M.ds[m0 + j]);
+            if (j > i) atomicMax(&s_kl, j - i);
+            else if (i > j) atomicMax(&s_ku, i - j);
+        } else {
+            ckey[c] = -1;
+        }
+    }
+    __syncthreads();
+    const int kl = s_kl, ku = s_ku, W = 2 * kl + ku + 1;
+    if (kl < 32 && kl + ku < 32 && (long long)dim * W + 2 * dim <= band_doubles) {
+        double* Bd = band;
+        double* y = Bd + (size_t)dim * W;
+        int* sp = reinterpret_cast<int*>(y + dim);
+        int* fp = sp + dim;
+        for (int q = threadIdx.x; q < dim * W; q += blockDim.x) Bd[q] = 0.0;
+        for (int i = threadIdx.x; i < dim; i += blockDim.x) y[i] = 1.0;
+        __syncthreads();
+        for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+            const int pp = ckey[c];
+            if (pp >= 0) bd(Bd, W, kl, pp % dim, pp / dim) = cval[c];
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            band_factor_smem(Bd, dim, kl, ku, W, sp);
+            band_solve_warp(Bd, dim, kl, ku, W, sp, fp, y);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < dim; i += blockDim.x) M.eps[m0 + i] = y[i];
+        __syncthreads();
+        return true;
+    }
+    // wide band: dense system in global scratch, same entries
+    for (long long q = threadIdx.x; q < (long long)dim * dim; q += blockDim.x) A[q] = 0.0;
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) bx[i] = 1.0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        const int pp = ckey[c];
+        if (pp >= 0) A[pp] = cval[c];
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        warp_lu_factor(A, dim, 0, kl, ku, piv, lmax);
+        warp_lu_solve(A, dim, 0, kl, ku, piv, lmax, bx, bx);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) M.eps[m0 + i] = bx[i];
+    __syncthreads();
+    return true;
+}
+
+// Direct path (marker sets beyond the shared-memory plan): entries evaluated
+// pair by pair, band LU in `smem` when it fits, else the dense LU in A.
 __device__ void epsilon_range(const FsiDev& F, const MarkerDev& M, int m0, int dim, double* A, double* bx, int* piv,
                               int* lmax, double* smem = nullptr, int smem_doubles = 0) {
+    if (epsilon_fast(F, M, m0, dim, A, bx, piv, lmax, smem, smem_doubles)) return;
     __shared__ int s_kl, s_ku;
     if (threadIdx.x == 0) { s_kl = 0; s_ku = 0; }
     __syncthreads();
@@ -545,7 +752,8 @@ __device__ void epsilon_range(const FsiDev& F, const MarkerDev& M, int m0, int d
         __syncthreads();
         if (threadIdx.x < 32) {
             band_factor_smem(Bd, dim, kl, ku, W, sp);
-            if (threadIdx.x == 0) band_solve_smem(Bd, dim, kl, ku, W, sp, fp, y);
+            if (kl + ku < 32) band_solve_warp(Bd, dim, kl, ku, W, sp, fp, y);
+            else if (threadIdx.x == 0) band_solve_smem(Bd, dim, kl, ku, W, sp, fp, y);
         }
         __syncthreads();
         for (int i = threadIdx.x; i < dim; i += blockDim.x) M.eps[m0 + i] = y[i];
@@ -569,7 +777,7 @@ __device__ void epsilon_range(const FsiDev& F, const MarkerDev& M, int m0, int d
     __syncthreads();
 }
 
-constexpr int kEpsSmemDoubles = 6000;  // 48000 bytes of dynamic shared memory
+constexpr int kEpsSmemDoubles = 25000;  // 200000 bytes of dynamic shared memory (opt-in)
 
 __global__ void __launch_bounds__(256) k_fsi_epsilon_body(FsiDev F, MarkerDev M) {
     extern __shared__ double eps_smem[];
@@ -750,7 +958,7 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
         // delU = solveLAPACK(K, F, bcDOFs) (src/Utils.cpp:288-311)
         if (threadIdx.x < 32) {
             band_factor_smem(sBd, nn, 5, 5, KW, sPiv);
-            if (threadIdx.x == 0) band_solve_smem(sBd, nn, 5, 5, KW, sPiv, sFp, sY);
+            band_solve_warp(sBd, nn, 5, 5, KW, sPiv, sFp, sY);
         }
         __syncthreads();
         {
@@ -764,11 +972,15 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
             for (int i = threadIdx.x; i < n; i += blockDim.x) U[i] = U[i] + dU[i];
         }
         __syncthreads();
+        // squares in parallel, then the sum in index order (one thread)
+        {
+            const double* dU = vec(B, V_delU);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) sV[i] = dU[i] * dU[i];
+        }
         update_fem_values(B);
         if (threadIdx.x == 0) {
-            const double* dU = vec(B, V_delU);
             double dd = 0.0;
-            for (int i = 0; i < n; i++) dd += dU[i] * dU[i];
+            for (int i = 0; i < n; i++) dd += sV[i];
             s_res = sqrt(dd) / (F.ref_L * sqrt((double)n));
             s_it++;
         }
@@ -779,20 +991,37 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
     if (threadIdx.x == 0) {
         B.itNR = s_it;
         B.resNR = s_res;
-        // FEMBodyClass::subResidual (src/FEMBody.cpp:244-256)
         swap_slots(B, V_Rkm1, V_Rk);
+    }
+    __syncthreads();
+    // FEMBodyClass::subResidual (src/FEMBody.cpp:244-256): the terms in
+    // parallel, each of the three sums in index order by one thread of its
+    // own warp.
+    {
         double* Rk = vec(B, V_Rk);
         const double* Rkm1 = vec(B, V_Rkm1);
         const double* U = vec(B, V_U);
         const double* Uk = vec(B, V_Ukm1);
-        for (int i = 0; i < n; i++) Rk[i] = U[i] - Uk[i];
-        double res = 0.0, num = 0.0, den = 0.0;
-        for (int i = 0; i < n; i++) res += Rk[i] * Rk[i];
-        for (int i = 0; i < n; i++) num += Rkm1[i] * (Rk[i] - Rkm1[i]);
-        for (int i = 0; i < n; i++) den += (Rk[i] - Rkm1[i]) * (Rk[i] - Rkm1[i]);
-        B.subRes = res;
-        B.subNum = num;
-        B.subDen = den;
+        double* tr = sMb;
+        double* tn = sMb + n;
+        double* td = sMb + 2 * n;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double r = U[i] - Uk[i];
+            const double d = r - Rkm1[i];
+            Rk[i] = r;
+            tr[i] = r * r;
+            tn[i] = Rkm1[i] * d;
+            td[i] = d * d;
+        }
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0 && threadIdx.x < 96) {
+            const double* t = sMb + (threadIdx.x >> 5) * n;
+            double acc = 0.0;
+            for (int i = 0; i < n; i++) acc += t[i];
+            if (threadIdx.x == 0) B.subRes = acc;
+            else if (threadIdx.x == 32) B.subNum = acc;
+            else B.subDen = acc;
+        }
     }
 }
 
@@ -800,14 +1029,33 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
 // (A: n*n, b: n, piv, lmax: n).
 __global__ void __launch_bounds__(256) k_epsilon_markers(FsiDev F, MarkerDev M, int n, double* A, double* b, int* piv,
                                                          int* lmax) {
-    epsilon_range(F, M, 0, n, A, b, piv, lmax);
+    extern __shared__ double eps_smem[];
+    epsilon_range(F, M, 0, n, A, b, piv, lmax, eps_smem, kEpsSmemDoubles);
+}
+
+// The epsilon kernels take 200000 bytes of dynamic shared memory (opt-in);
+// the attribute is set once per device.
+cudaError_t epsilon_configure() {
+    static std::atomic<int> done[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < 64 && done[dev].load()) return cudaSuccess;
+    const int bytes = kEpsSmemDoubles * (int)sizeof(double);
+    e = cudaFuncSetAttribute(k_fsi_epsilon_body, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fsi_epsilon_uni, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_epsilon_markers, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev].store(1);
+    return e;
 }
 
 cudaError_t launch_epsilon_markers(const MarkerDev& M, int n, double Dx, double* A, double* b, int* piv, int* lmax,
                                    cudaStream_t s) {
     FsiDev F{};
     F.Dx = Dx;
-    k_epsilon_markers<<<1, 256, 0, s>>>(F, M, n, A, b, piv, lmax);
+    cudaError_t e = epsilon_configure();
+    if (e != cudaSuccess) return e;
+    k_epsilon_markers<<<1, 256, kEpsSmemDoubles * sizeof(double), s>>>(F, M, n, A, b, piv, lmax);
     return cudaGetLastError();
 }
 
@@ -855,7 +1103,9 @@ size_t fem_dynamic_smem(int n, int bc) {
 }
 
 cudaError_t fem_dynamic_configure(size_t smem) {
-    return cudaFuncSetAttribute(k_fem_dynamic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_fem_dynamic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = epsilon_configure();
+    return e;
 }
 
 cudaError_t launch_fsi_begin(const FsiDev& F, int t, cudaStream_t s) {
@@ -867,7 +1117,7 @@ cudaError_t launch_fsi_subiteration(const FsiDev& F, const MarkerDev& M, const v
                                     double velScale, cudaStream_t s, int* launches,
                                     const cudaGraphConditionalHandle* cond) {
     k_fsi_predict<<<F.nFlex, 256, 0, s>>>(F, M);
-    k_fsi_support<<<(F.nFlexMarkers + 127) / 128, 128, 0, s>>>(F, M);
+    k_fsi_support<<<(F.nFlexMarkers + 3) / 4, 128, 0, s>>>(F, M);
     if (F.uni) k_fsi_epsilon_uni<<<1, 256, kEpsSmemDoubles * sizeof(double), s>>>(F, M);
     else k_fsi_epsilon_body<<<F.nFlex, 256, kEpsSmemDoubles * sizeof(double), s>>>(F, M);
     cudaError_t e = launch_ibm_interp(P, L, t, M, velScale, s, cond ? &F.s->t : nullptr);
