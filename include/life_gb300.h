@@ -223,6 +223,50 @@ int life_case_total_force(LifeCase* c, double* fx, double* fy);
 int life_case_bench_steps(LifeCase* c, int32_t nsteps, double* total_ms, double* interior_ms,
                           int32_t* launches);
 
+/* ---- Batched ensembles (no counterpart in the reference, which runs one case
+ * per process). A batch steps many independent cases of uneven lattice size,
+ * body count and collision model together: the interior stream-collide of all
+ * cases runs in one persistent launch over per-case tile ranges, the rest of
+ * each case's step runs on the case's own stream, and one batch step is a
+ * replayed CUDA graph (a case's FSI subiteration loop is a conditional WHILE
+ * node in it). Each case computes exactly what it computes alone. All cases
+ * must use the same population storage form. */
+typedef struct LifeBatch LifeBatch;
+
+typedef struct LifeBatchInfo {
+    int32_t n_cases, precision;
+    int64_t sites;             /* lattice sites over all cases */
+    int32_t tile_w, tile_h;    /* tile shape of the batched interior launch */
+    int32_t tiles, grid;       /* tiles over all cases, persistent CTAs */
+    int32_t kernel_nodes;      /* kernel nodes of one step graph (loop bodies once) */
+    size_t device_bytes;       /* device memory held by the cases */
+} LifeBatchInfo;
+
+/* Creates n_cases cases: params[k] with n_bodies[k] consecutive entries of
+ * `bodies` (as life_case_create). */
+int life_batch_create(const LifeCaseParams* params, const LifeBodyDesc* bodies, const int32_t* n_bodies,
+                      int32_t n_cases, LifeBatch** out);
+int life_batch_destroy(LifeBatch* b);
+/* Advances every case by nsteps steps; returns the first case's device status
+ * error (with the case index in the message) if one was raised. */
+int life_batch_step(LifeBatch* b, int32_t nsteps);
+int life_batch_sync(LifeBatch* b);
+/* Borrowed handle of case k for the life_case_get_* and status calls (the
+ * batch keeps ownership; stepping it alone makes the batch recapture). */
+int life_batch_case(LifeBatch* b, int32_t k, LifeCase** out);
+int life_batch_info(LifeBatch* b, LifeBatchInfo* info);
+/* Tile shape of the batched interior launch: tile_w in 32..256 (multiple of
+ * 32, one CTA row), tile_h rows per tile. */
+int life_batch_set_tile(LifeBatch* b, int32_t tile_w, int32_t tile_h);
+/* Times the batched interior kernel for tile_w in {64,128,256} x tile_h in
+ * {1,2,4,8} on this batch and keeps the fastest; returns it and its time. */
+int life_batch_autotune(LifeBatch* b, int32_t* tile_w, int32_t* tile_h, float* best_ms);
+/* Mean device time of the batched interior kernel alone (measurement hook). */
+int life_batch_interior_ms(LifeBatch* b, int32_t reps, float* ms);
+/* Runs nsteps batch steps between CUDA events on the batch stream and returns
+ * their device time and the kernel nodes per step graph (measurement hook). */
+int life_batch_bench_steps(LifeBatch* b, int32_t nsteps, double* total_ms, int32_t* kernels_per_step);
+
 /* Parses geometry.config text with the reference's rules (leading '#' lines
  * skipped, whitespace tokens; src/Objects.cpp:338-458). Writes at most cap
  * descriptors, returns the number found in *n. */

@@ -60,6 +60,14 @@ class LifeCaseInfo(C.Structure):
     ]
 
 
+class LifeBatchInfo(C.Structure):
+    _fields_ = [
+        ("n_cases", C.c_int32), ("precision", C.c_int32), ("sites", C.c_int64),
+        ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("tiles", C.c_int32), ("grid", C.c_int32),
+        ("kernel_nodes", C.c_int32), ("device_bytes", C.c_size_t),
+    ]
+
+
 class LifeStatus(C.Structure):
     _fields_ = [
         ("code", C.c_int32), ("t", C.c_int32), ("last_subits", C.c_int32),

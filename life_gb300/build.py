@@ -45,6 +45,7 @@ UNITS: List[Tuple[str, List[str]]] = [
     ("ibm_host.cu", ["--fmad=false"]),
     ("fem_host.cu", ["--fmad=false"]),
     ("ibm_noalloc.cu", ["--fmad=false"]),
+    ("batch.cu", ["--fmad=false"]),
     ("objects.cpp", []),
 ]
 

@@ -1091,8 +1091,8 @@ __global__ void k_fsi_residual(FsiDev F, cudaGraphConditionalHandle cond, int us
     if (use_cond) cudaGraphSetConditional(cond, cont ? 1u : 0u);
 }
 
-__global__ void k_fsi_begin(FsiDev F, int t) {
-    F.s->t = t;
+__global__ void k_fsi_begin(FsiDev F, int t, const int* t_dev, int t_off) {
+    F.s->t = t_dev ? *t_dev + t_off : t;
     F.s->subIt = 0;
     *F.cont = 1;
 }
@@ -1102,14 +1102,27 @@ size_t fem_dynamic_smem(int n, int bc) {
     return sizeof(double) * ((size_t)nn * 16 + (size_t)n * 22 + n + nn) + sizeof(int) * 2 * (size_t)nn;
 }
 
+// The opt-in shared-memory size is an attribute of the kernel, shared by every
+// case on the device, so it only ever grows: a case created later with
+// smaller bodies must not lower it below what a live case launches with.
 cudaError_t fem_dynamic_configure(size_t smem) {
-    cudaError_t e = cudaFuncSetAttribute(k_fem_dynamic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) e = epsilon_configure();
-    return e;
+    static std::atomic<size_t> set[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    size_t cur = set[dev].load();
+    if (smem > cur) {
+        e = cudaFuncSetAttribute(k_fem_dynamic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        while (cur < smem && !set[dev].compare_exchange_weak(cur, smem)) {
+        }
+    }
+    return epsilon_configure();
 }
 
-cudaError_t launch_fsi_begin(const FsiDev& F, int t, cudaStream_t s) {
-    k_fsi_begin<<<1, 1, 0, s>>>(F, t);
+cudaError_t launch_fsi_begin(const FsiDev& F, int t, cudaStream_t s, const int* t_dev, int t_off) {
+    k_fsi_begin<<<1, 1, 0, s>>>(F, t, t_dev, t_off);
     return cudaGetLastError();
 }
 

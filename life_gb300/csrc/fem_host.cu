@@ -241,12 +241,48 @@ static int build_fsi_graph(LifeCase* c, FemHost* H, int key, int t, const void* 
     return LIFE_OK;
 }
 
+// While a batch captures the case's stream, the WHILE node of the loop goes
+// straight into the graph being captured: it is added after the capture's
+// current dependencies, its body is captured on the case's side stream, and
+// the capture continues after the node.
+static int embed_fsi_loop(LifeCase* c, FemHost* H, int t, const void* A, const LatDev& L) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(H->cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    cudaError_t el = launch_fsi_subiteration(H->F, c->M, A, L, t, c->Dt / c->Dx, H->cap, nullptr, &h);
+    cudaError_t e = cudaStreamEndCapture(H->cap, &body);
+    if (el != cudaSuccess) return cuda_fail(el, "FSI loop body");
+    if (e != cudaSuccess) return cuda_fail(e, "FSI loop body capture");
+    size_t nn = 0;
+    CK(cudaGraphGetNodes(body, nullptr, &nn));
+    c->loop_body_kernels = (int)nn;
+    CK(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    c->ibm_launches += 1;
+    return LIFE_OK;
+}
+
 // The subiteration loop of one step; the spread follows in ibm_step().
 int fem_fsi_loop(LifeCase* c, int t, const void* A, const LatDev& L) {
     FemHost* H = fem_of(c);
-    cudaError_t e = launch_fsi_begin(H->F, t, c->stream);
+    cudaError_t e = launch_fsi_begin(H->F, t, c->stream, c->t_dev, c->t_off);
     if (e != cudaSuccess) return cuda_fail(e, "fsi_begin");
     c->ibm_launches += 1;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(c->stream, &cs));
+    if (cs == cudaStreamCaptureStatusActive) return embed_fsi_loop(c, H, t, A, L);
     if (!H->host_loop) {
         const int key = (A == c->P[0] ? 0 : 2) + (t & 1);
         if (!H->graph[key].exec)

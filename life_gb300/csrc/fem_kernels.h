@@ -81,7 +81,8 @@ cudaError_t fem_dynamic_configure(size_t smem);
 cudaError_t launch_fsi_subiteration(const FsiDev& F, const MarkerDev& M, const void* P, const LatDev& L, int t,
                                     double velScale, cudaStream_t s, int* launches,
                                     const cudaGraphConditionalHandle* cond = nullptr);
-cudaError_t launch_fsi_begin(const FsiDev& F, int t, cudaStream_t s);
+// With t_dev (inside a replayed graph) the step is *t_dev + t_off.
+cudaError_t launch_fsi_begin(const FsiDev& F, int t, cudaStream_t s, const int* t_dev = nullptr, int t_off = 0);
 // Epsilon system of markers [0, n) of M into M.eps, with caller-provided scratch.
 cudaError_t launch_epsilon_markers(const MarkerDev& M, int n, double Dx, double* A, double* b, int* piv, int* lmax,
                                    cudaStream_t s);

@@ -28,7 +28,7 @@ __global__ void k_ibm_interp(const typename S::T* __restrict__ P, LatDev L, int 
                              const int* __restrict__ t_dev) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= M.n) return;
-    if (t_dev) t = *t_dev;  // inside a replayed graph the step comes from the device
+    t = t_dev ? *t_dev : step_t(L, t);  // inside a replayed graph the step comes from the device
     double iRho = 0.0, iMx = 0.0, iMy = 0.0;
     const int ns = M.nsupp[k];
     int imin = 1 << 30, imax = -(1 << 30), jmin = 1 << 30, jmax = -(1 << 30);
@@ -83,6 +83,7 @@ __global__ void __launch_bounds__(256) k_ibm_spread(const typename S::T* __restr
     __shared__ double s_fx[256], s_fy[256];
     __shared__ int s_ns[256];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    t = step_t(L, t);
     const int ntiles = *W.ntiles;
     for (int q = blockIdx.x; q < ntiles; q += gridDim.x) {
         const int tile = W.tiles[q];

@@ -181,6 +181,9 @@ __device__ __forceinline__ void collide_bgk(const double f[9], double rho, doubl
 __device__ __forceinline__ void collide_cm(const double f[9], double rho, double ux, double uy, double Fx,
                                            double Fy, double omega, double cs, double fs[9]);
 
+// Step index of a launch: its argument, or the device counter in a graph.
+__device__ __forceinline__ int step_t(const LatDev& L, int t) { return L.t_dev ? *L.t_dev + L.t_off : t; }
+
 // One time step's scalars: the inlet ramp used by the boundary conditions of
 // step t and the uniform pressure-gradient force of step t (Womersley).
 __device__ __forceinline__ void force_xy_at(const LatDev& L, int t, double& Fx, double& Fy) {

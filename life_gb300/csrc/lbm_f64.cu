@@ -74,10 +74,8 @@ __global__ void k_init(typename S::T* __restrict__ B, LatDev L, int t0) {
 // sites are collided again by the IBM fix-up kernel once the spread force is
 // known. Same arithmetic as site_state() for a fluid site.
 template <bool CM>
-__global__ void __launch_bounds__(128) k_interior_f64(const double* __restrict__ A, double* __restrict__ B, LatDev L,
-                                                      int t) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-    if (i >= L.Nx) return;
+__device__ __forceinline__ void interior_site_f64(const double* __restrict__ A, double* __restrict__ B,
+                                                  const LatDev& L, int t, int i, int j) {
     if (site_type(L, i, j) != LIFE_FLUID) return;
     double f[9], rho, ux, uy, Fx, Fy;
     const bool edge = (i == 0) | (i == L.Nx - 1) | (j == 0) | (j == L.Ny - 1);
@@ -94,11 +92,42 @@ __global__ void __launch_bounds__(128) k_interior_f64(const double* __restrict__
     store_collided<CM, StoreF64>(B, L, t + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
 }
 
+template <bool CM>
+__global__ void __launch_bounds__(128) k_interior_f64(const double* __restrict__ A, double* __restrict__ B, LatDev L,
+                                                      int t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= L.Nx) return;
+    interior_site_f64<CM>(A, B, L, step_t(L, t), i, j);
+}
+
+// All cases of a batch in one persistent launch (see k_interior_batch_lowp).
+__global__ void __launch_bounds__(256) k_interior_batch_f64(const BatchLatCase* __restrict__ cases,
+                                                            const int* __restrict__ tile_case, int ntiles, int tile_h,
+                                                            int phase) {
+    for (int q = blockIdx.x; q < ntiles; q += gridDim.x) {
+        const BatchLatCase& C = cases[tile_case[q]];
+        const LatDev& L = C.L[phase];
+        const int lt = q - C.tile0;
+        const int tx = lt % C.tiles_x, ty = lt / C.tiles_x;
+        const int i = tx * blockDim.x + threadIdx.x;
+        if (i >= L.Nx) continue;
+        const int t = step_t(L, 0);
+        const double* A = (const double*)C.A[phase];
+        double* B = (double*)C.B[phase];
+        const int j1 = (ty + 1) * tile_h < L.Ny ? (ty + 1) * tile_h : L.Ny;
+        for (int j = ty * tile_h; j < j1; j++) {
+            if (L.cm) interior_site_f64<true>(A, B, L, t, i, j);
+            else interior_site_f64<false>(A, B, L, t, i, j);
+        }
+    }
+}
+
 // Boundary-condition sites of one step (any storage form, FP64 arithmetic):
 // the perimeter is enumerated bottom row, top row, left column, right column.
 template <bool CM, class S>
 __global__ void k_perimeter(const typename S::T* __restrict__ A, typename S::T* __restrict__ B, LatDev L, int t) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    t = step_t(L, t);
     const int Nx = L.Nx, Ny = L.Ny;
     int i, j;
     if (q < Nx) { i = q; j = 0; }
@@ -269,6 +298,18 @@ cudaError_t launch_interior_f64(const double* A, double* B, const LatDev& L, int
     if (L.cm) k_interior_f64<true><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
     else k_interior_f64<false><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
     return cudaGetLastError();
+}
+
+cudaError_t launch_interior_batch_f64(const BatchLatCase* cases, const int* tile_case, int ntiles, int tile_w,
+                                      int tile_h, int grid, int phase, cudaStream_t s) {
+    k_interior_batch_f64<<<grid, tile_w, 0, s>>>(cases, tile_case, ntiles, tile_h, phase);
+    return cudaGetLastError();
+}
+
+int batch_blocks_per_sm_f64(int tile_w) {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_interior_batch_f64, tile_w, 0);
+    return n;
 }
 
 cudaError_t launch_perimeter(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {

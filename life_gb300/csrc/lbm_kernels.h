@@ -19,6 +19,23 @@ cudaError_t launch_export(const void* P, const LatDev& L, int t, bool initial, d
                           double* fibm, cudaStream_t s);
 cudaError_t launch_maxvel(const void* P, const LatDev& L, int t, unsigned long long* out, cudaStream_t s);
 
+// One case of a batched interior launch: its lattice view and buffers for the
+// two step parities of a batch (phase 0: P[cur] -> P[cur^1], phase 1: back),
+// and its first tile and tiles per row.
+struct BatchLatCase {
+    LatDev L[2];
+    const void* A[2];
+    void* B[2];
+    int tile0, tiles_x;
+};
+
+cudaError_t launch_interior_batch_f64(const BatchLatCase* cases, const int* tile_case, int ntiles, int tile_w,
+                                      int tile_h, int grid, int phase, cudaStream_t s);
+cudaError_t launch_interior_batch_lowp(int prec, const BatchLatCase* cases, const int* tile_case, int ntiles,
+                                       int tile_w, int tile_h, int grid, int phase, cudaStream_t s);
+int batch_blocks_per_sm_f64(int tile_w);
+int batch_blocks_per_sm_lowp(int prec, int tile_w);
+
 // One lattice step: interior sites, then the boundary-condition perimeter.
 // Both read A and write disjoint sites of B.
 inline cudaError_t launch_step(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {

@@ -108,13 +108,11 @@ __device__ __forceinline__ void collide_dev32(const float g[9], float dr, float 
     }
 }
 
-// Interior sites, reduced-precision storage. Sites on a boundary-condition
+// One interior site, reduced-precision storage. Sites on a boundary-condition
 // wall are left to the perimeter kernel.
 template <bool CM, class S>
-__global__ void __launch_bounds__(256) k_interior_lowp(const typename S::T* __restrict__ A,
-                                                       typename S::T* __restrict__ B, LatDev L, int t) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-    if (i >= L.Nx) return;
+__device__ __forceinline__ void interior_site_lowp(const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
+                                                   const LatDev& L, int t, int i, int j) {
     if (site_type(L, i, j) != LIFE_FLUID) return;
     const bool edge = (i == 0) | (i == L.Nx - 1) | (j == 0) | (j == L.Ny - 1);
     float g[9];
@@ -152,6 +150,40 @@ __global__ void __launch_bounds__(256) k_interior_lowp(const typename S::T* __re
     for (int v = 0; v < 9; v++) B[(size_t)v * L.S + base] = S::put(gs[v], v);
 }
 
+template <bool CM, class S>
+__global__ void __launch_bounds__(256) k_interior_lowp(const typename S::T* __restrict__ A,
+                                                       typename S::T* __restrict__ B, LatDev L, int t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= L.Nx) return;
+    interior_site_lowp<CM, S>(A, B, L, step_t(L, t), i, j);
+}
+
+// All cases of a batch in one persistent launch. Tile q of the batch belongs
+// to case tile_case[q]; inside the case it covers tile_w sites of tile_h rows
+// (tile_w = blockDim.x). Each CTA walks tiles q = blockIdx.x, +gridDim.x, ...
+// The collision model is a per-case value, uniform over a CTA.
+template <class S>
+__global__ void __launch_bounds__(256) k_interior_batch_lowp(const BatchLatCase* __restrict__ cases,
+                                                             const int* __restrict__ tile_case, int ntiles,
+                                                             int tile_h, int phase) {
+    for (int q = blockIdx.x; q < ntiles; q += gridDim.x) {
+        const BatchLatCase& C = cases[tile_case[q]];
+        const LatDev& L = C.L[phase];
+        const int lt = q - C.tile0;
+        const int tx = lt % C.tiles_x, ty = lt / C.tiles_x;
+        const int i = tx * blockDim.x + threadIdx.x;
+        if (i >= L.Nx) continue;
+        const int t = step_t(L, 0);
+        const typename S::T* A = (const typename S::T*)C.A[phase];
+        typename S::T* B = (typename S::T*)C.B[phase];
+        const int j1 = (ty + 1) * tile_h < L.Ny ? (ty + 1) * tile_h : L.Ny;
+        for (int j = ty * tile_h; j < j1; j++) {
+            if (L.cm) interior_site_lowp<true, S>(A, B, L, t, i, j);
+            else interior_site_lowp<false, S>(A, B, L, t, i, j);
+        }
+    }
+}
+
 cudaError_t launch_interior_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
     const dim3 grid((L.Nx + 255) / 256, L.Ny);
     if (L.prec == LIFE_PREC_F32) {
@@ -162,6 +194,24 @@ cudaError_t launch_interior_lowp(const void* A, void* B, const LatDev& L, int t,
         else k_interior_lowp<false, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t);
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_interior_batch_lowp(int prec, const BatchLatCase* cases, const int* tile_case, int ntiles,
+                                       int tile_w, int tile_h, int grid, int phase, cudaStream_t s) {
+    if (prec == LIFE_PREC_F32)
+        k_interior_batch_lowp<StoreF32><<<grid, tile_w, 0, s>>>(cases, tile_case, ntiles, tile_h, phase);
+    else
+        k_interior_batch_lowp<StoreF16><<<grid, tile_w, 0, s>>>(cases, tile_case, ntiles, tile_h, phase);
+    return cudaGetLastError();
+}
+
+int batch_blocks_per_sm_lowp(int prec, int tile_w) {
+    int n = 0;
+    if (prec == LIFE_PREC_F32)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_interior_batch_lowp<StoreF32>, tile_w, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_interior_batch_lowp<StoreF16>, tile_w, 0);
+    return n;
 }
 
 }  // namespace life

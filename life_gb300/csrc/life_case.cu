@@ -132,6 +132,8 @@ LatDev life::lattice_view(const LifeCase* c, int t) {
     L.outlet_f_next = c->d_outlet_f[t & 1];
     L.delU = c->d_delU;
     L.force_ibm = c->W.force_ibm;
+    L.t_dev = c->t_dev;
+    L.t_off = c->t_off;
     return L;
 }
 

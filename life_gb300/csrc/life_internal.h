@@ -72,6 +72,11 @@ struct LifeCase {
     int status_code = 0, status_t = 0;
     int ibm_launches = 0;     // kernels launched by the IBM/FEM sequence so far
     std::string status_msg;
+    // Set while a batch captures this case's step into a graph: kernels then
+    // take the step index from *t_dev + t_off (see LatDev).
+    const int* t_dev = nullptr;
+    int t_off = 0;
+    int loop_body_kernels = 0;  // kernels in one pass of a captured FSI loop body
 };
 
 namespace life {

@@ -44,6 +44,10 @@ struct LatDev {
     double* outlet_f_next;      // [Ny][3] written by the current step
     const double* delU;         // [Ny][2] convective speed term of the current step
     const double* force_ibm;    // [2][S] dense IBM force of the current step, or null
+    // Inside a replayed graph the step index comes from device memory: when
+    // t_dev is set, kernels use *t_dev + t_off instead of their t argument.
+    const int* t_dev;
+    int t_off;
 };
 
 }  // namespace life

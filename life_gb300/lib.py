@@ -16,7 +16,7 @@ from typing import Dict, Optional, Sequence
 
 import numpy as np
 
-from .abi import ERRORS, LifeCaseInfo, LifeStatus, body_structs, params_struct
+from .abi import ERRORS, LifeBatchInfo, LifeCaseInfo, LifeStatus, body_structs, params_struct
 from .case import CaseParams
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -52,6 +52,16 @@ SIGNATURES = {
                                    C.c_int32, C.c_double, C.c_void_p, C.c_void_p]),
     "life_ibm_epsilon_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.c_int32, C.c_double, C.c_void_p, C.c_void_p]),
+    "life_batch_create": (C.c_int, [C.c_void_p, C.c_void_p, _ip, C.c_int32, C.POINTER(C.c_void_p)]),
+    "life_batch_destroy": (C.c_int, [C.c_void_p]),
+    "life_batch_step": (C.c_int, [C.c_void_p, C.c_int32]),
+    "life_batch_sync": (C.c_int, [C.c_void_p]),
+    "life_batch_case": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "life_batch_info": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "life_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "life_batch_autotune": (C.c_int, [C.c_void_p, _ip, _ip, C.POINTER(C.c_float)]),
+    "life_batch_interior_ms": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
+    "life_batch_bench_steps": (C.c_int, [C.c_void_p, C.c_int32, _dp, _ip]),
 }
 
 
@@ -94,20 +104,24 @@ def _p(a: Optional[np.ndarray]):
 class Case:
     """A LIFE case running on the GPU through the C-ABI."""
 
-    def __init__(self, params: CaseParams, bodies: Sequence = ()):
+    def __init__(self, params: CaseParams, bodies: Sequence = (), _handle=None):
         L = lib()
         self.params = params
-        ps = params_struct(params)
-        bs = body_structs(bodies)
-        h = C.c_void_p()
-        _check(L.life_case_create(C.byref(ps), C.byref(bs), len(bodies), C.byref(h)))
-        self._h = h
+        self._owned = _handle is None
+        if _handle is None:
+            ps = params_struct(params)
+            bs = body_structs(bodies)
+            h = C.c_void_p()
+            _check(L.life_case_create(C.byref(ps), C.byref(bs), len(bodies), C.byref(h)))
+            _handle = h
+        self._h = _handle
         info = self.info()
         self.n_markers, self.n_bodies, self.n_flex = info.n_markers, info.n_bodies, info.n_flex
 
     def close(self) -> None:
         if getattr(self, "_h", None):
-            lib().life_case_destroy(self._h)
+            if self._owned:
+                lib().life_case_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -216,6 +230,89 @@ class Case:
         fx, fy = C.c_double(), C.c_double()
         _check(lib().life_case_total_force(self._h, C.byref(fx), C.byref(fy)))
         return fx.value, fy.value
+
+
+class Batch:
+    """Many independent cases stepped together (``life_batch_*``).
+
+    ``cases`` is a sequence of ``(params, bodies)``. :meth:`case` returns a
+    borrowed :class:`Case` view of case k for the field, marker and FEM getters.
+    """
+
+    def __init__(self, cases: Sequence):
+        L = lib()
+        self._cases = [(p, list(b)) for p, b in cases]
+        n = len(self._cases)
+        ps = (type(params_struct(self._cases[0][0])) * n)()
+        for k, (p, _) in enumerate(self._cases):
+            ps[k] = params_struct(p)
+        allb = [b for _, bl in self._cases for b in bl]
+        bs = body_structs(allb)
+        nb = (C.c_int32 * n)(*[len(bl) for _, bl in self._cases])
+        h = C.c_void_p()
+        _check(L.life_batch_create(ps, C.byref(bs), nb, n, C.byref(h)))
+        self._h = h
+        self._views = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            for v in self._views.values():
+                v._h = None
+            lib().life_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self) -> int:
+        return len(self._cases)
+
+    def step(self, n: int = 1) -> None:
+        _check(lib().life_batch_step(self._h, int(n)))
+
+    def sync(self) -> None:
+        _check(lib().life_batch_sync(self._h))
+
+    def case(self, k: int) -> Case:
+        if k not in self._views:
+            h = C.c_void_p()
+            _check(lib().life_batch_case(self._h, int(k), C.byref(h)))
+            self._views[k] = Case(self._cases[k][0], _handle=h)
+        _check(lib().life_batch_sync(self._h))
+        return self._views[k]
+
+    def info(self) -> LifeBatchInfo:
+        inf = LifeBatchInfo()
+        _check(lib().life_batch_info(self._h, C.byref(inf)))
+        return inf
+
+    def set_tile(self, w: int, h: int) -> None:
+        _check(lib().life_batch_set_tile(self._h, int(w), int(h)))
+
+    def autotune(self):
+        w, h, ms = C.c_int32(), C.c_int32(), C.c_float()
+        _check(lib().life_batch_autotune(self._h, C.byref(w), C.byref(h), C.byref(ms)))
+        return w.value, h.value, ms.value
+
+    def interior_ms(self, reps: int = 10) -> float:
+        ms = C.c_float()
+        _check(lib().life_batch_interior_ms(self._h, int(reps), C.byref(ms)))
+        return ms.value
+
+    def bench_steps(self, n: int):
+        """Run n batch steps; return (device ms, kernel nodes per step graph)."""
+        tot, kn = C.c_double(), C.c_int32()
+        _check(lib().life_batch_bench_steps(self._h, int(n), C.byref(tot), C.byref(kn)))
+        return tot.value, kn.value
 
 
 def parse_geometry(text: str):
