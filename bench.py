@@ -215,6 +215,11 @@ def run_workload(args, world, rank):
     from life_gb300.case import PREC_F32, PREC_F64
     build()
     from life_gb300.lib import Case
+    if args.workload == "ensemble":
+        out = {"workload": "ensemble64", **ensemble_leg(args.steps, args.warmup)}
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        return 0
     make = cylinder_params if args.workload == "cylinder" else filament_params
     out = {"workload": args.workload}
     for prec, tag in ((PREC_F64, "fp64"), (PREC_F32, "fp32")):
@@ -233,6 +238,49 @@ def run_workload(args, world, rank):
     if rank == 0:
         print(json.dumps(out), flush=True)
     return 0
+
+
+def ensemble_leg(steps: int, warmup: int) -> dict:
+    """The 64-case batched ensemble (uneven lattices, cylinders or filament
+    rows, BGK/CM, Re 50-300): batched FP32 and FP16 (one persistent interior
+    launch and one replayed graph per batch step, autotuned tiles) against the
+    same cases stepped one after another through life_case_step in FP64 and
+    FP32. MLUPS = sum of lattice sites x steps / device time."""
+    from life_gb300.ensemble import ensemble_cases, sites
+    from life_gb300.lib import Batch, Case
+    out = {}
+    for prec, tag in ((1, "fp32"), (2, "fp16")):
+        cs = ensemble_cases(precision=prec)
+        with Batch(cs) as B:
+            B.step(warmup)
+            w, h, ms = B.autotune()
+            B.step(warmup)
+            tot, kn = B.bench_steps(steps)
+            inf = B.info()
+            out[f"batched_{tag}_mlups"] = round(inf.sites * steps / (tot * 1e-3) / 1e6, 1)
+            out[f"batched_{tag}_ms_per_step"] = round(tot / steps, 4)
+            out[f"batched_{tag}_interior_ms"] = round(B.interior_ms(10), 4)
+            out[f"batched_{tag}_tile"] = [w, h]
+            out[f"batched_{tag}_kernel_nodes_per_step"] = kn
+            out[f"batched_{tag}_device_gb"] = round(inf.device_bytes / 1e9, 3)
+    for prec, tag in ((0, "fp64"), (1, "fp32")):
+        cs = ensemble_cases(precision=prec)
+        n_ss, ms_tot = 0, 0.0
+        k = max(10, steps // 5)
+        for p, b in cs:
+            with Case(p, b) as c:
+                c.step(warmup)
+                tt, _, _ = c.bench_steps(k)
+            ms_tot += tt
+            n_ss += p.Nx * p.Ny * k
+        out[f"sequential_{tag}_mlups"] = round(n_ss / (ms_tot * 1e-3) / 1e6, 1)
+    out["batched_fp32_over_sequential_fp64"] = round(out["batched_fp32_mlups"] / out["sequential_fp64_mlups"], 2)
+    out["batched_fp32_over_sequential_fp32"] = round(out["batched_fp32_mlups"] / out["sequential_fp32_mlups"], 2)
+    cs = ensemble_cases()
+    out["cases"] = len(cs)
+    out["sites"] = sites(cs)
+    out["bodies"] = sum(len(b) for _, b in cs)
+    return out
 
 
 def run_gb300(args, world, rank, local):
@@ -304,6 +352,8 @@ def run_gb300(args, world, rank, local):
             extras[f"filament_1200x400_bgk_{tag}_ms_per_step"] = round(tt / 50, 3)
             extras["filament_subiterations_last_step"] = st.last_subits
             del cf
+        # ---- 64-case batched ensemble
+        extras["ensemble"] = ensemble_leg(100, args.warmup)
 
     # ---- end to end through the C-ABI: create from params (host), K steps,
     # read the velocity field back to host memory
@@ -364,8 +414,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nx", type=int, default=4096)
     ap.add_argument("--quick", action="store_true", help="headline measurement only")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "cylinder", "filament"],
-                    help="cavity: the headline line; cylinder/filament: timing of one IBM case")
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "cylinder", "filament", "ensemble"],
+                    help="cavity: the headline line; cylinder/filament: timing of one IBM case; "
+                         "ensemble: the 64-case batch against sequential per-case runs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
