@@ -220,6 +220,11 @@ def run_workload(args, world, rank):
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
+    if args.workload == "serve":
+        out = {"workload": "serving_canopy", **serving_leg(args.requests, args.step_scale)}
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        return 0
     make = cylinder_params if args.workload == "cylinder" else filament_params
     out = {"workload": args.workload}
     for prec, tag in ((PREC_F64, "fp64"), (PREC_F32, "fp32")):
@@ -280,6 +285,91 @@ def ensemble_leg(steps: int, warmup: int) -> dict:
     out["cases"] = len(cs)
     out["sites"] = sites(cs)
     out["bodies"] = sum(len(b) for _, b in cs)
+    return out
+
+
+def serving_leg(n_requests: int = 24, step_scale: float = 0.02, seed: int = 7, load: float = 0.8) -> dict:
+    """Serving: a seeded Poisson stream of canopy requests (8-32 stalks of 20
+    elements, 512-4096 x 256-1024 lattices, FP32 lattice / FP64 FEM) against
+    a 160 GB admission budget, continuous batching on one GB300.
+
+    1. capacity: the first 8 requests submitted at once, aggregate site
+       updates per second until they drain;
+    2. stream: arrivals at rate load x capacity / mean request work, each
+       request released as soon as it finishes; latency = finish - submit;
+    3. baseline: the same kind of request solved alone in FP64 through
+       life_case_step, one after another (bounded sample of steps).
+    Step counts are the request's 2000-20000 steps times step_scale."""
+    import numpy as np
+    from life_gb300.ensemble import canopy_case
+    from life_gb300.lib import Case, Server
+    rng = np.random.Generator(np.random.PCG64(seed))
+    reqs = []
+    for _ in range(n_requests):
+        p, b, steps = canopy_case(rng, precision=1)
+        reqs.append((p, b, max(10, int(round(steps * step_scale)))))
+    work = [p.Nx * p.Ny * s for p, _, s in reqs]
+    budget = 160 << 30
+    out = {"requests": n_requests, "step_scale": step_scale, "hbm_budget_gb": 160, "load": load}
+    # 1. capacity at saturation
+    with Server(hbm_budget=budget, steps_per_round=100) as S:
+        burst = reqs[:8]
+        ids = [S.submit(p, b, s) for p, b, s in burst]
+        S.drain(timeout=600)
+        infos = [S.query(i) for i in ids]
+        span = max(i.done_s for i in infos) - min(i.submit_s for i in infos)
+        cap = sum(work[:8]) / span
+        for i in ids:
+            S.release(i)
+    out["capacity_mlups"] = round(cap / 1e6, 1)
+    # 2. Poisson stream at `load` of capacity
+    lam = load * cap / float(np.mean(work))
+    gaps = rng.exponential(1.0 / lam, size=n_requests)
+    with Server(hbm_budget=budget, steps_per_round=100) as S:
+        t0 = time.perf_counter()
+        ids = []
+        for k, (p, b, s) in enumerate(reqs):
+            due = t0 + float(np.sum(gaps[:k + 1]))
+            while True:
+                dt = due - time.perf_counter()
+                if dt <= 0:
+                    break
+                time.sleep(min(dt, 0.01))
+            ids.append(S.submit(p, b, s))
+        lat, infos = [], []
+        for i in ids:
+            S.wait(i, timeout=1800)
+            inf = S.query(i)
+            infos.append(inf)
+            lat.append(inf.done_s - inf.submit_s)
+            S.release(i)
+        st = S.stats()
+    span = max(i.done_s for i in infos) - min(i.submit_s for i in infos)
+    lat = np.array(lat)
+    out.update({
+        "arrival_rate_per_s": round(lam, 3),
+        "latency_s_p50": round(float(np.percentile(lat, 50)), 4),
+        "latency_s_p95": round(float(np.percentile(lat, 95)), 4),
+        "latency_s_p99": round(float(np.percentile(lat, 99)), 4),
+        "latency_s_max": round(float(lat.max()), 4),
+        "aggregate_mlups": round(sum(work) / span / 1e6, 1),
+        "busy_fraction": round(st.busy_s / max(st.clock_s, 1e-9), 3),
+        "peak_device_gb": round(st.bytes_peak / 1e9, 2),
+        "rounds": st.rounds, "regroups": st.regroups, "failed": st.failed,
+    })
+    # 3. sequential plain FP64, bounded sample
+    n_ss, ms_tot = 0, 0.0
+    for p, b, s in reqs[:4]:
+        import dataclasses
+        p64 = dataclasses.replace(p, precision=0)
+        with Case(p64, b) as c:
+            c.step(3)
+            k = min(s, 40)
+            tt, _, _ = c.bench_steps(k)
+        ms_tot += tt
+        n_ss += p.Nx * p.Ny * k
+    out["sequential_fp64_mlups"] = round(n_ss / (ms_tot * 1e-3) / 1e6, 1)
+    out["aggregate_over_sequential_fp64"] = round(out["aggregate_mlups"] / out["sequential_fp64_mlups"], 2)
     return out
 
 
@@ -354,6 +444,8 @@ def run_gb300(args, world, rank, local):
             del cf
         # ---- 64-case batched ensemble
         extras["ensemble"] = ensemble_leg(100, args.warmup)
+        # ---- serving: Poisson stream of canopy requests
+        extras["serving"] = serving_leg()
 
     # ---- end to end through the C-ABI: create from params (host), K steps,
     # read the velocity field back to host memory
@@ -414,7 +506,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nx", type=int, default=4096)
     ap.add_argument("--quick", action="store_true", help="headline measurement only")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "cylinder", "filament", "ensemble"],
+    ap.add_argument("--requests", type=int, default=24, help="serve: requests in the stream")
+    ap.add_argument("--step-scale", type=float, default=0.02, help="serve: fraction of each request's steps")
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "cylinder", "filament", "ensemble", "serve"],
                     help="cavity: the headline line; cylinder/filament: timing of one IBM case; "
                          "ensemble: the 64-case batch against sequential per-case runs")
     args = ap.parse_args()

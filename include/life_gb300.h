@@ -267,6 +267,62 @@ int life_batch_interior_ms(LifeBatch* b, int32_t reps, float* ms);
  * their device time and the kernel nodes per step graph (measurement hook). */
 int life_batch_bench_steps(LifeBatch* b, int32_t nsteps, double* total_ms, int32_t* kernels_per_step);
 
+/* ---- Serving (no counterpart in the reference). A server owns a thread that
+ * admits submitted solves in arrival order while their estimated device
+ * footprint fits hbm_budget, keeps their state on the device, and steps all
+ * admitted requests together as one batch per storage form, in rounds of at
+ * most steps_per_round steps; the active set is regrouped whenever a request
+ * is admitted or finishes (continuous batching). A finished request keeps its
+ * state on the device (counted against the budget) until it is taken or
+ * released. Each request computes exactly what it computes alone. The server
+ * calls are thread-safe. */
+typedef struct LifeServer LifeServer;
+
+typedef struct LifeServerConfig {
+    size_t hbm_budget;         /* bytes the admitted requests may hold */
+    int32_t max_active;        /* requests stepped together at most (0: no limit) */
+    int32_t steps_per_round;   /* steps per scheduling round (0: 200) */
+} LifeServerConfig;
+
+enum { LIFE_REQ_QUEUED = 0, LIFE_REQ_RUNNING = 1, LIFE_REQ_DONE = 2, LIFE_REQ_FAILED = 3 };
+
+typedef struct LifeRequestInfo {
+    int32_t state;             /* LIFE_REQ_* */
+    int32_t error;             /* LIFE_ERR_* of a failed request */
+    int32_t steps_done, steps;
+    double submit_s, start_s, done_s;  /* server clock, seconds since creation */
+    size_t device_bytes;
+    int64_t sites;
+} LifeRequestInfo;
+
+typedef struct LifeServerStats {
+    int64_t submitted, admitted, completed, failed;
+    int32_t active, queued;
+    size_t bytes_in_use, bytes_peak;
+    int64_t rounds, regroups;
+    double site_steps;         /* lattice-site updates done */
+    double busy_s;             /* server-clock time with admitted work */
+    double clock_s;            /* server clock now */
+} LifeServerStats;
+
+int life_server_create(const LifeServerConfig* cfg, LifeServer** out);
+/* Queues a solve of nsteps steps of the case (params, bodies); returns its id. */
+int life_server_submit(LifeServer* s, const LifeCaseParams* params, const LifeBodyDesc* bodies,
+                       int32_t n_bodies, int32_t nsteps, int64_t* id);
+int life_server_query(LifeServer* s, int64_t id, LifeRequestInfo* info);
+/* Blocks until the request is done or failed (its error), or LIFE_ERR_TIMEOUT
+ * after timeout_s seconds (negative: no limit). */
+int life_server_wait(LifeServer* s, int64_t id, double timeout_s);
+/* Hands a done request's case (device state) to the caller, who destroys it. */
+int life_server_take(LifeServer* s, int64_t id, LifeCase** out);
+/* Frees a done or failed request. */
+int life_server_release(LifeServer* s, int64_t id);
+int life_server_stats(LifeServer* s, LifeServerStats* st);
+/* Blocks until nothing is queued or running (LIFE_ERR_TIMEOUT after timeout_s). */
+int life_server_drain(LifeServer* s, double timeout_s);
+/* Stops the thread (queued requests are dropped) and frees everything. */
+int life_server_destroy(LifeServer* s);
+
 /* Parses geometry.config text with the reference's rules (leading '#' lines
  * skipped, whitespace tokens; src/Objects.cpp:338-458). Writes at most cap
  * descriptors, returns the number found in *n. */

@@ -68,6 +68,27 @@ class LifeBatchInfo(C.Structure):
     ]
 
 
+class LifeServerConfig(C.Structure):
+    _fields_ = [("hbm_budget", C.c_size_t), ("max_active", C.c_int32), ("steps_per_round", C.c_int32)]
+
+
+class LifeRequestInfo(C.Structure):
+    _fields_ = [
+        ("state", C.c_int32), ("error", C.c_int32), ("steps_done", C.c_int32), ("steps", C.c_int32),
+        ("submit_s", C.c_double), ("start_s", C.c_double), ("done_s", C.c_double),
+        ("device_bytes", C.c_size_t), ("sites", C.c_int64),
+    ]
+
+
+class LifeServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+        ("active", C.c_int32), ("queued", C.c_int32), ("bytes_in_use", C.c_size_t), ("bytes_peak", C.c_size_t),
+        ("rounds", C.c_int64), ("regroups", C.c_int64), ("site_steps", C.c_double), ("busy_s", C.c_double),
+        ("clock_s", C.c_double),
+    ]
+
+
 class LifeStatus(C.Structure):
     _fields_ = [
         ("code", C.c_int32), ("t", C.c_int32), ("last_subits", C.c_int32),

@@ -46,6 +46,7 @@ UNITS: List[Tuple[str, List[str]]] = [
     ("fem_host.cu", ["--fmad=false"]),
     ("ibm_noalloc.cu", ["--fmad=false"]),
     ("batch.cu", ["--fmad=false"]),
+    ("server.cu", ["--fmad=false"]),
     ("objects.cpp", []),
 ]
 

@@ -73,6 +73,7 @@ struct LifeBatch {
     std::vector<int> ring_end;  // step tables are valid for t < ring_end[k]
     std::string status_msg;
     int status_code = 0;
+    bool owns_cases = true;
 };
 
 static void drop_graphs(LifeBatch* b) {
@@ -87,7 +88,8 @@ static void free_batch(LifeBatch* b) {
     if (!b) return;
     if (b->stream) cudaStreamSynchronize(b->stream);
     drop_graphs(b);
-    for (LifeCase* c : b->cases) life_case_destroy(c);
+    if (b->owns_cases)
+        for (LifeCase* c : b->cases) life_case_destroy(c);
     if (b->d_tnow) cudaFree(b->d_tnow);
     if (b->d_cases) cudaFree(b->d_cases);
     if (b->d_tile_case) cudaFree(b->d_tile_case);
@@ -241,6 +243,7 @@ static int capture_step(LifeBatch* b, int phase, cudaGraphExec_t* out, int* kern
 
 static int build_graphs(LifeBatch* b) {
     drop_graphs(b);
+    for (LifeCase* c : b->cases) CK(cudaStreamSynchronize(c->stream));
     const int n = (int)b->cases.size();
     if (int rc = refill_steps(b, 4)) return rc;
     if (int rc = upload_case_table(b)) return rc;
@@ -331,6 +334,59 @@ static int run_batch(LifeBatch* b, int nsteps, cudaEvent_t start, cudaEvent_t st
     return check_status(b);
 }
 
+static int init_batch(LifeBatch* b, int n_cases) {
+    cudaGetDevice(&b->device);
+    cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, b->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_int, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->t1);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_tnow, sizeof(int) * n_cases);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_cases, sizeof(BatchLatCase) * n_cases);
+    if (e != cudaSuccess) return cuda_fail(e, "batch setup");
+    return LIFE_OK;
+}
+
+namespace life {
+// A batch over cases the caller keeps (the server's active set). The cases
+// must share one storage form; each case's queued work must be complete.
+int batch_wrap(const std::vector<LifeCase*>& cases, LifeBatch** out) {
+    *out = nullptr;
+    if (cases.empty()) return set_error(LIFE_ERR_INVALID, "empty batch");
+    LifeBatch* b = new LifeBatch();
+    b->owns_cases = false;
+    b->prec = cases[0]->p.precision;
+    for (LifeCase* c : cases) {
+        if (c->p.precision != b->prec) {
+            delete b;
+            return set_error(LIFE_ERR_INVALID, "all cases of a batch must use the same population storage form");
+        }
+        b->sites += (long long)c->Nx * c->Ny;
+    }
+    if (int rc = init_batch(b, (int)cases.size())) {
+        free_batch(b);
+        return rc;
+    }
+    b->cases = cases;
+    b->ring_end.assign(cases.size(), 0);
+    *out = b;
+    return LIFE_OK;
+}
+void batch_free(LifeBatch* b) { free_batch(b); }
+int batch_steps(LifeBatch* b, int nsteps) { return life_batch_step(b, nsteps); }
+// Per-case device status after a failed batch run: the index of the first
+// failing case (or -1) and its code.
+int batch_failed_case(LifeBatch* b, int* code) {
+    for (size_t k = 0; k < b->cases.size(); k++)
+        if (b->cases[k]->status_code) {
+            *code = b->cases[k]->status_code;
+            return (int)k;
+        }
+    return -1;
+}
+}  // namespace life
+
 extern "C" int life_batch_create(const LifeCaseParams* params, const LifeBodyDesc* bodies, const int32_t* n_bodies,
                                  int32_t n_cases, LifeBatch** out) {
     if (!out) return set_error(LIFE_ERR_INVALID, "out is NULL");
@@ -340,19 +396,10 @@ extern "C" int life_batch_create(const LifeCaseParams* params, const LifeBodyDes
         if (params[k].precision != params[0].precision)
             return set_error(LIFE_ERR_INVALID, "all cases of a batch must use the same population storage form");
     LifeBatch* b = new LifeBatch();
-    cudaGetDevice(&b->device);
     b->prec = params[0].precision;
-    cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, b->device);
-    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_int, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
-    if (e == cudaSuccess) e = cudaEventCreate(&b->t1);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_tnow, sizeof(int) * n_cases);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_cases, sizeof(BatchLatCase) * n_cases);
-    if (e != cudaSuccess) {
+    if (int rc = init_batch(b, n_cases)) {
         free_batch(b);
-        return cuda_fail(e, "life_batch_create");
+        return rc;
     }
     size_t off = 0;
     for (int k = 0; k < n_cases; k++) {

@@ -16,7 +16,8 @@ from typing import Dict, Optional, Sequence
 
 import numpy as np
 
-from .abi import ERRORS, LifeBatchInfo, LifeCaseInfo, LifeStatus, body_structs, params_struct
+from .abi import (ERRORS, LifeBatchInfo, LifeCaseInfo, LifeRequestInfo, LifeServerConfig, LifeServerStats,
+                  LifeStatus, body_structs, params_struct)
 from .case import CaseParams
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -62,6 +63,16 @@ SIGNATURES = {
     "life_batch_autotune": (C.c_int, [C.c_void_p, _ip, _ip, C.POINTER(C.c_float)]),
     "life_batch_interior_ms": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
     "life_batch_bench_steps": (C.c_int, [C.c_void_p, C.c_int32, _dp, _ip]),
+    "life_server_create": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "life_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                     C.POINTER(C.c_int64)]),
+    "life_server_query": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
+    "life_server_wait": (C.c_int, [C.c_void_p, C.c_int64, C.c_double]),
+    "life_server_take": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]),
+    "life_server_release": (C.c_int, [C.c_void_p, C.c_int64]),
+    "life_server_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "life_server_drain": (C.c_int, [C.c_void_p, C.c_double]),
+    "life_server_destroy": (C.c_int, [C.c_void_p]),
 }
 
 
@@ -313,6 +324,73 @@ class Batch:
         tot, kn = C.c_double(), C.c_int32()
         _check(lib().life_batch_bench_steps(self._h, int(n), C.byref(tot), C.byref(kn)))
         return tot.value, kn.value
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
+
+
+class Server:
+    """Request loop on the GPU (``life_server_*``): submit cases, wait for
+    them, take their final state as a :class:`Case`."""
+
+    def __init__(self, hbm_budget: int, max_active: int = 0, steps_per_round: int = 0):
+        cfg = LifeServerConfig(int(hbm_budget), int(max_active), int(steps_per_round))
+        h = C.c_void_p()
+        _check(lib().life_server_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self._params = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().life_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, params: CaseParams, bodies: Sequence, steps: int) -> int:
+        ps = params_struct(params)
+        bs = body_structs(bodies)
+        rid = C.c_int64()
+        _check(lib().life_server_submit(self._h, C.byref(ps), C.byref(bs), len(bodies), int(steps),
+                                        C.byref(rid)))
+        self._params[rid.value] = params
+        return rid.value
+
+    def query(self, rid: int) -> LifeRequestInfo:
+        inf = LifeRequestInfo()
+        _check(lib().life_server_query(self._h, int(rid), C.byref(inf)))
+        return inf
+
+    def wait(self, rid: int, timeout: float = -1.0) -> None:
+        _check(lib().life_server_wait(self._h, int(rid), float(timeout)))
+
+    def take(self, rid: int) -> Case:
+        h = C.c_void_p()
+        _check(lib().life_server_take(self._h, int(rid), C.byref(h)))
+        c = Case(self._params[rid], _handle=h)
+        c._owned = True
+        return c
+
+    def release(self, rid: int) -> None:
+        _check(lib().life_server_release(self._h, int(rid)))
+
+    def stats(self) -> LifeServerStats:
+        st = LifeServerStats()
+        _check(lib().life_server_stats(self._h, C.byref(st)))
+        return st
+
+    def drain(self, timeout: float = -1.0) -> None:
+        _check(lib().life_server_drain(self._h, float(timeout)))
 
 
 def parse_geometry(text: str):
