@@ -32,7 +32,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "MLUPS"
+METRIC = "MLUPS & HBM-roofline %, FP32 vs FP64 at stated error; p50/p99 solve latency"
 WORKLOAD = "lid_driven_cavity_4096x4096_d2q9_bgk"
 
 
@@ -84,8 +84,61 @@ def peaks():
     return 6800.0, "fallback"
 
 
+class NvmlSampler:
+    """SM clock and clock-event reasons read through NVML (libnvidia-ml, read
+    only) every `period` seconds on a thread, so that timed regions of tens of
+    milliseconds still get many samples."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, device: int, period: float = 0.002):
+        import ctypes
+        import threading
+        self.C, self.period = ctypes, period
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(device, ctypes.byref(self.h)) != 0:
+            raise RuntimeError("no NVML handle")
+        self.reason_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.rows, self.stop, self.th = [], threading.Event(), None
+        self.threading = threading
+
+    def _read(self):
+        C = self.C
+        mhz, mx, rs = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        self.lib.nvmlDeviceGetClockInfo(self.h, 1, C.byref(mhz))
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, C.byref(mx))
+        self.reason_fn(self.h, C.byref(rs))
+        return mhz.value, mx.value, rs.value
+
+    def __enter__(self):
+        def run():
+            while not self.stop.is_set():
+                self.rows.append(self._read())
+                self.stop.wait(self.period)
+        self.rows.append(self._read())
+        self.th = self.threading.Thread(target=run, daemon=True)
+        self.th.start()
+        return self
+
+    def __exit__(self, *exc):
+        self.stop.set()
+        self.th.join()
+        self.rows.append(self._read())
+
+    def summary(self):
+        sm = sorted(r[0] for r in self.rows)
+        reasons = sorted({name for r in self.rows for bit, name in self.REASONS.items() if r[2] & bit})
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(r[1] for r in self.rows), "reasons": reasons,
+                "samples": len(self.rows), "source": "nvml"}
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region."""
+    """Clocks and throttle reasons during the timed region: NVML when it
+    loads, else nvidia-smi at 200 ms."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -100,8 +153,14 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.path = None
+        self.nvml = None
 
     def __enter__(self):
+        try:
+            self.nvml = NvmlSampler(self.device).__enter__()
+            return self
+        except Exception:
+            self.nvml = None
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
@@ -113,6 +172,9 @@ class ClockSampler:
         return self
 
     def __exit__(self, *exc):
+        if self.nvml is not None:
+            self.nvml.__exit__(*exc)
+            return
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -121,6 +183,8 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml is not None:
+            return self.nvml.summary()
         rows = []
         try:
             for line in open(self.path):
@@ -469,9 +533,11 @@ def run_gb300(args, world, rank, local):
     cpu = None
     if rank == 0 and world == 1 and not args.quick:
         cp = cavity_params(n, PREC_F64)
-        mlups, dt = cpu_oracle_mlups(cp, 2, 1)
+        m1, d1 = cpu_oracle_mlups(cp, 1, 1)
+        k = max(2, min(400, int(10.0 / max(d1, 1e-3))))  # about 10 s of CPU work
+        mlups, dt = cpu_oracle_mlups(cp, k, 1)
         cpu = {"value": round(mlups, 3), "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"2 full steps of the {n}x{n} FP64 lattice after 1 warm-up ({dt:.1f} s)"}
+               "sample": f"{k} full steps of the {n}x{n} FP64 lattice after 1 warm-up ({dt:.1f} s)"}
 
     if rank == 0:
         line = {
@@ -494,6 +560,16 @@ def run_gb300(args, world, rank, local):
             "clocks": clocks,
             "extras": extras,
         }
+        if "fp64_mlups" in extras:
+            line["fp32_vs_fp64"] = {"fp32_over_fp64_mlups": extras["fp32_over_fp64"],
+                                    "fp32_velocity_rel_err": extras["fp32_velocity_rel_err"],
+                                    "fp16_velocity_rel_err": extras["fp16_velocity_rel_err"]}
+        if "serving" in extras:
+            sv = extras["serving"]
+            line["latency"] = {"p50_s": sv["latency_s_p50"], "p95_s": sv["latency_s_p95"],
+                               "p99_s": sv["latency_s_p99"],
+                               "workload": f"Poisson stream of {sv['requests']} canopy solves at "
+                                           f"{sv['load']:.0%} of measured capacity"}
         print(json.dumps(line), flush=True)
     return 0
 
