@@ -465,30 +465,121 @@ __device__ void band_factor_smem(double* Bd, int nn, int kl, int ku, int W, int*
     }
 }
 
-// Transposed solve M^T x = y in place by one warp; kl + ku <= 31, kl <= 31.
-// Forward (U^T): column-oriented. Lane r % 32 keeps the partial sum of row r;
-// when y[k] is final every row r in (k, k + kl + ku] subtracts U(k, r) y[k].
-// Each row still subtracts its terms in ascending k, as the row-oriented
-// loop does, so every sum is formed in the same order.
-// Backward (L^T): lane l forms the product of the multiplier stored in band
-// row i+1+l with y at its final row Fp[i+1+l]; the products are subtracted
-// in ascending final row, the order of the dense solve.
-__device__ void band_solve_warp(const double* Bd_, int nn, int kl, int ku, int W, const int* piv, int* Fp, double* y) {
-    double* Bd = const_cast<double*>(Bd_);
-    const int lane = threadIdx.x & 31;
-    const int w = kl + ku;
-    double t = lane < nn ? y[lane] : 0.0;
-    for (int k = 0; k < nn; k++) {
-        const int owner = k & 31;
-        const double tk = __shfl_sync(0xffffffffu, t, owner);
-        const double yk = tk / bd(Bd, W, kl, k, k);
-        if (lane == owner) {
-            y[k] = yk;
-            t = k + 32 < nn ? y[k + 32] : 0.0;
+__device__ __forceinline__ void named_bar(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// Band LU of M and the forward half of the transposed solve (U^T y = b, y in
+// place), pipelined over warps 0-2 of the CTA; kl <= 31 and kl + ku <= 31.
+// The operations are those of band_factor_smem followed by the row-ordered
+// forward substitution; only who does them, and when, differs:
+//   warp 0: column j's pivot (and its reciprocal), the row swap, the scaling,
+//           and the step-j update of column j+1, then barrier 1;
+//   warp 1: after barrier 1, the step-j update of columns j+2..kmax, then
+//           barrier 2 (which warp 0 waits on before the swap of step j+1,
+//           the first thing to touch those rows again);
+//   warp 2: after barrier 1, forward row j (row j of U is final once the swap
+//           of step j is done): y_j = t_j / U(j,j) and every row r in
+//           (j, j+kl+ku] subtracts U(j,r) y_j. Each row still subtracts its
+//           terms in ascending order, so every sum is formed as before.
+// Barrier counts: warp 0 calls barrier 1 nn times and barrier 2 nn-1 times
+// (before each swap after the first), warp 1 calls barrier 1 nn times and
+// barrier 2 after every step but the last, warp 2 calls barrier 1 nn times;
+// the k-th calls pair up, so every barrier completes.
+__device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* piv, double* y) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (blockDim.x < 96) {  // fewer than three warps: the same operations on warp 0
+        if (warp == 0) {
+            band_factor_smem(Bd, nn, kl, ku, W, piv);
+            if (lane == 0)
+                for (int i = 0; i < nn; i++) {
+                    double t = y[i];
+                    for (int k = (i - kl - ku > 0 ? i - kl - ku : 0); k < i; k++) t -= bd(Bd, W, kl, k, i) * y[k];
+                    y[i] = t / bd(Bd, W, kl, i, i);
+                }
+            __syncwarp();
         }
-        const int r = k + 1 + ((lane - k - 1) & 31);
-        if (r <= k + w && r < nn) t = t - bd(Bd, W, kl, k, r) * yk;
+        return;
     }
+    if (warp == 0) {
+        for (int j = 0; j < nn; j++) {
+            const int imax = j + kl < nn - 1 ? j + kl : nn - 1;
+            const int kmax = j + kl + ku < nn - 1 ? j + kl + ku : nn - 1;
+            const bool valid = j + lane <= imax;
+            const double v = valid ? bd(Bd, W, kl, j + lane, j) : 0.0;
+            const double rc = 1.0 / v;
+            unsigned long long key = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+            if (key > 0x7ff0000000000000ull) key = lane == 0 ? ~0ull : 0ull;
+            const unsigned kh = (unsigned)(key >> 32), klo = (unsigned)key;
+            const unsigned mh = __reduce_max_sync(0xffffffffu, valid ? kh : 0u);
+            const bool c1 = valid && kh == mh;
+            const unsigned ml = __reduce_max_sync(0xffffffffu, c1 ? klo : 0u);
+            const int src = __ffs(__ballot_sync(0xffffffffu, c1 && klo == ml)) - 1;
+            const int jp = j + src;
+            const double pv = __shfl_sync(0xffffffffu, v, src);
+            const double r = __shfl_sync(0xffffffffu, rc, src);
+            if (lane == 0) piv[j] = jp;
+            if (j > 0) named_bar(2, 64);
+            if (pv != 0.0) {
+                if (jp != j) {
+                    for (int c = j + lane; c <= kmax; c += 32) {
+                        const double t = bd(Bd, W, kl, j, c);
+                        bd(Bd, W, kl, j, c) = bd(Bd, W, kl, jp, c);
+                        bd(Bd, W, kl, jp, c) = t;
+                    }
+                    __syncwarp();
+                }
+                for (int i = j + 1 + lane; i <= imax; i += 32) bd(Bd, W, kl, i, j) *= r;
+            }
+            __syncwarp();
+            if (j + 1 <= kmax)
+                for (int i = j + 1 + lane; i <= imax; i += 32) {
+                    const double t = -bd(Bd, W, kl, j, j + 1);
+                    bd(Bd, W, kl, i, j + 1) += bd(Bd, W, kl, i, j) * t;
+                }
+            named_bar(1, 96);
+        }
+    } else if (warp == 1) {
+        for (int j = 0; j < nn; j++) {
+            named_bar(1, 96);
+            const int imax = j + kl < nn - 1 ? j + kl : nn - 1;
+            const int kmax = j + kl + ku < nn - 1 ? j + kl + ku : nn - 1;
+            const int rows = imax - j, cols = kmax - j - 1;
+            for (int q = lane; q < rows * cols; q += 32) {
+                const int i = j + 1 + q % rows, k = j + 2 + q / rows;
+                const double t = -bd(Bd, W, kl, j, k);
+                bd(Bd, W, kl, i, k) += bd(Bd, W, kl, i, j) * t;
+            }
+            if (j < nn - 1) named_bar(2, 64);
+        }
+    } else if (warp == 2) {
+        const int w = kl + ku;
+        double t = lane < nn ? y[lane] : 0.0;
+        for (int k = 0; k < nn; k++) {
+            named_bar(1, 96);
+            const int owner = k & 31;
+            const double tk = __shfl_sync(0xffffffffu, t, owner);
+            const double yk = tk / bd(Bd, W, kl, k, k);
+            if (lane == owner) {
+                y[k] = yk;
+                t = k + 32 < nn ? y[k + 32] : 0.0;
+            }
+            const int rr = k + 1 + ((lane - k - 1) & 31);
+            if (rr <= k + w && rr < nn) t = t - bd(Bd, W, kl, k, rr) * yk;
+        }
+        __syncwarp();
+    }
+}
+
+// Backward half of the transposed solve (L^T), one warp, after
+// band_lu_forward: lane l forms the product of the multiplier stored in band
+// row i+1+l with y at its final row Fp[i+1+l] (Fp: nn ints of scratch) and
+// puts it at its rank among those rows; lane 0 subtracts them in ascending
+// final row, the order of the dense solve. Then the row interchanges.
+__device__ void band_solve_back(const double* Bd_, int nn, int kl, int W, const int* piv, int* Fp, double* y) {
+    double* Bd = const_cast<double*>(Bd_);
+    __shared__ double s_prod[32];
+    const int lane = threadIdx.x & 31;
     for (int r = lane; r < nn; r += 32) Fp[r] = r;
     __syncwarp();
     for (int i = nn - 1; i >= 0; i--) {
@@ -496,16 +587,13 @@ __device__ void band_solve_warp(const double* Bd_, int nn, int kl, int ku, int W
         const int m = rmax - i;
         const bool act = lane < m;
         const int fk = act ? Fp[i + 1 + lane] : 0x7fffffff;
-        const double pr = act ? bd(Bd, W, kl, i + 1 + lane, i) * y[fk] : 0.0;
         int rank = 0;
         for (int q = 0; q < m; q++) rank += __shfl_sync(0xffffffffu, fk, q) < fk ? 1 : 0;
-        double ti = y[i];
-        for (int q = 0; q < m; q++) {
-            const int src = __ffs(__ballot_sync(0xffffffffu, act && rank == q)) - 1;
-            ti = ti - __shfl_sync(0xffffffffu, pr, src);
-        }
+        if (act) s_prod[rank] = bd(Bd, W, kl, i + 1 + lane, i) * y[fk];
         __syncwarp();
         if (lane == 0) {
+            double ti = y[i];
+            for (int q = 0; q < m; q++) ti = ti - s_prod[q];
             y[i] = ti;
             const int p = piv[i];
             const int tmp = Fp[i];
@@ -514,13 +602,13 @@ __device__ void band_solve_warp(const double* Bd_, int nn, int kl, int ku, int W
         }
         __syncwarp();
     }
-    for (int i = nn - 1; i >= 0; i--) {
-        if (lane == 0 && piv[i] != i) {
-            const double tt = y[i];
-            y[i] = y[piv[i]];
-            y[piv[i]] = tt;
-        }
-    }
+    if (lane == 0)
+        for (int i = nn - 1; i >= 0; i--)
+            if (piv[i] != i) {
+                const double tt = y[i];
+                y[i] = y[piv[i]];
+                y[piv[i]] = tt;
+            }
     __syncwarp();
 }
 
@@ -687,10 +775,9 @@ __device__ bool epsilon_fast(const FsiDev& F, const MarkerDev& M, int m0, int di
             if (pp >= 0) bd(Bd, W, kl, pp % dim, pp / dim) = cval[c];
         }
         __syncthreads();
-        if (threadIdx.x < 32) {
-            band_factor_smem(Bd, dim, kl, ku, W, sp);
-            band_solve_warp(Bd, dim, kl, ku, W, sp, fp, y);
-        }
+        if (threadIdx.x < 96) band_lu_forward(Bd, dim, kl, ku, W, sp, y);
+        __syncthreads();
+        if (threadIdx.x < 32) band_solve_back(Bd, dim, kl, W, sp, fp, y);
         __syncthreads();
         for (int i = threadIdx.x; i < dim; i += blockDim.x) M.eps[m0 + i] = y[i];
         __syncthreads();
@@ -750,10 +837,13 @@ __device__ void epsilon_range(const FsiDev& F, const MarkerDev& M, int m0, int d
             if (eps_near(M, m0 + i, m0 + j, Dx)) bd(Bd, W, kl, j, i) = eps_entry(M, m0 + i, m0 + j, Dx);
         }
         __syncthreads();
-        if (threadIdx.x < 32) {
+        if (kl + ku < 32) {
+            if (threadIdx.x < 96) band_lu_forward(Bd, dim, kl, ku, W, sp, y);
+            __syncthreads();
+            if (threadIdx.x < 32) band_solve_back(Bd, dim, kl, W, sp, fp, y);
+        } else if (threadIdx.x < 32) {
             band_factor_smem(Bd, dim, kl, ku, W, sp);
-            if (kl + ku < 32) band_solve_warp(Bd, dim, kl, ku, W, sp, fp, y);
-            else if (threadIdx.x == 0) band_solve_smem(Bd, dim, kl, ku, W, sp, fp, y);
+            if (threadIdx.x == 0) band_solve_smem(Bd, dim, kl, ku, W, sp, fp, y);
         }
         __syncthreads();
         for (int i = threadIdx.x; i < dim; i += blockDim.x) M.eps[m0 + i] = y[i];
@@ -956,10 +1046,9 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
         }
         __syncthreads();
         // delU = solveLAPACK(K, F, bcDOFs) (src/Utils.cpp:288-311)
-        if (threadIdx.x < 32) {
-            band_factor_smem(sBd, nn, 5, 5, KW, sPiv);
-            band_solve_warp(sBd, nn, 5, 5, KW, sPiv, sFp, sY);
-        }
+        if (threadIdx.x < 96) band_lu_forward(sBd, nn, 5, 5, KW, sPiv, sY);
+        __syncthreads();
+        if (threadIdx.x < 32) band_solve_back(sBd, nn, 5, KW, sPiv, sFp, sY);
         __syncthreads();
         {
             double* dU = vec(B, V_delU);
