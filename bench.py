@@ -280,7 +280,9 @@ def run_workload(args, world, rank):
     build()
     from life_gb300.lib import Case
     if args.workload == "ensemble":
-        out = {"workload": "ensemble64", **ensemble_leg(args.steps, args.warmup)}
+        tile = tuple(int(x) for x in args.tile.split("x")) if args.tile else None
+        out = {"workload": f"ensemble{args.cases}",
+               **ensemble_leg(args.steps, args.warmup, args.cases, tile, not args.batch_only)}
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
@@ -309,7 +311,7 @@ def run_workload(args, world, rank):
     return 0
 
 
-def ensemble_leg(steps: int, warmup: int) -> dict:
+def ensemble_leg(steps: int, warmup: int, n_cases: int = 64, tile=None, sequential: bool = True) -> dict:
     """The 64-case batched ensemble (uneven lattices, cylinders or filament
     rows, BGK/CM, Re 50-300): batched FP32 and FP16 (one persistent interior
     launch and one replayed graph per batch step, autotuned tiles) against the
@@ -319,10 +321,14 @@ def ensemble_leg(steps: int, warmup: int) -> dict:
     from life_gb300.lib import Batch, Case
     out = {}
     for prec, tag in ((1, "fp32"), (2, "fp16")):
-        cs = ensemble_cases(precision=prec)
+        cs = ensemble_cases(n=n_cases, precision=prec)
         with Batch(cs) as B:
             B.step(warmup)
-            w, h, ms = B.autotune()
+            if tile:
+                w, h = tile
+                B.set_tile(w, h)
+            else:
+                w, h, ms = B.autotune()
             B.step(warmup)
             tot, kn = B.bench_steps(steps)
             inf = B.info()
@@ -332,8 +338,14 @@ def ensemble_leg(steps: int, warmup: int) -> dict:
             out[f"batched_{tag}_tile"] = [w, h]
             out[f"batched_{tag}_kernel_nodes_per_step"] = kn
             out[f"batched_{tag}_device_gb"] = round(inf.device_bytes / 1e9, 3)
+    cs = ensemble_cases(n=n_cases)
+    out["cases"] = len(cs)
+    out["sites"] = sites(cs)
+    out["bodies"] = sum(len(b) for _, b in cs)
+    if not sequential:
+        return out
     for prec, tag in ((0, "fp64"), (1, "fp32")):
-        cs = ensemble_cases(precision=prec)
+        cs = ensemble_cases(n=n_cases, precision=prec)
         n_ss, ms_tot = 0, 0.0
         k = max(10, steps // 5)
         for p, b in cs:
@@ -345,10 +357,6 @@ def ensemble_leg(steps: int, warmup: int) -> dict:
         out[f"sequential_{tag}_mlups"] = round(n_ss / (ms_tot * 1e-3) / 1e6, 1)
     out["batched_fp32_over_sequential_fp64"] = round(out["batched_fp32_mlups"] / out["sequential_fp64_mlups"], 2)
     out["batched_fp32_over_sequential_fp32"] = round(out["batched_fp32_mlups"] / out["sequential_fp32_mlups"], 2)
-    cs = ensemble_cases()
-    out["cases"] = len(cs)
-    out["sites"] = sites(cs)
-    out["bodies"] = sum(len(b) for _, b in cs)
     return out
 
 
@@ -583,6 +591,9 @@ def main():
     ap.add_argument("--nx", type=int, default=4096)
     ap.add_argument("--quick", action="store_true", help="headline measurement only")
     ap.add_argument("--requests", type=int, default=24, help="serve: requests in the stream")
+    ap.add_argument("--cases", type=int, default=64, help="ensemble: cases in the batch")
+    ap.add_argument("--tile", default="", help="ensemble: fixed tile WxH instead of the autotuner")
+    ap.add_argument("--batch-only", action="store_true", help="ensemble: skip the sequential per-case runs")
     ap.add_argument("--step-scale", type=float, default=0.02, help="serve: fraction of each request's steps")
     ap.add_argument("--workload", default="cavity", choices=["cavity", "cylinder", "filament", "ensemble", "serve"],
                     help="cavity: the headline line; cylinder/filament: timing of one IBM case; "
