@@ -208,6 +208,26 @@ int life_case_get_fem(LifeCase* c, int32_t k, double* U, double* Udot, double* U
                       double* el_angle, double* node_pos, double* node_angle);
 int life_case_get_relax(LifeCase* c, double* relax);
 
+/* Restart readers for bodies, the counterpart of life_case_set_fields for
+ * ObjectsClass::readRestart (src/Objects.cpp:979-1203). set_markers loads
+ * marker pos/vel/force [n*2] in global marker order (NULL skips a field) and
+ * then recomputes every marker's support and ds and the epsilon weights
+ * (src/Objects.cpp:1181-1192). set_fem loads flexible body k's FEM.restart
+ * arrays (3*n_fem_nodes DOF vectors, n_el element lengths/angles, n_node
+ * positions [n*2] and angles; NULL keeps the case's own) and recomputes the
+ * element transforms (src/Objects.cpp:1195-1200). set_relax sets the Aitken
+ * factor stored in FEM.restart. A restart loads fields, markers, FEM bodies
+ * and relax, in any order, before the next step. */
+int life_case_set_markers(LifeCase* c, const double* pos, const double* vel, const double* force);
+int life_case_set_fem(LifeCase* c, int32_t k, const double* U, const double* Udot, const double* Udotdot,
+                      const double* U_n, const double* U_nm1, const double* R_k, const double* el_L,
+                      const double* el_angle, const double* node_pos0, const double* node_pos,
+                      const double* node_angle0, const double* node_angle);
+int life_case_set_relax(LifeCase* c, double relax);
+/* Undeformed node positions [n*2] and angles [n] of flexible body k (the pos0
+ * and angle0 columns of FEM.restart). */
+int life_case_get_fem0(LifeCase* c, int32_t k, double* node_pos0, double* node_angle0);
+
 /* Scalar observables computed on the device without copying the field:
  * max |u| over the lattice with a NaN check (GridClass::writeInfo,
  * src/Grid.cpp:562-588) and the total IBM force (writeTotalForces,

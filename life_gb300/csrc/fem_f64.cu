@@ -1122,6 +1122,24 @@ __global__ void __launch_bounds__(256) k_epsilon_markers(FsiDev F, MarkerDev M, 
     epsilon_range(F, M, 0, n, A, b, piv, lmax, eps_smem, kEpsSmemDoubles);
 }
 
+// Element transform after a restart load (FEMElementClass::setElementTransform,
+// src/FEMElement.cpp:255-262, called from ObjectsClass::readRestart,
+// src/Objects.cpp:1195-1200): cos and sin of the loaded angles, with the
+// same functions update_fem_values uses during a step.
+__global__ void k_fem_element_trig(double* el, int nEl) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nEl) return;
+    const double ang = el[(size_t)e * EL_STRIDE + EL_ANG];
+    el[(size_t)e * EL_STRIDE + EL_COS] = cos(ang);
+    el[(size_t)e * EL_STRIDE + EL_SIN] = sin(ang);
+}
+
+cudaError_t launch_fem_element_trig(double* el, int nEl, cudaStream_t s) {
+    if (nEl <= 0) return cudaSuccess;
+    k_fem_element_trig<<<(nEl + 127) / 128, 128, 0, s>>>(el, nEl);
+    return cudaGetLastError();
+}
+
 // The epsilon kernels take 200000 bytes of dynamic shared memory (opt-in);
 // the attribute is set once per device.
 cudaError_t epsilon_configure() {

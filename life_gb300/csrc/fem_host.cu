@@ -340,6 +340,89 @@ extern "C" int life_case_get_fem(LifeCase* c, int32_t k, double* U, double* Udot
     return LIFE_OK;
 }
 
+// Reference configuration of flexible body k's nodes (FEMNodeClass pos0 and
+// angle0, written to FEM.restart by src/Objects.cpp:1345-1360).
+extern "C" int life_case_get_fem0(LifeCase* c, int32_t k, double* node_pos0, double* node_angle0) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    FemHost* H = fem_of(c);
+    if (!H || k < 0 || k >= (int)H->bodies.size()) return set_error(LIFE_ERR_INVALID, "no such flexible body");
+    FemBodyDev D;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(&D, H->F.bodies + k, sizeof D, cudaMemcpyDeviceToHost));
+    std::vector<double> node((size_t)D.nNodes * 6);
+    CK(cudaMemcpy(node.data(), D.node, sizeof(double) * node.size(), cudaMemcpyDeviceToHost));
+    for (int q = 0; q < D.nNodes; q++) {
+        if (node_pos0) {
+            node_pos0[q * 2] = node[q * 6 + 0];
+            node_pos0[q * 2 + 1] = node[q * 6 + 1];
+        }
+        if (node_angle0) node_angle0[q] = node[q * 6 + 4];
+    }
+    return LIFE_OK;
+}
+
+// The FEM half of ObjectsClass::readRestart (src/Objects.cpp:1055-1175) for
+// flexible body k, then setElementTransform of its elements
+// (src/Objects.cpp:1195-1200). NULL skips an array.
+extern "C" int life_case_set_fem(LifeCase* c, int32_t k, const double* U, const double* Udot, const double* Udotdot,
+                                 const double* U_n, const double* U_nm1, const double* R_k, const double* el_L,
+                                 const double* el_angle, const double* node_pos0, const double* node_pos,
+                                 const double* node_angle0, const double* node_angle) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    FemHost* H = fem_of(c);
+    if (!H || k < 0 || k >= (int)H->bodies.size()) return set_error(LIFE_ERR_INVALID, "no such flexible body");
+    FemBodyDev D;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(&D, H->F.bodies + k, sizeof D, cudaMemcpyDeviceToHost));
+    const int n = D.n;
+    auto vecin = [&](int name, const double* src) -> cudaError_t {
+        if (!src) return cudaSuccess;
+        return cudaMemcpy(D.pool + (size_t)D.slots[name] * n, src, sizeof(double) * n, cudaMemcpyHostToDevice);
+    };
+    CK(vecin(V_U, U));
+    CK(vecin(V_Udot, Udot));
+    CK(vecin(V_Udotdot, Udotdot));
+    CK(vecin(V_Un, U_n));
+    CK(vecin(V_Unm1, U_nm1));
+    CK(vecin(V_Rk, R_k));
+    std::vector<double> el((size_t)D.nEl * EL_STRIDE), node((size_t)D.nNodes * 6);
+    CK(cudaMemcpy(el.data(), D.el, sizeof(double) * el.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(node.data(), D.node, sizeof(double) * node.size(), cudaMemcpyDeviceToHost));
+    for (int e = 0; e < D.nEl; e++) {
+        if (el_L) el[(size_t)e * EL_STRIDE + EL_L] = el_L[e];
+        if (el_angle) el[(size_t)e * EL_STRIDE + EL_ANG] = el_angle[e];
+    }
+    for (int q = 0; q < D.nNodes; q++) {
+        if (node_pos0) {
+            node[q * 6 + 0] = node_pos0[q * 2];
+            node[q * 6 + 1] = node_pos0[q * 2 + 1];
+        }
+        if (node_pos) {
+            node[q * 6 + 2] = node_pos[q * 2];
+            node[q * 6 + 3] = node_pos[q * 2 + 1];
+        }
+        if (node_angle0) node[q * 6 + 4] = node_angle0[q];
+        if (node_angle) node[q * 6 + 5] = node_angle[q];
+    }
+    CK(cudaMemcpy(D.el, el.data(), sizeof(double) * el.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.node, node.data(), sizeof(double) * node.size(), cudaMemcpyHostToDevice));
+    CK(launch_fem_element_trig(D.el, D.nEl, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return LIFE_OK;
+}
+
+// The Aitken factor of FEM.restart (src/Objects.cpp:1065-1073).
+extern "C" int life_case_set_relax(LifeCase* c, double relax) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    if (!c->d_fsi) return set_error(LIFE_ERR_INVALID, "case has no immersed bodies");
+    FsiScalars h{};
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(&h, c->d_fsi, sizeof h, cudaMemcpyDeviceToHost));
+    h.relax = relax;
+    CK(cudaMemcpy(c->d_fsi, &h, sizeof h, cudaMemcpyHostToDevice));
+    return LIFE_OK;
+}
+
 extern "C" int life_case_get_relax(LifeCase* c, double* relax) {
     if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
     if (!c->d_fsi) {

@@ -74,6 +74,7 @@ struct FsiDev {
 // Shared memory k_fem_dynamic needs for a body of n DOFs, bc constrained.
 size_t fem_dynamic_smem(int n, int bc);
 cudaError_t fem_dynamic_configure(size_t smem);
+cudaError_t launch_fem_element_trig(double* el, int nEl, cudaStream_t s);
 
 // One subiteration's kernels. With `cond`, the launch is being captured into
 // the body of a WHILE graph node and the residual kernel sets its condition;

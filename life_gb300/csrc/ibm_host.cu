@@ -143,6 +143,36 @@ extern "C" int life_case_get_markers(LifeCase* c, double* pos, double* vel, doub
     return LIFE_OK;
 }
 
+// The IBM half of ObjectsClass::readRestart (src/Objects.cpp:981-1053):
+// marker positions, velocities and forces in global marker order (NULL
+// skips a field), then findSupport + computeDs of every marker and
+// computeEpsilon (src/Objects.cpp:1181-1192), on the host as at start-up.
+// Rigid bodies keep their construction epsilon in the reference (it skips
+// them after step 0); recomputing it from the same positions gives the same
+// values.
+extern "C" int life_case_set_markers(LifeCase* c, const double* pos, const double* vel, const double* force) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    const int n = (int)c->obj.m.size();
+    if (n == 0) return LIFE_OK;
+    CK(cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < n; k++) {
+        HMarker& m = c->obj.m[k];
+        for (int d = 0; d < 2; d++) {
+            if (pos) m.pos[d] = pos[2 * k + d];
+            if (vel) m.vel[d] = vel[2 * k + d];
+            if (force) m.force[d] = force[2 * k + d];
+        }
+    }
+    std::string err;
+    for (int k = 0; k < n; k++)
+        if (int rc = host_find_support(c->g0, c->obj.m[k], &err)) return set_error(rc, err);
+    for (int k = 0; k < n; k++) host_compute_ds(c->g0, c->obj, k);
+    if (int rc = host_compute_epsilon(c->g0, c->obj, c->p.uni_epsilon != 0, true, &err)) return set_error(rc, err);
+    if (int rc = push_markers(c)) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return LIFE_OK;
+}
+
 extern "C" int life_case_get_bodies(LifeCase* c, int32_t* ids, int32_t* flexible, int32_t* n_markers,
                                     int32_t* n_fem_nodes) {
     if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");

@@ -44,6 +44,10 @@ SIGNATURES = {
     "life_case_get_bodies": (C.c_int, [C.c_void_p, _ip, _ip, _ip, _ip]),
     "life_case_get_fem": (C.c_int, [C.c_void_p, C.c_int32] + [_dp] * 10),
     "life_case_get_relax": (C.c_int, [C.c_void_p, _dp]),
+    "life_case_set_markers": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "life_case_set_fem": (C.c_int, [C.c_void_p, C.c_int32] + [_dp] * 12),
+    "life_case_set_relax": (C.c_int, [C.c_void_p, C.c_double]),
+    "life_case_get_fem0": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp]),
     "life_case_max_velocity": (C.c_int, [C.c_void_p, _dp, _ip]),
     "life_case_total_force": (C.c_int, [C.c_void_p, _dp, _dp]),
     "life_parse_geometry": (C.c_int, [C.c_char_p, C.c_void_p, C.c_int32, _ip]),
@@ -218,7 +222,22 @@ class Case:
         out["pos"], out["angle"] = np.empty((nn, 2)), np.empty(nn)
         _check(lib().life_case_get_fem(self._h, k, *[_p(out[key]) for key in keys], _p(out["el_L"]),
                                        _p(out["el_angle"]), _p(out["pos"]), _p(out["angle"])))
+        out["pos0"], out["angle0"] = np.empty((nn, 2)), np.empty(nn)
+        _check(lib().life_case_get_fem0(self._h, k, _p(out["pos0"]), _p(out["angle0"])))
         return out
+
+    def set_markers(self, pos=None, vel=None, force=None) -> None:
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (pos, vel, force)]
+        _check(lib().life_case_set_markers(self._h, *[_p(a) for a in arrs]))
+
+    def set_fem(self, k: int, U=None, Udot=None, Udotdot=None, U_n=None, U_nm1=None, R_k=None, el_L=None,
+                el_angle=None, pos0=None, pos=None, angle0=None, angle=None) -> None:
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+                for a in (U, Udot, Udotdot, U_n, U_nm1, R_k, el_L, el_angle, pos0, pos, angle0, angle)]
+        _check(lib().life_case_set_fem(self._h, int(k), *[_p(a) for a in arrs]))
+
+    def set_relax(self, relax: float) -> None:
+        _check(lib().life_case_set_relax(self._h, float(relax)))
 
     def relax(self) -> float:
         r = C.c_double()

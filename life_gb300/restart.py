@@ -164,3 +164,86 @@ def write_fem_restart(path: str, r: FEMRestart) -> None:
             fh.write(np.ascontiguousarray(np.stack([b.el_L, b.el_angle], 1), "<f8").tobytes())
             nd = np.hstack([b.pos0, b.pos, b.angle0[:, None], b.angle[:, None]])
             fh.write(np.ascontiguousarray(nd, "<f8").tobytes())
+
+
+def save_case(case, directory: str) -> None:
+    """Writes a running case's state as the reference's restart set:
+    ``Fluid.restart``, and ``IBM.restart`` / ``FEM.restart`` when it has
+    bodies (ObjectsClass::writeRestart, reference src/Objects.cpp:1206-1371)."""
+    import os
+    os.makedirs(directory, exist_ok=True)
+    inf = case.info()
+    fl = case.fields()
+    write_fluid_restart(os.path.join(directory, "Fluid.restart"), FluidRestart(
+        inf.t, inf.Nx, inf.Ny, case.params.omega, inf.Dx, inf.Dt, inf.Dm,
+        fl["rho"], fl["u"], fl["force_ibm"], fl["f"]))
+    if not case.n_markers:
+        return
+    b = case.bodies()
+    mk = case.markers()
+    ibm = IBMRestart([], [], [], [])
+    start = 0
+    for ib in range(len(b["ids"])):
+        n = int(b["n_markers"][ib])
+        sl = slice(start, start + n)
+        ibm.ids.append(int(b["ids"][ib]))
+        ibm.pos.append(mk["pos"][sl])
+        ibm.vel.append(mk["vel"][sl])
+        ibm.force.append(mk["force"][sl])
+        start += n
+    write_ibm_restart(os.path.join(directory, "IBM.restart"), ibm)
+    flex = [ib for ib in range(len(b["ids"])) if b["flexible"][ib]]
+    if not flex:
+        return
+    fem = FEMRestart(case.relax())
+    for k, ib in enumerate(flex):
+        d = case.fem(k)
+        fem.bodies.append(FEMBodyRestart(int(b["ids"][ib]), d["U"], d["Udot"], d["Udotdot"], d["U_n"], d["U_nm1"],
+                                         d["R_k"], d["el_L"], d["el_angle"], d["pos0"], d["pos"], d["angle0"],
+                                         d["angle"]))
+    write_fem_restart(os.path.join(directory, "FEM.restart"), fem)
+
+
+def load_case(case, directory: str) -> int:
+    """Loads a restart set into a freshly created case of the same geometry,
+    with the reference's rules (Utils::readRestart, src/Utils.cpp:82-101;
+    GridClass::readRestart, src/Grid.cpp:1072-1160; ObjectsClass::readRestart,
+    src/Objects.cpp:979-1203): bodies are matched by ID, bodies missing from
+    the case are skipped, a marker or node count that differs is an error.
+    Returns the restart time step."""
+    import os
+    fr = read_fluid_restart(os.path.join(directory, "Fluid.restart"))
+    if (fr.Nx, fr.Ny) != (case.params.Nx, case.params.Ny):
+        raise ValueError("Fluid.restart lattice does not match the case")
+    case.set_fields(fr.t, fr.rho, fr.u, fr.f, fr.force_ibm)
+    ipath, fpath = os.path.join(directory, "IBM.restart"), os.path.join(directory, "FEM.restart")
+    if case.n_markers and os.path.exists(ipath):
+        b = case.bodies()
+        mk = case.markers()
+        starts = np.concatenate([[0], np.cumsum(b["n_markers"])])
+        byid = {int(bid): ib for ib, bid in enumerate(b["ids"])}
+        ir = read_ibm_restart(ipath)
+        for bid, p, v, f in zip(ir.ids, ir.pos, ir.vel, ir.force):
+            ib = byid.get(bid)
+            if ib is None:
+                continue
+            sl = slice(int(starts[ib]), int(starts[ib + 1]))
+            if len(p) != sl.stop - sl.start:
+                raise ValueError("Number of nodes in IBM.restart do not match existing number of nodes")
+            mk["pos"][sl], mk["vel"][sl], mk["force"][sl] = p, v, f
+        case.set_markers(mk["pos"], mk["vel"], mk["force"])
+    if case.n_flex and os.path.exists(fpath):
+        b = case.bodies()
+        flex = [ib for ib in range(len(b["ids"])) if b["flexible"][ib]]
+        kof = {int(b["ids"][ib]): k for k, ib in enumerate(flex)}
+        fr2 = read_fem_restart(fpath)
+        case.set_relax(fr2.relax)
+        for fb in fr2.bodies:
+            k = kof.get(fb.ID)
+            if k is None:
+                continue
+            if len(fb.pos) != int(b["n_fem_nodes"][flex[k]]):
+                raise ValueError("Number of nodes/elements in FEM.restart do not match existing number")
+            case.set_fem(k, fb.U, fb.Udot, fb.Udotdot, fb.U_n, fb.U_nm1, fb.R_k, fb.el_L, fb.el_angle,
+                         fb.pos0, fb.pos, fb.angle0, fb.angle)
+    return fr.t
