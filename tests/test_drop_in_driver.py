@@ -1,6 +1,8 @@
 """The C++ drop-in driver (life_gb300/host/life_main.cpp) builds against an
 unmodified LIFE case directory (its params.h + input/geometry.config), and on
-the GPU writes a Fluid.restart equal to the reference's own dump."""
+the GPU writes a Fluid.restart equal to the reference's own dump. Run twice in
+one directory it resumes from its own restart set, as the reference's main
+does, and ends where one uninterrupted run of twice the steps ends."""
 import os
 import subprocess
 
@@ -15,11 +17,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLD = os.path.join(ROOT, "tests", "golden")
 
 
-def build_driver(tmp_path, name):
+def build_driver(tmp_path, name, params=None, tag=""):
     from life_gb300.build import build
     lib = build()
     p, bodies = golden_cases()[name]
-    case = tmp_path / name
+    if params is not None:
+        p = params
+    case = tmp_path / (name + tag)
     (case / "input").mkdir(parents=True)
     (case / "params.h").write_text(p.to_params_h())
     if bodies:
@@ -58,3 +62,27 @@ def test_driver_restart_dump_matches_reference(tmp_path, name):
         assert np.array_equal(r.f, g["f"])
         assert np.array_equal(r.u, g["u"])
         assert np.array_equal(r.rho, g["rho"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["cylinder_rigid_cm", "filament_flex_deflect", "honami_like_cm"])
+def test_driver_resumes_from_its_restart_set(tmp_path, name):
+    import dataclasses
+    p, _ = golden_cases()[name]
+    n = 30
+    half = dataclasses.replace(p, nSteps=n, tRestart=n, tinfo=n, tVTK=n)
+    full = dataclasses.replace(p, nSteps=2 * n, tRestart=2 * n, tinfo=2 * n, tVTK=2 * n)
+    case_a, exe_a = build_driver(tmp_path, name, half, "_half")
+    for _ in range(2):
+        res = subprocess.run([str(exe_a)], cwd=case_a, capture_output=True, text=True)
+        assert res.returncode == 0, res.stdout[-2000:]
+    assert "Restarting from time step 30" in res.stdout
+    case_b, exe_b = build_driver(tmp_path, name, full, "_full")
+    res = subprocess.run([str(exe_b)], cwd=case_b, capture_output=True, text=True)
+    assert res.returncode == 0, res.stdout[-2000:]
+    for fn in ("Fluid.restart", "IBM.restart", "FEM.restart"):
+        fa, fb = case_a / "Results" / "Restart" / fn, case_b / "Results" / "Restart" / fn
+        assert fa.exists() == fb.exists(), fn
+        if fa.exists():
+            assert fa.read_bytes() == fb.read_bytes(), fn
+    assert (case_a / "Results" / "Restart" / "FEM.restart").exists() == (name != "cylinder_rigid_cm")
