@@ -470,25 +470,29 @@ __device__ __forceinline__ void named_bar(int id, int nthreads) {
 }
 
 // Band LU of M and the forward half of the transposed solve (U^T y = b, y in
-// place), pipelined over warps 0-2 of the CTA; kl <= 31 and kl + ku <= 31.
+// place), pipelined over warps 0-3 of the CTA; kl <= 31 and kl + ku <= 31.
 // The operations are those of band_factor_smem followed by the row-ordered
 // forward substitution; only who does them, and when, differs:
-//   warp 0: column j's pivot (and its reciprocal), the row swap, the scaling,
-//           and the step-j update of column j+1, then barrier 1;
-//   warp 1: after barrier 1, the step-j update of columns j+2..kmax, then
-//           barrier 2 (which warp 0 waits on before the swap of step j+1,
-//           the first thing to touch those rows again);
+//   warp 0: column j's pivot, the row swap, the scaling and the step-j update
+//           of column j+1, then barrier 1. Column j+1's candidates are then
+//           already in its registers (the rows it just updated, plus one row
+//           no earlier step touched), so the reciprocal of the next pivot
+//           candidates starts before the barrier;
+//   warps 1, 3: after barrier 1, the step-j update of columns j+2..kmax,
+//           split between them, then barrier 2 (which warp 0 waits on before
+//           the swap of step j+1, the first thing to touch those rows again);
 //   warp 2: after barrier 1, forward row j (row j of U is final once the swap
 //           of step j is done): y_j = t_j / U(j,j) and every row r in
 //           (j, j+kl+ku] subtracts U(j,r) y_j. Each row still subtracts its
 //           terms in ascending order, so every sum is formed as before.
 // Barrier counts: warp 0 calls barrier 1 nn times and barrier 2 nn-1 times
-// (before each swap after the first), warp 1 calls barrier 1 nn times and
-// barrier 2 after every step but the last, warp 2 calls barrier 1 nn times;
-// the k-th calls pair up, so every barrier completes.
+// (before each swap after the first); warps 1 and 3 call barrier 1 nn times
+// and barrier 2 after every step but the last; warp 2 calls barrier 1 nn
+// times. The k-th calls pair up, so every barrier completes. Needs at least
+// 128 threads; with fewer, warp 0 does everything.
 __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* piv, double* y) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (blockDim.x < 96) {  // fewer than three warps: the same operations on warp 0
+    if (blockDim.x < 128) {
         if (warp == 0) {
             band_factor_smem(Bd, nn, kl, ku, W, piv);
             if (lane == 0)
@@ -502,12 +506,13 @@ __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* 
         return;
     }
     if (warp == 0) {
+        // lane l holds the pivot candidate M(j+l, j) and its reciprocal
+        double v = lane <= (kl < nn - 1 ? kl : nn - 1) ? bd(Bd, W, kl, lane, 0) : 0.0;
+        double rc = __drcp_rn(v);
         for (int j = 0; j < nn; j++) {
             const int imax = j + kl < nn - 1 ? j + kl : nn - 1;
             const int kmax = j + kl + ku < nn - 1 ? j + kl + ku : nn - 1;
             const bool valid = j + lane <= imax;
-            const double v = valid ? bd(Bd, W, kl, j + lane, j) : 0.0;
-            const double rc = 1.0 / v;
             unsigned long long key = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
             if (key > 0x7ff0000000000000ull) key = lane == 0 ? ~0ull : 0ull;
             const unsigned kh = (unsigned)(key >> 32), klo = (unsigned)key;
@@ -517,46 +522,89 @@ __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* 
             const int src = __ffs(__ballot_sync(0xffffffffu, c1 && klo == ml)) - 1;
             const int jp = j + src;
             const double pv = __shfl_sync(0xffffffffu, v, src);
-            const double r = __shfl_sync(0xffffffffu, rc, src);
+            const double v0 = __shfl_sync(0xffffffffu, v, 0);
             if (lane == 0) piv[j] = jp;
-            if (j > 0) named_bar(2, 64);
-            if (pv != 0.0) {
-                if (jp != j) {
-                    for (int c = j + lane; c <= kmax; c += 32) {
-                        const double t = bd(Bd, W, kl, j, c);
-                        bd(Bd, W, kl, j, c) = bd(Bd, W, kl, jp, c);
-                        bd(Bd, W, kl, jp, c) = t;
-                    }
-                    __syncwarp();
-                }
-                for (int i = j + 1 + lane; i <= imax; i += 32) bd(Bd, W, kl, i, j) *= r;
+            // pivot != 0 (NaN counts as non-zero), tested on the bits
+            const bool nz = ((unsigned long long)__double_as_longlong(pv) << 1) != 0ull;
+            const bool swapped = nz && jp != j;
+            if (j > 0) named_bar(2, 96);
+            const int c = j + lane;
+            double rj = 0.0, rp = 0.0;
+            if (c <= kmax) {
+                rj = bd(Bd, W, kl, j, c);
+                rp = bd(Bd, W, kl, jp, c);
             }
+            const bool mrow = lane >= 1 && j + lane <= imax;  // multiplier row i = j + lane
+            const bool early = j + 1 <= kmax;
+            double x = 0.0;
+            if (mrow && early) x = bd(Bd, W, kl, j + lane, j + 1);
+            const double oj1 = __shfl_sync(0xffffffffu, rj, 1);  // old M(j, j+1)
+            const double op1 = __shfl_sync(0xffffffffu, rp, 1);  // old M(jp, j+1)
+            const double r = __shfl_sync(0xffffffffu, rc, src);
             __syncwarp();
-            if (j + 1 <= kmax)
-                for (int i = j + 1 + lane; i <= imax; i += 32) {
-                    const double t = -bd(Bd, W, kl, j, j + 1);
-                    bd(Bd, W, kl, i, j + 1) += bd(Bd, W, kl, i, j) * t;
-                }
-            named_bar(1, 96);
+            // post-swap values
+            const double a = (swapped && j + lane == jp) ? v0 : v;
+            const double u1 = swapped ? op1 : oj1;
+            if (swapped && j + lane == jp) x = oj1;
+            const double L = nz ? a * r : a;
+            double nx = 0.0;
+            // x + L * (-u1), written as the identical x - L * u1
+            if (mrow && early) nx = x - L * u1;
+            // column j+1's candidates: rows j+1..imax were just updated (lane
+            // l+1 holds row j+1+l); row j+1+kl, if it exists, is untouched
+            if (j + 1 < nn) {
+                const int imax1 = j + 1 + kl < nn - 1 ? j + 1 + kl : nn - 1;
+                const int row = j + 1 + lane;
+                double nv = __shfl_down_sync(0xffffffffu, nx, 1);
+                if (row > imax1) nv = 0.0;
+                else if (row > imax) nv = bd(Bd, W, kl, row, j + 1);
+                v = nv;
+                rc = __drcp_rn(v);
+            }
+            if (swapped && c <= kmax) {
+                bd(Bd, W, kl, j, c) = rp;
+                if (c >= j + 2) bd(Bd, W, kl, jp, c) = rj;
+            }
+            if (mrow) {
+                bd(Bd, W, kl, j + lane, j) = L;
+                if (early) bd(Bd, W, kl, j + lane, j + 1) = nx;
+            }
+            named_bar(1, 128);
         }
-    } else if (warp == 1) {
+    } else if (warp == 1 || warp == 3) {
+        // entry q of the kl x (kl+ku-1) block of a full step, kept in registers
+        const int q0 = lane + (warp == 3 ? 32 : 0);
+        const int fr = kl > 0 ? kl : 1, fc = kl + ku - 1;
+        const int qi0 = q0 % fr, qk0 = q0 / fr, qi1 = (q0 + 64) % fr, qk1 = (q0 + 64) / fr;
         for (int j = 0; j < nn; j++) {
-            named_bar(1, 96);
+            named_bar(1, 128);
             const int imax = j + kl < nn - 1 ? j + kl : nn - 1;
             const int kmax = j + kl + ku < nn - 1 ? j + kl + ku : nn - 1;
             const int rows = imax - j, cols = kmax - j - 1;
-            for (int q = lane; q < rows * cols; q += 32) {
-                const int i = j + 1 + q % rows, k = j + 2 + q / rows;
-                const double t = -bd(Bd, W, kl, j, k);
-                bd(Bd, W, kl, i, k) += bd(Bd, W, kl, i, j) * t;
+            if (rows == kl && cols == fc && rows * cols <= 128) {
+                // bd(i,k) + bd(i,j) * (-bd(j,k)), written as the identical
+                // bd(i,k) - bd(i,j) * bd(j,k)
+                if (q0 < rows * cols) {
+                    const int i = j + 1 + qi0, k = j + 2 + qk0;
+                    bd(Bd, W, kl, i, k) = bd(Bd, W, kl, i, k) - bd(Bd, W, kl, i, j) * bd(Bd, W, kl, j, k);
+                }
+                if (q0 + 64 < rows * cols) {
+                    const int i = j + 1 + qi1, k = j + 2 + qk1;
+                    bd(Bd, W, kl, i, k) = bd(Bd, W, kl, i, k) - bd(Bd, W, kl, i, j) * bd(Bd, W, kl, j, k);
+                }
+            } else {
+                for (int q = q0; q < rows * cols; q += 64) {
+                    const int i = j + 1 + q % rows, k = j + 2 + q / rows;
+                    bd(Bd, W, kl, i, k) = bd(Bd, W, kl, i, k) - bd(Bd, W, kl, i, j) * bd(Bd, W, kl, j, k);
+                }
             }
-            if (j < nn - 1) named_bar(2, 64);
+            if (j < nn - 1) named_bar(2, 96);
         }
     } else if (warp == 2) {
         const int w = kl + ku;
         double t = lane < nn ? y[lane] : 0.0;
         for (int k = 0; k < nn; k++) {
-            named_bar(1, 96);
+            named_bar(1, 128);
             const int owner = k & 31;
             const double tk = __shfl_sync(0xffffffffu, t, owner);
             const double yk = tk / bd(Bd, W, kl, k, k);
@@ -580,6 +628,34 @@ __device__ void band_solve_back(const double* Bd_, int nn, int kl, int W, const 
     double* Bd = const_cast<double*>(Bd_);
     __shared__ double s_prod[32];
     const int lane = threadIdx.x & 31;
+    bool any = false;
+    for (int i0 = 0; i0 < nn; i0 += 32) {
+        const int i = i0 + lane;
+        any |= __any_sync(0xffffffffu, i < nn && piv[i] != i);
+    }
+    if (!any) {
+        // No interchange: every multiplier stays in its row, the final rows
+        // are i+1..i+kl in ascending order, and lane l's product is the l-th
+        // term. The newest value y[i+1] is lane 0's running sum of the
+        // previous row.
+        double ti = 0.0;
+        for (int i = nn - 1; i >= 0; i--) {
+            const int m = (i + kl < nn - 1 ? i + kl : nn - 1) - i;
+            const bool act = lane < m;
+            double yv = 0.0, bv = 0.0;
+            if (act) {
+                bv = bd(Bd, W, kl, i + 1 + lane, i);
+                yv = lane == 0 ? ti : y[i + 1 + lane];
+            }
+            const double pr = bv * yv;
+            double acc = y[i];
+            for (int q = 0; q < m; q++) acc = acc - __shfl_sync(0xffffffffu, pr, q);
+            ti = acc;
+            if (lane == 0) y[i] = ti;
+            __syncwarp();
+        }
+        return;
+    }
     for (int r = lane; r < nn; r += 32) Fp[r] = r;
     __syncwarp();
     for (int i = nn - 1; i >= 0; i--) {
@@ -775,7 +851,7 @@ __device__ bool epsilon_fast(const FsiDev& F, const MarkerDev& M, int m0, int di
             if (pp >= 0) bd(Bd, W, kl, pp % dim, pp / dim) = cval[c];
         }
         __syncthreads();
-        if (threadIdx.x < 96) band_lu_forward(Bd, dim, kl, ku, W, sp, y);
+        if (threadIdx.x < 128) band_lu_forward(Bd, dim, kl, ku, W, sp, y);
         __syncthreads();
         if (threadIdx.x < 32) band_solve_back(Bd, dim, kl, W, sp, fp, y);
         __syncthreads();
@@ -838,7 +914,7 @@ __device__ void epsilon_range(const FsiDev& F, const MarkerDev& M, int m0, int d
         }
         __syncthreads();
         if (kl + ku < 32) {
-            if (threadIdx.x < 96) band_lu_forward(Bd, dim, kl, ku, W, sp, y);
+            if (threadIdx.x < 128) band_lu_forward(Bd, dim, kl, ku, W, sp, y);
             __syncthreads();
             if (threadIdx.x < 32) band_solve_back(Bd, dim, kl, W, sp, fp, y);
         } else if (threadIdx.x < 32) {
@@ -1046,7 +1122,7 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
         }
         __syncthreads();
         // delU = solveLAPACK(K, F, bcDOFs) (src/Utils.cpp:288-311)
-        if (threadIdx.x < 96) band_lu_forward(sBd, nn, 5, 5, KW, sPiv, sY);
+        if (threadIdx.x < 128) band_lu_forward(sBd, nn, 5, 5, KW, sPiv, sY);
         __syncthreads();
         if (threadIdx.x < 32) band_solve_back(sBd, nn, 5, KW, sPiv, sFp, sY);
         __syncthreads();
