@@ -558,7 +558,8 @@ def run_gb300(args, world, rank, local):
                        "parallelism": f"replicas{world}", "l2": "state 1.2 GB > L2 (no flush needed)"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                          "frac": round(achieved / hbm, 4), "traffic": traffic,
-                         "peak_source": f"{hbm_kind} hbm_gbs", "kernel": "k_interior_lowp<BGK,F32>",
+                         "peak_source": f"{hbm_kind} hbm_gbs",
+                         "kernel": "k_step_lowp<BGK,F32> (boundary perimeter + interior, one launch per step)",
                          "algorithmic_bytes_per_site": bytes_per_site, "kernel_ms": round(inner_ms, 4)},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e, 1), "unit": "MLUPS", "h2d_bytes_per_step": round(h2d / args.steps),

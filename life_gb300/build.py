@@ -40,7 +40,7 @@ UNITS: List[Tuple[str, List[str]]] = [
     ("lbm_f64.cu", ["--fmad=false"]),
     ("ibm_f64.cu", ["--fmad=false"]),
     ("fem_f64.cu", ["--fmad=false"]),
-    ("lbm_lowp.cu", ["--fmad=true"]),
+    ("lbm_lowp.cu", ["--fmad=false"]),
     ("life_case.cu", ["--fmad=false"]),
     ("ibm_host.cu", ["--fmad=false"]),
     ("fem_host.cu", ["--fmad=false"]),

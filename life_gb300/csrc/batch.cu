@@ -74,6 +74,8 @@ struct LifeBatch {
     std::string status_msg;
     int status_code = 0;
     bool owns_cases = true;
+    bool owns_stream = true;
+    std::vector<BatchLatCase> h_cases;  // host copy of the case table
 };
 
 static void drop_graphs(LifeBatch* b) {
@@ -95,7 +97,7 @@ static void free_batch(LifeBatch* b) {
     if (b->d_tile_case) cudaFree(b->d_tile_case);
     for (cudaEvent_t e : {b->ev_fork, b->ev_int, b->t0, b->t1})
         if (e) cudaEventDestroy(e);
-    if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->stream && b->owns_stream) cudaStreamDestroy(b->stream);
     delete b;
 }
 
@@ -135,6 +137,7 @@ static int upload_case_table(LifeBatch* b) {
     const int per_sm = b->prec == LIFE_PREC_F64 ? batch_blocks_per_sm_f64(b->tile_w)
                                                 : batch_blocks_per_sm_lowp(b->prec, b->tile_w);
     b->grid = std::max(1, std::min(tile0, b->num_sms * std::max(per_sm, 1)));
+    b->h_cases = h;
     CK(cudaMemcpyAsync(b->d_cases, h.data(), sizeof(BatchLatCase) * n, cudaMemcpyHostToDevice, b->stream));
     CK(cudaMemcpyAsync(b->d_tile_case, tc.data(), sizeof(int) * tc.size(), cudaMemcpyHostToDevice, b->stream));
     std::vector<int> tn(n);
@@ -145,6 +148,15 @@ static int upload_case_table(LifeBatch* b) {
 }
 
 static cudaError_t launch_batch_interior(LifeBatch* b, int phase, cudaStream_t s) {
+    if (b->cases.size() == 1) {
+        // one case: its own interior kernel (one CTA row segment per block);
+        // in the reduced-precision forms the launch also takes the perimeter
+        const BatchLatCase& C = b->h_cases[0];
+        const LatDev& L = C.L[phase];
+        const int t = b->cases[0]->t + 1 + phase;  // ignored: kernels read *L.t_dev + L.t_off
+        if (b->prec == LIFE_PREC_F64) return launch_interior_f64((const double*)C.A[phase], (double*)C.B[phase], L, t, s);
+        return launch_step_lowp(C.A[phase], C.B[phase], L, t, s);
+    }
     if (b->prec == LIFE_PREC_F64)
         return launch_interior_batch_f64(b->d_cases, b->d_tile_case, b->ntiles, b->tile_w, b->tile_h, b->grid, phase,
                                          s);
@@ -168,38 +180,46 @@ static int refill_steps(LifeBatch* b, int n) {
 
 // Captures one batch step at the cases' current state and advances the host
 // view of every case by that step (t, buffer parity, IBM scratch parity).
+// Per case, the convective outlet and the boundary perimeter run on the
+// case's side stream; the interior launch waits only for the outlets (the
+// perimeter and the interior both read P[cur] and write disjoint sites of
+// P[cur^1], so they overlap); the immersed-boundary work waits for both.
 static int capture_step(LifeBatch* b, int phase, cudaGraphExec_t* out, int* kernels) {
     cudaStream_t bs = b->stream;
     const int n = (int)b->cases.size();
     CK(cudaStreamBeginCapture(bs, cudaStreamCaptureModeThreadLocal));
     int rc = LIFE_OK;
     cudaError_t e = cudaEventRecord(b->ev_fork, bs);
-    // outlet and boundary perimeter of every case, on the case streams
     for (int k = 0; k < n && e == cudaSuccess && rc == LIFE_OK; k++) {
         LifeCase* c = b->cases[k];
         c->t_dev = b->d_tnow + k;
         c->t_off = 1;
         const int tt = c->t + 1;
         const LatDev L = lattice_view(c, tt);
-        e = cudaStreamWaitEvent(c->stream, b->ev_fork, 0);
-        if (e == cudaSuccess && L.convective) e = launch_outlet(L, c->d_delU, c->stream);
-        if (e == cudaSuccess) e = launch_perimeter(c->P[c->cur], c->P[c->cur ^ 1], L, tt, c->stream);
-        if (e == cudaSuccess) e = cudaEventRecord(c->ev_fork, c->stream);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(bs, c->ev_fork, 0);
+        e = cudaStreamWaitEvent(c->side, b->ev_fork, 0);
+        if (e == cudaSuccess && L.convective) {
+            e = launch_outlet(L, c->d_delU, c->side);
+            if (e == cudaSuccess) e = cudaEventRecord(c->ev_out, c->side);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(bs, c->ev_out, 0);
+        }
+        const bool fused = n == 1 && b->prec != LIFE_PREC_F64;  // perimeter inside the interior launch
+        if (e == cudaSuccess && !fused) e = launch_perimeter(c->P[c->cur], c->P[c->cur ^ 1], L, tt, c->side);
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev_join, c->side);
     }
-    // every case's interior in one launch
     if (e == cudaSuccess && rc == LIFE_OK) e = launch_batch_interior(b, phase, bs);
     if (e == cudaSuccess) e = cudaEventRecord(b->ev_int, bs);
-    // immersed boundaries per case, then the join
     for (int k = 0; k < n && e == cudaSuccess && rc == LIFE_OK; k++) {
         LifeCase* c = b->cases[k];
         const int tt = c->t + 1;
         const void* A = c->P[c->cur];
         void* B = c->P[c->cur ^ 1];
-        e = cudaStreamWaitEvent(c->stream, b->ev_int, 0);
+        if (c->stream != bs) e = cudaStreamWaitEvent(c->stream, b->ev_int, 0);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_join, 0);
         if (e == cudaSuccess && c->obj.hasIBM) rc = ibm_step(c, tt, A, B);
-        if (e == cudaSuccess && rc == LIFE_OK) e = cudaEventRecord(c->ev_join, c->stream);
-        if (e == cudaSuccess && rc == LIFE_OK) e = cudaStreamWaitEvent(bs, c->ev_join, 0);
+        if (c->stream != bs) {
+            if (e == cudaSuccess && rc == LIFE_OK) e = cudaEventRecord(c->ev_done, c->stream);
+            if (e == cudaSuccess && rc == LIFE_OK) e = cudaStreamWaitEvent(bs, c->ev_done, 0);
+        }
         c->cur ^= 1;
         c->t = tt;
     }
@@ -306,7 +326,7 @@ static int check_status(LifeBatch* b) {
     return LIFE_OK;
 }
 
-static int run_batch(LifeBatch* b, int nsteps, cudaEvent_t start, cudaEvent_t stop) {
+static int run_batch(LifeBatch* b, int nsteps, cudaEvent_t start, cudaEvent_t stop, bool check = true) {
     if (graph_phase(b) < 0)
         if (int rc = build_graphs(b)) return rc;
     // the device step counters follow the host view
@@ -331,13 +351,19 @@ static int run_batch(LifeBatch* b, int nsteps, cudaEvent_t start, cudaEvent_t st
         }
     }
     if (stop) CK(cudaEventRecord(stop, b->stream));
-    return check_status(b);
+    return check ? check_status(b) : LIFE_OK;
 }
 
-static int init_batch(LifeBatch* b, int n_cases) {
+static int init_batch(LifeBatch* b, int n_cases, cudaStream_t use_stream = nullptr) {
     cudaGetDevice(&b->device);
     cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, b->device);
-    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    cudaError_t e = cudaSuccess;
+    if (use_stream) {
+        b->stream = use_stream;
+        b->owns_stream = false;
+    } else {
+        e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_int, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
@@ -374,6 +400,34 @@ int batch_wrap(const std::vector<LifeCase*>& cases, LifeBatch** out) {
     return LIFE_OK;
 }
 void batch_free(LifeBatch* b) { free_batch(b); }
+
+static int self_batch(LifeCase* c) {
+    if (c->self_batch) return LIFE_OK;
+    LifeBatch* b = new LifeBatch();
+    b->owns_cases = false;
+    b->prec = c->p.precision;
+    b->sites = (long long)c->Nx * c->Ny;
+    if (int rc = init_batch(b, 1, c->stream)) {
+        free_batch(b);
+        return rc;
+    }
+    b->cases = {c};
+    b->ring_end.assign(1, 0);
+    c->self_batch = b;
+    return LIFE_OK;
+}
+
+int case_graph_steps(LifeCase* c, int nsteps, cudaEvent_t start, cudaEvent_t stop) {
+    if (int rc = self_batch(c)) return rc;
+    return run_batch(c->self_batch, nsteps, start, stop, false);
+}
+
+int case_interior_ms(LifeCase* c, int reps, float* ms) {
+    if (int rc = self_batch(c)) return rc;
+    return life_batch_interior_ms(c->self_batch, reps, ms);
+}
+
+int case_kernels_per_step(LifeCase* c) { return c->self_batch ? c->self_batch->kernel_nodes[0] : 0; }
 int batch_steps(LifeBatch* b, int nsteps) { return life_batch_step(b, nsteps); }
 // Per-case device status after a failed batch run: the index of the first
 // failing case (or -1) and its code.

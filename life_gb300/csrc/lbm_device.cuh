@@ -318,4 +318,55 @@ __device__ __forceinline__ void collide(const double f[9], double rho, double ux
     else collide_bgk(f, rho, ux, uy, Fx, Fy, omega, fs);
 }
 
+// Outlet side outputs of step t: final u of the last three columns and the
+// post-BC f[2,6,8] of the outlet column.
+__device__ __forceinline__ void outlet_outputs(const LatDev& L, int i, int j, const double f[9], double ux, double uy) {
+    if (!L.convective) return;
+    int c = i - (L.Nx - 3);
+    if (c >= 0) {
+        L.outlet_u[((size_t)c * L.Ny + j) * 2 + 0] = ux;
+        L.outlet_u[((size_t)c * L.Ny + j) * 2 + 1] = uy;
+    }
+    if (i == L.Nx - 1) {
+        double* o = L.outlet_f_next + (size_t)j * 3;
+        o[0] = f[2];
+        o[1] = f[6];
+        o[2] = f[8];
+    }
+}
+
+template <bool CM, class S>
+__device__ __forceinline__ void store_collided(typename S::T* __restrict__ B, const LatDev& L, int t_next, int i,
+                                               int j, const double f[9], double rho, double ux, double uy, double Ix,
+                                               double Iy) {
+    double Fx, Fy, fs[9];
+    force_xy_at(L, t_next, Fx, Fy);
+    collide<CM>(f, rho, ux, uy, Fx + Ix, Fy + Iy, L.omega, L.cs, fs);
+    const size_t s = (size_t)j * L.pitch + i;
+#pragma unroll
+    for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = S::save(fs[v], v);
+}
+
+
+// Boundary-condition site q of the perimeter, enumerated bottom row, top row,
+// left column, right column: its step-t state by site_state() (regularised /
+// convective conditions applied), the outlet side outputs, and the collision
+// of the next step into B. FP64 arithmetic for every storage form.
+template <bool CM, class S>
+__device__ __forceinline__ void perimeter_site(const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
+                                               const LatDev& L, int t, int q) {
+    const int Nx = L.Nx, Ny = L.Ny;
+    int i, j;
+    if (q < Nx) { i = q; j = 0; }
+    else if (q < 2 * Nx) { i = q - Nx; j = Ny - 1; }
+    else if (q < 2 * Nx + (Ny - 2)) { i = 0; j = q - 2 * Nx + 1; }
+    else if (q < 2 * Nx + 2 * (Ny - 2)) { i = Nx - 1; j = q - 2 * Nx - (Ny - 2) + 1; }
+    else return;
+    if (site_type(L, i, j) == LIFE_FLUID) return;
+    double f[9], rho, ux, uy;
+    site_state<CM, S>(A, L, t, i, j, f, rho, ux, uy);
+    outlet_outputs(L, i, j, f, ux, uy);
+    store_collided<CM, S>(B, L, t + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
+}
+
 }  // namespace life

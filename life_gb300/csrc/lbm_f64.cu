@@ -21,35 +21,6 @@
 
 namespace life {
 
-// Outlet side outputs of step t: final u of the last three columns and the
-// post-BC f[2,6,8] of the outlet column.
-__device__ __forceinline__ void outlet_outputs(const LatDev& L, int i, int j, const double f[9], double ux, double uy) {
-    if (!L.convective) return;
-    int c = i - (L.Nx - 3);
-    if (c >= 0) {
-        L.outlet_u[((size_t)c * L.Ny + j) * 2 + 0] = ux;
-        L.outlet_u[((size_t)c * L.Ny + j) * 2 + 1] = uy;
-    }
-    if (i == L.Nx - 1) {
-        double* o = L.outlet_f_next + (size_t)j * 3;
-        o[0] = f[2];
-        o[1] = f[6];
-        o[2] = f[8];
-    }
-}
-
-template <bool CM, class S>
-__device__ __forceinline__ void store_collided(typename S::T* __restrict__ B, const LatDev& L, int t_next, int i,
-                                               int j, const double f[9], double rho, double ux, double uy, double Ix,
-                                               double Iy) {
-    double Fx, Fy, fs[9];
-    force_xy_at(L, t_next, Fx, Fy);
-    collide<CM>(f, rho, ux, uy, Fx + Ix, Fy + Iy, L.omega, L.cs, fs);
-    const size_t s = (size_t)j * L.pitch + i;
-#pragma unroll
-    for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = S::save(fs[v], v);
-}
-
 // GridClass::initialiseGrid (reference src/Grid.cpp:998-1061): rho = 1,
 // initial velocity, f = feq; then the collision of step t0+1.
 template <bool CM, class S>
@@ -122,24 +93,11 @@ __global__ void __launch_bounds__(256) k_interior_batch_f64(const BatchLatCase* 
     }
 }
 
-// Boundary-condition sites of one step (any storage form, FP64 arithmetic):
-// the perimeter is enumerated bottom row, top row, left column, right column.
+// Boundary-condition sites of one step, FP64 storage (perimeter_site,
+// lbm_device.cuh); the reduced-precision forms have theirs in lbm_lowp.cu.
 template <bool CM, class S>
 __global__ void k_perimeter(const typename S::T* __restrict__ A, typename S::T* __restrict__ B, LatDev L, int t) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    t = step_t(L, t);
-    const int Nx = L.Nx, Ny = L.Ny;
-    int i, j;
-    if (q < Nx) { i = q; j = 0; }
-    else if (q < 2 * Nx) { i = q - Nx; j = Ny - 1; }
-    else if (q < 2 * Nx + (Ny - 2)) { i = 0; j = q - 2 * Nx + 1; }
-    else if (q < 2 * Nx + 2 * (Ny - 2)) { i = Nx - 1; j = q - 2 * Nx - (Ny - 2) + 1; }
-    else return;
-    if (site_type(L, i, j) == LIFE_FLUID) return;
-    double f[9], rho, ux, uy;
-    site_state<CM, S>(A, L, t, i, j, f, rho, ux, uy);
-    outlet_outputs(L, i, j, f, ux, uy);
-    store_collided<CM, S>(B, L, t + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
+    perimeter_site<CM, S>(A, B, L, step_t(L, t), blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // GridClass::convectiveSpeed (src/Grid.cpp:477-495): the mean outlet speed is
@@ -313,18 +271,10 @@ int batch_blocks_per_sm_f64(int tile_w) {
 }
 
 cudaError_t launch_perimeter(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
+    if (L.prec != LIFE_PREC_F64) return launch_perimeter_lowp(A, B, L, t, s);
     const int n = 2 * L.Nx + 2 * (L.Ny - 2);
-    const dim3 grid((n + 127) / 128);
-    if (L.prec == LIFE_PREC_F64) {
-        if (L.cm) k_perimeter<true, StoreF64><<<grid, 128, 0, s>>>((const double*)A, (double*)B, L, t);
-        else k_perimeter<false, StoreF64><<<grid, 128, 0, s>>>((const double*)A, (double*)B, L, t);
-    } else if (L.prec == LIFE_PREC_F32) {
-        if (L.cm) k_perimeter<true, StoreF32><<<grid, 128, 0, s>>>((const float*)A, (float*)B, L, t);
-        else k_perimeter<false, StoreF32><<<grid, 128, 0, s>>>((const float*)A, (float*)B, L, t);
-    } else {
-        if (L.cm) k_perimeter<true, StoreF16><<<grid, 128, 0, s>>>((const __half*)A, (__half*)B, L, t);
-        else k_perimeter<false, StoreF16><<<grid, 128, 0, s>>>((const __half*)A, (__half*)B, L, t);
-    }
+    if (L.cm) k_perimeter<true, StoreF64><<<(n + 127) / 128, 128, 0, s>>>((const double*)A, (double*)B, L, t);
+    else k_perimeter<false, StoreF64><<<(n + 127) / 128, 128, 0, s>>>((const double*)A, (double*)B, L, t);
     return cudaGetLastError();
 }
 

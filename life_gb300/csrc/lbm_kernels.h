@@ -12,6 +12,9 @@ cudaError_t launch_init(void* B, const LatDev& L, int t0, cudaStream_t s);
 cudaError_t launch_interior_f64(const double* A, double* B, const LatDev& L, int t, cudaStream_t s);
 cudaError_t launch_interior_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s);
 cudaError_t launch_perimeter(const void* A, void* B, const LatDev& L, int t, cudaStream_t s);
+cudaError_t launch_perimeter_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s);
+// Perimeter and interior of one reduced-precision case in one launch.
+cudaError_t launch_step_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s);
 cudaError_t launch_outlet(const LatDev& L, double* delU, cudaStream_t s);
 cudaError_t launch_state(void* B, const LatDev& L, int t, const double* rho, const double* u, const double* f,
                          const double* fibm, cudaStream_t s);

@@ -1,5 +1,8 @@
 // Reduced-precision lattice kernels: FP32 shifted populations and FP16
-// storage, both collided in FP32 (compiled with FMA contraction).
+// storage, both collided in FP32. The unit is compiled without FMA
+// contraction (so the FP64 boundary code it shares with lbm_f64.cu rounds
+// exactly as there); the FP32 arithmetic spells its fused multiply-adds out
+// with fmaf().
 //
 // Interior (fluid) sites take this fast path. It holds only the deviations
 // g_v = f_v - w_v in registers:
@@ -22,6 +25,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include "collide_cm.cuh"
 #include "lbm_device.cuh"
 #include "lbm_kernels.h"
 
@@ -33,8 +37,8 @@ __device__ __forceinline__ void e1d(float u, float e[3], float w[3], float d[3])
     w[0] = 2.0f / 3.0f;
     w[1] = w[2] = 1.0f / 6.0f;
     d[0] = -u2;
-    d[1] = 0.5f * u + 0.5f * u2;
-    d[2] = -0.5f * u + 0.5f * u2;
+    d[1] = fmaf(0.5f, u, 0.5f * u2);
+    d[2] = fmaf(-0.5f, u, 0.5f * u2);
     e[0] = w[0] + d[0];
     e[1] = w[1] + d[1];
     e[2] = w[2] + d[2];
@@ -42,28 +46,40 @@ __device__ __forceinline__ void e1d(float u, float e[3], float w[3], float d[3])
 
 __device__ __forceinline__ int ax(int c) { return c == 0 ? 0 : (c > 0 ? 1 : 2); }
 
+// c_v . (a, b) for the D2Q9 velocity v (components 0 or +-1, known at
+// compile time after unrolling): only the additions and signs it needs.
+__device__ __forceinline__ float cdot(int v, float a, float b) {
+    const int cx = cx_of(v), cy = cy_of(v);
+    const float xa = cx == 0 ? 0.0f : (cx > 0 ? a : -a);
+    if (cy == 0) return xa;
+    const float yb = cy > 0 ? b : -b;
+    return cx == 0 ? yb : xa + yb;
+}
+
 template <bool CM>
 __device__ __forceinline__ void collide_dev32(const float g[9], float dr, float rho, float mx, float my, float ux,
                                               float uy, float Gx, float Gy, float omega, float gs[9]) {
     if (!CM) {
-        const float usq15 = 1.5f * (ux * ux + uy * uy);
-        const float uF = ux * Gx + uy * Gy;
-        const float fo = 1.0f - 0.5f * omega;
+        const float usq15 = 1.5f * fmaf(ux, ux, uy * uy);
+        const float uF = fmaf(ux, Gx, uy * Gy);
+        const float fo = fmaf(-0.5f, omega, 1.0f);
 #pragma unroll
         for (int v = 0; v < 9; v++) {
-            const float cx = (float)cx_of(v), cy = (float)cy_of(v), w = wgt_f(v);
-            const float cu = cx * ux + cy * uy;
-            const float cF = cx * Gx + cy * Gy;
-            const float geq = w * (dr + rho * (3.0f * cu + 4.5f * cu * cu - usq15));
-            const float Fv = 3.0f * w * ((cF - uF) + 3.0f * cu * cF);
-            gs[v] = g[v] + omega * (geq - g[v]) + fo * Fv;
+            const float w = wgt_f(v);
+            const float cu = cdot(v, ux, uy);
+            const float cF = cdot(v, Gx, Gy);
+            const float inner = fmaf(4.5f * cu, cu, fmaf(3.0f, cu, -usq15));
+            const float geq = w * fmaf(rho, inner, dr);
+            const float Fv = (3.0f * w) * fmaf(3.0f * cu, cF, cF - uF);
+            gs[v] = fmaf(fo, Fv, fmaf(omega, geq - g[v], g[v]));
         }
     } else {
         // raw second moments of the deviations
         const float dxxyy = (g[1] + g[2]) - (g[3] + g[4]);
         const float gxy = (g[5] + g[6]) - (g[7] + g[8]);
-        const float k4 = (1.0f - omega) * (dxxyy - 2.0f * ux * mx + 2.0f * uy * my + (ux * ux - uy * uy) * rho);
-        const float k5 = (1.0f - omega) * (gxy - uy * mx - ux * my + ux * uy * rho);
+        const float om1 = 1.0f - omega;
+        const float k4 = om1 * fmaf(ux * ux - uy * uy, rho, fmaf(2.0f * uy, my, fmaf(-2.0f * ux, mx, dxxyy)));
+        const float k5 = om1 * fmaf(ux * uy, rho, fmaf(-ux, my, fmaf(-uy, mx, gxy)));
         const float k1 = 0.5f * Gx, k2 = 0.5f * Gy, k7 = Gx * (1.0f / 6.0f), k6 = Gy * (1.0f / 6.0f);
         float ex[3], wx[3], dx[3], ey[3], wy[3], dy[3];
         e1d(ux, ex, wx, dx);
@@ -102,8 +118,14 @@ __device__ __forceinline__ void collide_dev32(const float g[9], float dr, float 
         for (int v = 0; v < 9; v++) {
             const int a = ax(cx_of(v)), b = ax(cy_of(v));
             const float E = ex[a] * ey[b];
-            const float D = wx[a] * dy[b] + dx[a] * wy[b] + dx[a] * dy[b];
-            gs[v] = dr * E + D + T1[v] * k1 + T2[v] * k2 + T4[v] * k4 + T5[v] * k5 + T6[v] * k6 + T7[v] * k7;
+            const float D = fmaf(dx[a], dy[b], fmaf(wx[a], dy[b], dx[a] * wy[b]));
+            float acc = fmaf(dr, E, D);
+            acc = fmaf(T1[v], k1, acc);
+            acc = fmaf(T2[v], k2, acc);
+            acc = fmaf(T4[v], k4, acc);
+            acc = fmaf(T5[v], k5, acc);
+            acc = fmaf(T6[v], k6, acc);
+            gs[v] = fmaf(T7[v], k7, acc);
         }
     }
 }
@@ -138,7 +160,7 @@ __device__ __forceinline__ void interior_site_lowp(const typename S::T* __restri
     const float mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
     const float my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
     const float inv = 1.0f / rho;
-    const float ux = (mx + 0.5f * (float)Fxd) * inv, uy = (my + 0.5f * (float)Fyd) * inv;
+    const float ux = fmaf(0.5f, (float)Fxd, mx) * inv, uy = fmaf(0.5f, (float)Fyd, my) * inv;
     if (L.convective && i >= L.Nx - 3) {
         const int c = i - (L.Nx - 3);
         L.outlet_u[((size_t)c * L.Ny + j) * 2 + 0] = ux;
@@ -192,6 +214,69 @@ cudaError_t launch_interior_lowp(const void* A, void* B, const LatDev& L, int t,
     } else {
         if (L.cm) k_interior_lowp<true, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t);
         else k_interior_lowp<false, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t);
+    }
+    return cudaGetLastError();
+}
+
+// Boundary-condition sites, reduced-precision storage (perimeter_site,
+// lbm_device.cuh; FP64 arithmetic, rounded as in lbm_f64.cu).
+template <bool CM, class S>
+__global__ void k_perimeter_lowp(const typename S::T* __restrict__ A, typename S::T* __restrict__ B, LatDev L, int t) {
+    perimeter_site<CM, S>(A, B, L, step_t(L, t), blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+cudaError_t launch_perimeter_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
+    const int n = 2 * L.Nx + 2 * (L.Ny - 2);
+    const int g = (n + 127) / 128;
+    if (L.prec == LIFE_PREC_F32) {
+        if (L.cm) k_perimeter_lowp<true, StoreF32><<<g, 128, 0, s>>>((const float*)A, (float*)B, L, t);
+        else k_perimeter_lowp<false, StoreF32><<<g, 128, 0, s>>>((const float*)A, (float*)B, L, t);
+    } else {
+        if (L.cm) k_perimeter_lowp<true, StoreF16><<<g, 128, 0, s>>>((const __half*)A, (__half*)B, L, t);
+        else k_perimeter_lowp<false, StoreF16><<<g, 128, 0, s>>>((const __half*)A, (__half*)B, L, t);
+    }
+    return cudaGetLastError();
+}
+
+// The perimeter path of k_step_lowp as a separate (not inlined) function: it
+// needs more registers than the interior path, and the spills the launch
+// bound forces stay inside it.
+template <bool CM, class S>
+__device__ __noinline__ void perimeter_site_call(const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
+                                                 const LatDev& L, int t, int q) {
+    perimeter_site<CM, S>(A, B, L, t, q);
+}
+
+// One whole step of one case in one launch: the first `pb` blocks take the
+// boundary perimeter (long FP64 chains on few sites), the rest the interior
+// rows (256 sites per block). Blocks are dispatched in index order, so the
+// perimeter starts at once and finishes under the interior's time. The
+// launch bound keeps the interior's register budget (and occupancy); the
+// perimeter path spills to local memory instead.
+template <bool CM, class S>
+__global__ void __launch_bounds__(256, 6) k_step_lowp(const typename S::T* __restrict__ A,
+                                                      typename S::T* __restrict__ B, LatDev L, int t, int pb, int bx) {
+    t = step_t(L, t);
+    if ((int)blockIdx.x < pb) {
+        perimeter_site_call<CM, S>(A, B, L, t, blockIdx.x * blockDim.x + threadIdx.x);
+        return;
+    }
+    const int b = blockIdx.x - pb;
+    const int i = (b % bx) * blockDim.x + threadIdx.x, j = b / bx;
+    if (i >= L.Nx) return;
+    interior_site_lowp<CM, S>(A, B, L, t, i, j);
+}
+
+cudaError_t launch_step_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
+    const int n = 2 * L.Nx + 2 * (L.Ny - 2);
+    const int pb = (n + 255) / 256, bx = (L.Nx + 255) / 256;
+    const unsigned grid = (unsigned)(pb + bx * L.Ny);
+    if (L.prec == LIFE_PREC_F32) {
+        if (L.cm) k_step_lowp<true, StoreF32><<<grid, 256, 0, s>>>((const float*)A, (float*)B, L, t, pb, bx);
+        else k_step_lowp<false, StoreF32><<<grid, 256, 0, s>>>((const float*)A, (float*)B, L, t, pb, bx);
+    } else {
+        if (L.cm) k_step_lowp<true, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t, pb, bx);
+        else k_step_lowp<false, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t, pb, bx);
     }
     return cudaGetLastError();
 }

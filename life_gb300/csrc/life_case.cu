@@ -9,6 +9,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -173,8 +174,11 @@ static void free_case(LifeCase* c) {
     for (void* p : c->allocs)
         if (p) cudaFree(p);
     if (c->side) cudaStreamSynchronize(c->side);
+    if (c->self_batch) batch_free(c->self_batch);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->ev_out) cudaEventDestroy(c->ev_out);
+    if (c->ev_done) cudaEventDestroy(c->ev_done);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (prev >= 0) cudaSetDevice(prev);
@@ -217,9 +221,19 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
     c->init_mode = p.has_inlet_ramp ? 0 : (p.profile >= 0 ? 1 : 2);
     c->elem = p.precision == LIFE_PREC_F64 ? 8 : (p.precision == LIFE_PREC_F32 ? 4 : 2);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    // The side stream (outlet, boundary perimeter) has the highest priority:
+    // its few blocks are then dispatched ahead of the interior launch's
+    // queued blocks and run beside them instead of after them.
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_hi);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming);
+    for (const char* var : {"LIFE_CASE_HOSTLOOP", "LIFE_FSI_HOSTLOOP"})
+        if (const char* v = std::getenv(var))
+            if (v[0] == '1') c->host_steps = true;
     if (e != cudaSuccess) {
         free_case(c);
         return cuda_fail(e, "cudaStreamCreate");
@@ -326,7 +340,21 @@ struct StepTiming {
 };
 
 static int run_steps(LifeCase* c, int nsteps, StepTiming* tm) {
-    int rc = ensure_steps(c, c->t, (nsteps < kStepChunk ? nsteps : kStepChunk) + 2);
+    int rc;
+    if (!c->host_steps) {
+        // the case's captured step graphs; the same kernels in the same order
+        if ((rc = case_graph_steps(c, nsteps, tm ? tm->start : nullptr, tm ? tm->stop : nullptr))) return rc;
+        if (tm) tm->launches = case_kernels_per_step(c) * nsteps;
+        if (c->obj.hasFlex) {
+            if ((rc = check_device_status(c))) return rc;
+            if (c->status_code) {
+                c->status_msg = "Subiteration scheme hit 20 iterations...exiting";
+                return set_error(c->status_code, c->status_msg);
+            }
+        }
+        return LIFE_OK;
+    }
+    rc = ensure_steps(c, c->t, (nsteps < kStepChunk ? nsteps : kStepChunk) + 2);
     if (rc) return rc;
     const bool conv = c->p.wall_right == LIFE_CONVECTIVE;
     if (tm) cudaEventRecord(tm->start, c->stream);
@@ -409,9 +437,15 @@ extern "C" int life_case_bench_steps(LifeCase* c, int32_t nsteps, double* total_
         float ms = 0.f;
         cudaEventElapsedTime(&ms, tm.start, tm.stop);
         tot = ms;
-        for (int k = 0; k < nsteps; k++) {
-            cudaEventElapsedTime(&ms, tm.ev[2 * k], tm.ev[2 * k + 1]);
-            inner += ms;
+        if (c->host_steps) {
+            for (int k = 0; k < nsteps; k++) {
+                cudaEventElapsedTime(&ms, tm.ev[2 * k], tm.ev[2 * k + 1]);
+                inner += ms;
+            }
+        } else {
+            // inside a graph the interior launch is timed alone afterwards
+            rc = case_interior_ms(c, 10, &ms);
+            inner = (double)ms * nsteps;
         }
     }
     for (auto& ev : tm.ev) cudaEventDestroy(ev);

@@ -32,6 +32,8 @@ int cuda_fail(cudaError_t e, const char* where);
 
 }  // namespace life
 
+struct LifeBatch;  // batch.cu
+
 struct LifeCase {
     LifeCaseParams p{};
     int device = -1;
@@ -58,7 +60,12 @@ struct LifeCase {
     unsigned long long* d_red = nullptr;
     cudaStream_t stream = nullptr;   // every kernel of the case is ordered on this stream
     cudaStream_t side = nullptr;     // perimeter kernel, forked from and joined to `stream`
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_out = nullptr, ev_done = nullptr;
+    // Captured step graphs of this case alone (a one-case batch on the case's
+    // own stream), used by life_case_step; and whether steps are launched from
+    // the host instead (LIFE_CASE_HOSTLOOP=1 or LIFE_FSI_HOSTLOOP=1).
+    LifeBatch* self_batch = nullptr;
+    bool host_steps = false;
     size_t dev_bytes = 0;
     std::vector<void*> allocs;
     // immersed bodies
@@ -81,6 +88,14 @@ struct LifeCase {
 
 namespace life {
 LatDev lattice_view(const LifeCase* c, int t);
+void batch_free(LifeBatch* b);
+// nsteps steps of one case through its cached step graphs (asynchronous);
+// with start/stop, CUDA events recorded around them on the case's stream.
+int case_graph_steps(LifeCase* c, int nsteps, cudaEvent_t start, cudaEvent_t stop);
+// Mean device time of the case's interior kernel alone over reps launches.
+int case_interior_ms(LifeCase* c, int reps, float* ms);
+// Kernel nodes of one captured step of the case (0 before the first capture).
+int case_kernels_per_step(LifeCase* c);
 void free_fem(LifeCase* c);
 int ensure_steps(LifeCase* c, int t0, int n);
 }  // namespace life
