@@ -181,6 +181,18 @@ __device__ __forceinline__ void collide_bgk(const double f[9], double rho, doubl
 __device__ __forceinline__ void collide_cm(const double f[9], double rho, double ux, double uy, double Fx,
                                            double Fy, double omega, double cs, double fs[9]);
 
+// force_xy_at in float for the FP32 kernels (values rounded on the host).
+__device__ __forceinline__ void force_xy_at_f(const LatDev& L, int t, float& Fx, float& Fy) {
+    if (L.womersley) {
+        const StepScalars& s = L.steps[t % L.steps_cap];
+        Fx = s.fx_f;
+        Fy = s.fy_f;
+    } else {
+        Fx = L.Fx0_f;
+        Fy = L.Fy0_f;
+    }
+}
+
 // Step index of a launch: its argument, or the device counter in a graph.
 __device__ __forceinline__ int step_t(const LatDev& L, int t) { return L.t_dev ? *L.t_dev + L.t_off : t; }
 

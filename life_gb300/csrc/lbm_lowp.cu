@@ -152,22 +152,22 @@ __device__ __forceinline__ void interior_site_lowp(const typename S::T* __restri
             g[v] = S::dev(A[(size_t)v * L.S + (size_t)sj * L.pitch + si], v);
         }
     }
-    double Fxd, Fyd, Gxd, Gyd;
-    force_xy_at(L, t, Fxd, Fyd);
-    force_xy_at(L, t + 1, Gxd, Gyd);
+    float Fxd, Fyd, Gxd, Gyd;
+    force_xy_at_f(L, t, Fxd, Fyd);
+    force_xy_at_f(L, t + 1, Gxd, Gyd);
     const float dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
     const float rho = 1.0f + dr;
     const float mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
     const float my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
     const float inv = 1.0f / rho;
-    const float ux = fmaf(0.5f, (float)Fxd, mx) * inv, uy = fmaf(0.5f, (float)Fyd, my) * inv;
+    const float ux = fmaf(0.5f, Fxd, mx) * inv, uy = fmaf(0.5f, Fyd, my) * inv;
     if (L.convective && i >= L.Nx - 3) {
         const int c = i - (L.Nx - 3);
         L.outlet_u[((size_t)c * L.Ny + j) * 2 + 0] = ux;
         L.outlet_u[((size_t)c * L.Ny + j) * 2 + 1] = uy;
     }
     float gs[9];
-    collide_dev32<CM>(g, dr, rho, mx, my, ux, uy, (float)Gxd, (float)Gyd, (float)L.omega, gs);
+    collide_dev32<CM>(g, dr, rho, mx, my, ux, uy, Gxd, Gyd, L.omega_f, gs);
 #pragma unroll
     for (int v = 0; v < 9; v++) B[(size_t)v * L.S + base] = S::put(gs[v], v);
 }

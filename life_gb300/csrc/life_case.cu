@@ -87,6 +87,8 @@ int life::ensure_steps(LifeCase* c, int t0, int n) {
             const double sc = (c->Dx * c->Dt) * (c->Dx * c->Dt);
             s.fx = (0.0 + p.dpdx * ph) * sc / c->Dm;
             s.fy = (0.0 + p.dpdy * ph) * sc / c->Dm;
+            s.fx_f = (float)s.fx;
+            s.fy_f = (float)s.fy;
         }
         h[k] = s;
     }
@@ -121,6 +123,9 @@ LatDev life::lattice_view(const LifeCase* c, int t) {
     L.cs = c->cs;
     L.Fx0 = c->Fx0;
     L.Fy0 = c->Fy0;
+    L.omega_f = (float)c->p.omega;
+    L.Fx0_f = (float)c->Fx0;
+    L.Fy0_f = (float)c->Fy0;
     L.u0x = c->u0x;
     L.u0y = c->u0y;
     L.init_mode = c->init_mode;

@@ -15,7 +15,7 @@ namespace life {
 struct StepScalars {
     double ramp;
     double fx, fy;
-    double pad;
+    float fx_f, fy_f;  // (float)fx, (float)fy for the reduced-precision kernels
 };
 
 // Everything a lattice kernel needs, passed by value.
@@ -30,6 +30,9 @@ struct LatDev {
     int has_ibm;
     double omega, cs;
     double Fx0, Fy0;      // constant force_xy (reference src/Grid.cpp:1035-1045)
+    // the same values rounded to float once, on the host (FP32 kernels read
+    // these instead of converting per site)
+    float omega_f, Fx0_f, Fy0_f;
     double u0x, u0y;      // initial uniform velocity (ux0_p*Dt/Dx, uy0_p*Dt/Dx)
     int init_mode;        // 0: zero velocity (ramp), 1: inlet profile, 2: uniform u0
     int steps_cap;        // steps[] is a ring: time step t lives at t % steps_cap
