@@ -117,6 +117,16 @@ __device__ __forceinline__ void gather(const typename S::T* __restrict__ P, cons
     }
 }
 
+// Terms of the reference's sums that multiply a population or velocity by a
+// lattice-velocity component of 0 are exact zeros: adding one leaves a sum
+// unchanged (the sums start at +0 and never hold -0), so the FP64 code below
+// does not form them. A component of +-1 multiplies exactly. The remaining
+// terms keep the reference's order. (After unrolling, the component tests are
+// compile-time constants.)
+__device__ __forceinline__ double add_c(double acc, int c, double x) {
+    return c == 0 ? acc : (c > 0 ? acc + x : acc - x);
+}
+
 // GridClass::macroscopic (src/Grid.cpp:282-299)
 __device__ __forceinline__ void macroscopic(const double f[9], double Fx, double Fy, double& rho,
                                             double& ux, double& uy) {
@@ -124,8 +134,8 @@ __device__ __forceinline__ void macroscopic(const double f[9], double Fx, double
 #pragma unroll
     for (int v = 0; v < 9; v++) {
         r = r + f[v];
-        mx = mx + (double)cx_of(v) * f[v];
-        my = my + (double)cy_of(v) * f[v];
+        mx = add_c(mx, cx_of(v), f[v]);
+        my = add_c(my, cy_of(v), f[v]);
     }
     rho = r;
     ux = (mx + 0.5 * Fx) / r;
@@ -140,8 +150,8 @@ __device__ __forceinline__ void macroscopic_ibm(const double f[9], double Fx, do
 #pragma unroll
     for (int v = 0; v < 9; v++) {
         r = r + f[v];
-        mx = mx + (double)cx_of(v) * f[v];
-        my = my + (double)cy_of(v) * f[v];
+        mx = add_c(mx, cx_of(v), f[v]);
+        my = add_c(my, cy_of(v), f[v]);
     }
     rho = r;
     ux = (mx + 0.5 * (Fx + Ix)) / r;
@@ -150,22 +160,35 @@ __device__ __forceinline__ void macroscopic_ibm(const double f[9], double Fx, do
 
 // GridClass::equilibrium (src/Grid.cpp:249-264): 2nd-order Hermite (BGK) or
 // the 4th-order product form used with central moments.
+// c . u without its zero-component products (c of a D2Q9 direction)
+__device__ __forceinline__ double cdot_d(int cx, int cy, double ux, double uy) {
+    if (cx == 0) return cy == 0 ? 0.0 : cy * uy;
+    return cy == 0 ? cx * ux : cx * ux + cy * uy;
+}
+
 template <bool CM>
 __device__ __forceinline__ double equilibrium(int v, double rho, double ux, double uy) {
     const int cx = cx_of(v), cy = cy_of(v);
-    if (CM)
-        return 0.25 * rho * wgt(v) * (9.0 * LSQ(cx) * LSQ(ux) + 6.0 * cx * ux - 3.0 * LSQ(ux) + 2.0) *
-               (9.0 * LSQ(cy) * LSQ(uy) + 6.0 * cy * uy - 3.0 * LSQ(uy) + 2.0);
-    return rho * wgt(v) *
-           (1.0 + 3.0 * (cx * ux + cy * uy) + 4.5 * (LSQ(ux) * (LSQ(cx) - 1.0 / 3.0) + LSQ(uy) * (LSQ(cy) - 1.0 / 3.0)) +
-            9.0 * cx * cy * ux * uy);
+    if (CM) {
+        // (9 c^2 u^2 + 6 c u - 3 u^2 + 2) per axis; for c = 0 the first two
+        // terms are exact zeros
+        const double ax = cx == 0 ? -3.0 * LSQ(ux) + 2.0 : 9.0 * LSQ(cx) * LSQ(ux) + 6.0 * cx * ux - 3.0 * LSQ(ux) + 2.0;
+        const double ay = cy == 0 ? -3.0 * LSQ(uy) + 2.0 : 9.0 * LSQ(cy) * LSQ(uy) + 6.0 * cy * uy - 3.0 * LSQ(uy) + 2.0;
+        return 0.25 * rho * wgt(v) * ax * ay;
+    }
+    double s = 1.0 + 3.0 * cdot_d(cx, cy, ux, uy);
+    s = s + 4.5 * (LSQ(ux) * (LSQ(cx) - 1.0 / 3.0) + LSQ(uy) * (LSQ(cy) - 1.0 / 3.0));
+    if (cx != 0 && cy != 0) s = s + 9.0 * cx * cy * ux * uy;
+    return rho * wgt(v) * s;
 }
 
 // GridClass::latticeForce (src/Grid.cpp:267-279), Guo forcing for BGK.
 __device__ __forceinline__ double lattice_force(int v, double ux, double uy, double Fx, double Fy) {
     const int cx = cx_of(v), cy = cy_of(v);
-    return 3.0 * wgt(v) *
-           (Fx * (cx - ux + cx * 3.0 * (cx * ux + cy * uy)) + (Fy * (cy - uy + cy * 3.0 * (cx * ux + cy * uy))));
+    const double cu = cdot_d(cx, cy, ux, uy);
+    const double tx = cx == 0 ? -ux : (cx - ux) + cx * 3.0 * cu;
+    const double ty = cy == 0 ? -uy : (cy - uy) + cy * 3.0 * cu;
+    return 3.0 * wgt(v) * (Fx * tx + Fy * ty);
 }
 
 // BGK collision (src/Grid.cpp:236-244).
