@@ -192,12 +192,16 @@ __device__ __forceinline__ double lattice_force(int v, double ux, double uy, dou
 }
 
 // BGK collision (src/Grid.cpp:236-244).
+// With no force at all (Fx = Fy = 0, a value the whole launch shares) the
+// forcing term is an exact zero added to a nonzero sum, so it is not formed.
 __device__ __forceinline__ void collide_bgk(const double f[9], double rho, double ux, double uy, double Fx,
                                             double Fy, double omega, double fs[9]) {
+    const bool forced = Fx != 0.0 || Fy != 0.0;
 #pragma unroll
-    for (int v = 0; v < 9; v++)
-        fs[v] = f[v] + omega * (equilibrium<false>(v, rho, ux, uy) - f[v]) +
-                (1.0 - 0.5 * omega) * lattice_force(v, ux, uy, Fx, Fy);
+    for (int v = 0; v < 9; v++) {
+        const double a = f[v] + omega * (equilibrium<false>(v, rho, ux, uy) - f[v]);
+        fs[v] = forced ? a + (1.0 - 0.5 * omega) * lattice_force(v, ux, uy, Fx, Fy) : a;
+    }
 }
 
 // Central-moments collision (De Rosis 2019; src/Grid.cpp:106-233), in collide_cm.cuh.
