@@ -33,7 +33,8 @@
 
 using namespace life;
 
-int ibm_step(LifeCase* c, int t, const void* A, void* B);
+int ibm_forces(LifeCase* c, int t, const void* A, cudaStream_t s);
+int ibm_apply(LifeCase* c, int t, const void* A, void* B, cudaStream_t s);
 
 #define CK(call)                                              \
     do {                                                      \
@@ -147,6 +148,16 @@ static int upload_case_table(LifeBatch* b) {
     return LIFE_OK;
 }
 
+// One reduced-precision case runs its whole lattice step in one launch when
+// the lattice is large enough for the interior to cover the boundary blocks'
+// FP64 chains; on smaller lattices the separate perimeter kernel (no register
+// cap, so no spills) runs beside the interior instead.
+static bool fused_step(const LifeBatch* b) {
+    if (b->cases.size() != 1 || b->prec == LIFE_PREC_F64) return false;
+    const LifeCase* c = b->cases[0];
+    return (long long)c->Nx * c->Ny >= (1LL << 22);
+}
+
 static cudaError_t launch_batch_interior(LifeBatch* b, int phase, cudaStream_t s) {
     if (b->cases.size() == 1) {
         // one case: its own interior kernel (one CTA row segment per block);
@@ -155,7 +166,8 @@ static cudaError_t launch_batch_interior(LifeBatch* b, int phase, cudaStream_t s
         const LatDev& L = C.L[phase];
         const int t = b->cases[0]->t + 1 + phase;  // ignored: kernels read *L.t_dev + L.t_off
         if (b->prec == LIFE_PREC_F64) return launch_interior_f64((const double*)C.A[phase], (double*)C.B[phase], L, t, s);
-        return launch_step_lowp(C.A[phase], C.B[phase], L, t, s);
+        if (fused_step(b)) return launch_step_lowp(C.A[phase], C.B[phase], L, t, s);
+        return launch_interior_lowp(C.A[phase], C.B[phase], L, t, s);
     }
     if (b->prec == LIFE_PREC_F64)
         return launch_interior_batch_f64(b->d_cases, b->d_tile_case, b->ntiles, b->tile_w, b->tile_h, b->grid, phase,
@@ -183,7 +195,9 @@ static int refill_steps(LifeBatch* b, int n) {
 // Per case, the convective outlet and the boundary perimeter run on the
 // case's side stream; the interior launch waits only for the outlets (the
 // perimeter and the interior both read P[cur] and write disjoint sites of
-// P[cur^1], so they overlap); the immersed-boundary work waits for both.
+// P[cur^1], so they overlap). The IBM forces (interpolation, or the FSI
+// subiteration loop) read only P[cur] and run beside the lattice step on the
+// case's aux stream after the outlet; the spread waits for all of them.
 static int capture_step(LifeBatch* b, int phase, cudaGraphExec_t* out, int* kernels) {
     cudaStream_t bs = b->stream;
     const int n = (int)b->cases.size();
@@ -197,14 +211,18 @@ static int capture_step(LifeBatch* b, int phase, cudaGraphExec_t* out, int* kern
         const int tt = c->t + 1;
         const LatDev L = lattice_view(c, tt);
         e = cudaStreamWaitEvent(c->side, b->ev_fork, 0);
-        if (e == cudaSuccess && L.convective) {
-            e = launch_outlet(L, c->d_delU, c->side);
-            if (e == cudaSuccess) e = cudaEventRecord(c->ev_out, c->side);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(bs, c->ev_out, 0);
-        }
-        const bool fused = n == 1 && b->prec != LIFE_PREC_F64;  // perimeter inside the interior launch
+        // the outlet reads the outlet columns before the interior rewrites them
+        if (e == cudaSuccess && L.convective) e = launch_outlet(L, c->d_delU, c->side);
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev_out, c->side);
+        if (e == cudaSuccess && L.convective) e = cudaStreamWaitEvent(bs, c->ev_out, 0);
+        const bool fused = fused_step(b);  // perimeter inside the interior launch
         if (e == cudaSuccess && !fused) e = launch_perimeter(c->P[c->cur], c->P[c->cur ^ 1], L, tt, c->side);
         if (e == cudaSuccess) e = cudaEventRecord(c->ev_join, c->side);
+        if (e == cudaSuccess && c->obj.hasIBM) {
+            e = cudaStreamWaitEvent(c->aux, c->ev_out, 0);
+            if (e == cudaSuccess) rc = ibm_forces(c, tt, c->P[c->cur], c->aux);
+            if (e == cudaSuccess && rc == LIFE_OK) e = cudaEventRecord(c->ev_aux, c->aux);
+        }
     }
     if (e == cudaSuccess && rc == LIFE_OK) e = launch_batch_interior(b, phase, bs);
     if (e == cudaSuccess) e = cudaEventRecord(b->ev_int, bs);
@@ -215,7 +233,8 @@ static int capture_step(LifeBatch* b, int phase, cudaGraphExec_t* out, int* kern
         void* B = c->P[c->cur ^ 1];
         if (c->stream != bs) e = cudaStreamWaitEvent(c->stream, b->ev_int, 0);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_join, 0);
-        if (e == cudaSuccess && c->obj.hasIBM) rc = ibm_step(c, tt, A, B);
+        if (e == cudaSuccess && c->obj.hasIBM) e = cudaStreamWaitEvent(c->stream, c->ev_aux, 0);
+        if (e == cudaSuccess && c->obj.hasIBM) rc = ibm_apply(c, tt, A, B, c->stream);
         if (c->stream != bs) {
             if (e == cudaSuccess && rc == LIFE_OK) e = cudaEventRecord(c->ev_done, c->stream);
             if (e == cudaSuccess && rc == LIFE_OK) e = cudaStreamWaitEvent(bs, c->ev_done, 0);

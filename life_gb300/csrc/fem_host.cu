@@ -245,12 +245,12 @@ static int build_fsi_graph(LifeCase* c, FemHost* H, int key, int t, const void* 
 // straight into the graph being captured: it is added after the capture's
 // current dependencies, its body is captured on the case's side stream, and
 // the capture continues after the node.
-static int embed_fsi_loop(LifeCase* c, FemHost* H, int t, const void* A, const LatDev& L) {
+static int embed_fsi_loop(LifeCase* c, FemHost* H, int t, const void* A, const LatDev& L, cudaStream_t stream) {
     cudaStreamCaptureStatus st;
     cudaGraph_t g = nullptr;
     const cudaGraphNode_t* deps = nullptr;
     size_t nd = 0;
-    CK(cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &nd));
+    CK(cudaStreamGetCaptureInfo(stream, &st, nullptr, &g, &deps, nullptr, &nd));
     cudaGraphConditionalHandle h;
     CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
     cudaGraphNodeParams np{};
@@ -269,34 +269,35 @@ static int embed_fsi_loop(LifeCase* c, FemHost* H, int t, const void* A, const L
     size_t nn = 0;
     CK(cudaGraphGetNodes(body, nullptr, &nn));
     c->loop_body_kernels = (int)nn;
-    CK(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    CK(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
     c->ibm_launches += 1;
     return LIFE_OK;
 }
 
-// The subiteration loop of one step; the spread follows in ibm_step().
-int fem_fsi_loop(LifeCase* c, int t, const void* A, const LatDev& L) {
+// The subiteration loop of one step on `stream`; the spread follows in
+// ibm_apply().
+int fem_fsi_loop(LifeCase* c, int t, const void* A, const LatDev& L, cudaStream_t stream) {
     FemHost* H = fem_of(c);
-    cudaError_t e = launch_fsi_begin(H->F, t, c->stream, c->t_dev, c->t_off);
+    cudaError_t e = launch_fsi_begin(H->F, t, stream, c->t_dev, c->t_off);
     if (e != cudaSuccess) return cuda_fail(e, "fsi_begin");
     c->ibm_launches += 1;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    CK(cudaStreamIsCapturing(c->stream, &cs));
-    if (cs == cudaStreamCaptureStatusActive) return embed_fsi_loop(c, H, t, A, L);
+    CK(cudaStreamIsCapturing(stream, &cs));
+    if (cs == cudaStreamCaptureStatusActive) return embed_fsi_loop(c, H, t, A, L, stream);
     if (!H->host_loop) {
         const int key = (A == c->P[0] ? 0 : 2) + (t & 1);
         if (!H->graph[key].exec)
             if (int rc = build_fsi_graph(c, H, key, t, A, L)) return rc;
-        e = cudaGraphLaunch(H->graph[key].exec, c->stream);
+        e = cudaGraphLaunch(H->graph[key].exec, stream);
         if (e != cudaSuccess) return cuda_fail(e, "FSI loop graph launch");
         c->ibm_launches += 1;
         return LIFE_OK;
     }
     for (int it = 0; it < 20; it++) {
-        e = launch_fsi_subiteration(H->F, c->M, A, L, t, c->Dt / c->Dx, c->stream, &c->ibm_launches);
+        e = launch_fsi_subiteration(H->F, c->M, A, L, t, c->Dt / c->Dx, stream, &c->ibm_launches);
         if (e != cudaSuccess) return cuda_fail(e, "fsi_subiteration");
-        e = cudaMemcpyAsync(H->h_cont, H->F.cont, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        e = cudaMemcpyAsync(H->h_cont, H->F.cont, sizeof(int), cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) return cuda_fail(e, "fsi_loop");
         if (!*H->h_cont) break;
     }

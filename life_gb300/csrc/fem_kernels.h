@@ -91,4 +91,4 @@ cudaError_t launch_epsilon_markers(const MarkerDev& M, int n, double Dx, double*
 }  // namespace life
 
 int setup_fem(LifeCase* c);
-int fem_fsi_loop(LifeCase* c, int t, const void* A, const life::LatDev& L);
+int fem_fsi_loop(LifeCase* c, int t, const void* A, const life::LatDev& L, cudaStream_t stream);

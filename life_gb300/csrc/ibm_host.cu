@@ -107,24 +107,32 @@ int upload_markers(LifeCase* c) {
     return LIFE_OK;
 }
 
-// One step of ObjectsClass::objectKernel on the device.
-int ibm_step(LifeCase* c, int t, const void* A, void* B) {
+// One step of ObjectsClass::objectKernel on the device, in two parts. The
+// forces (interpolation and forceCalc, or the whole FSI subiteration loop)
+// read only the step's input populations A, so they can run beside the
+// lattice step; the spread writes the support sites of B and follows both.
+int ibm_forces(LifeCase* c, int t, const void* A, cudaStream_t s) {
     LatDev L = lattice_view(c, t);
-    cudaError_t e;
-    if (c->obj.hasFlex) {
-        int rc = fem_fsi_loop(c, t, A, L);
-        if (rc) return rc;
-    } else {
-        e = launch_ibm_interp(A, L, t, c->M, c->Dt / c->Dx, c->stream);
-        if (e != cudaSuccess) return cuda_fail(e, "ibm_interp");
-        c->ibm_launches += 1;
-    }
-    e = launch_ibm_spread(A, B, L, t, c->M, c->W, c->stream);
+    if (c->obj.hasFlex) return fem_fsi_loop(c, t, A, L, s);
+    cudaError_t e = launch_ibm_interp(A, L, t, c->M, c->Dt / c->Dx, s);
+    if (e != cudaSuccess) return cuda_fail(e, "ibm_interp");
+    c->ibm_launches += 1;
+    return LIFE_OK;
+}
+
+int ibm_apply(LifeCase* c, int t, const void* A, void* B, cudaStream_t s) {
+    LatDev L = lattice_view(c, t);
+    cudaError_t e = launch_ibm_spread(A, B, L, t, c->M, c->W, s);
     if (e != cudaSuccess) return cuda_fail(e, "ibm_spread");
     c->ibm_launches += 3;
     std::swap(c->W.sites, c->W.sites_prev);
     std::swap(c->W.nsites, c->W.nsites_prev);
     return LIFE_OK;
+}
+
+int ibm_step(LifeCase* c, int t, const void* A, void* B) {
+    if (int rc = ibm_forces(c, t, A, c->stream)) return rc;
+    return ibm_apply(c, t, A, B, c->stream);
 }
 
 extern "C" int life_case_get_markers(LifeCase* c, double* pos, double* vel, double* force, double* epsilon,

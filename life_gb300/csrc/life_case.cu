@@ -184,6 +184,11 @@ static void free_case(LifeCase* c) {
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->ev_out) cudaEventDestroy(c->ev_out);
     if (c->ev_done) cudaEventDestroy(c->ev_done);
+    if (c->ev_aux) cudaEventDestroy(c->ev_aux);
+    if (c->aux) {
+        cudaStreamSynchronize(c->aux);
+        cudaStreamDestroy(c->aux);
+    }
     if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (prev >= 0) cudaSetDevice(prev);
@@ -236,6 +241,8 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_aux, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
     for (const char* var : {"LIFE_CASE_HOSTLOOP", "LIFE_FSI_HOSTLOOP"})
         if (const char* v = std::getenv(var))
             if (v[0] == '1') c->host_steps = true;

@@ -60,7 +60,8 @@ struct LifeCase {
     unsigned long long* d_red = nullptr;
     cudaStream_t stream = nullptr;   // every kernel of the case is ordered on this stream
     cudaStream_t side = nullptr;     // perimeter kernel, forked from and joined to `stream`
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_out = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_out = nullptr, ev_done = nullptr, ev_aux = nullptr;
+    cudaStream_t aux = nullptr;      // IBM forces (interpolation / FSI loop) beside the lattice step
     // Captured step graphs of this case alone (a one-case batch on the case's
     // own stream), used by life_case_step; and whether steps are launched from
     // the host instead (LIFE_CASE_HOSTLOOP=1 or LIFE_FSI_HOSTLOOP=1).
