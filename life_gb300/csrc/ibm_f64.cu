@@ -23,30 +23,47 @@ namespace life {
 
 constexpr int TILE = 16;
 
+// One warp per marker: lane s reconstructs support site s, and every lane
+// then adds the nsupp terms in support order (the reference's loop), so the
+// sums are formed exactly as in a sequential loop while the nine site states
+// are computed side by side.
 template <bool CM, class S>
-__global__ void k_ibm_interp(const typename S::T* __restrict__ P, LatDev L, int t, MarkerDev M, double velScale,
-                             const int* __restrict__ t_dev) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= M.n) return;
+__global__ void __launch_bounds__(128) k_ibm_interp(const typename S::T* __restrict__ P, LatDev L, int t, MarkerDev M,
+                                                    double velScale, const int* __restrict__ t_dev) {
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (k >= M.n) return;  // uniform per warp
     t = t_dev ? *t_dev : step_t(L, t);  // inside a replayed graph the step comes from the device
-    double iRho = 0.0, iMx = 0.0, iMy = 0.0;
     const int ns = M.nsupp[k];
-    int imin = 1 << 30, imax = -(1 << 30), jmin = 1 << 30, jmax = -(1 << 30);
-    for (int s = 0; s < ns; s++) {
-        const int i = M.si[k * 9 + s], j = M.sj[k * 9 + s];
-        const double d = M.sd[k * 9 + s];
+    double tr = 0.0, tx = 0.0, ty = 0.0;
+    int i = 0, j = 0;
+    if (lane < ns) {
+        i = M.si[k * 9 + lane];
+        j = M.sj[k * 9 + lane];
+        const double d = M.sd[k * 9 + lane];
         double f[9], rho, ux, uy;
         site_state<CM, S>(P, L, t, i, j, f, rho, ux, uy);
-        iRho += rho * d * 1.0 * 1.0;
-        iMx += rho * ux * d * 1.0 * 1.0;
-        iMy += rho * uy * d * 1.0 * 1.0;
-        imin = min(imin, i); imax = max(imax, i);
-        jmin = min(jmin, j); jmax = max(jmax, j);
+        tr = rho * d * 1.0 * 1.0;
+        tx = rho * ux * d * 1.0 * 1.0;
+        ty = rho * uy * d * 1.0 * 1.0;
     }
-    const double sc = velScale * iRho;
-    M.force[k * 2 + 0] = 2.0 * (sc * M.vel[k * 2 + 0] - iMx);
-    M.force[k * 2 + 1] = 2.0 * (sc * M.vel[k * 2 + 1] - iMy);
-    M.bbox[k] = make_int4(imin, imax, jmin, jmax);
+    double iRho = 0.0, iMx = 0.0, iMy = 0.0;
+    for (int q = 0; q < ns; q++) {
+        iRho += __shfl_sync(0xffffffffu, tr, q);
+        iMx += __shfl_sync(0xffffffffu, tx, q);
+        iMy += __shfl_sync(0xffffffffu, ty, q);
+    }
+    const bool act = lane < ns;
+    const int imin = __reduce_min_sync(0xffffffffu, act ? i : (1 << 30));
+    const int imax = __reduce_max_sync(0xffffffffu, act ? i : -(1 << 30));
+    const int jmin = __reduce_min_sync(0xffffffffu, act ? j : (1 << 30));
+    const int jmax = __reduce_max_sync(0xffffffffu, act ? j : -(1 << 30));
+    if (lane == 0) {
+        const double sc = velScale * iRho;
+        M.force[k * 2 + 0] = 2.0 * (sc * M.vel[k * 2 + 0] - iMx);
+        M.force[k * 2 + 1] = 2.0 * (sc * M.vel[k * 2 + 1] - iMy);
+        M.bbox[k] = make_int4(imin, imax, jmin, jmax);
+    }
 }
 
 __global__ void k_ibm_clear(IbmScratch W, LatDev L) {
@@ -82,6 +99,10 @@ __global__ void __launch_bounds__(256) k_ibm_spread(const typename S::T* __restr
     __shared__ double s_d[256][9];
     __shared__ double s_fx[256], s_fy[256];
     __shared__ int s_ns[256];
+    // touched sites of the tile, compacted onto the first warps
+    __shared__ int s_tij[256];
+    __shared__ double s_tax[256], s_tay[256];
+    __shared__ int s_nt;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     t = step_t(L, t);
     const int ntiles = *W.ntiles;
@@ -137,8 +158,30 @@ __global__ void __launch_bounds__(256) k_ibm_spread(const typename S::T* __restr
             }
             __syncthreads();
         }
-        if (tid == 0) W.tile_flag[tile] = 0u;
-        if (touched && i < L.Nx && j < L.Ny) {
+        if (tid == 0) {
+            W.tile_flag[tile] = 0u;
+            s_nt = 0;
+        }
+        __syncthreads();
+        {
+            const bool mine = touched && i < L.Nx && j < L.Ny;
+            const unsigned bal = __ballot_sync(0xffffffffu, mine);
+            int base = 0;
+            if (lane == 0 && bal) base = atomicAdd(&s_nt, __popc(bal));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (mine) {
+                const int r = base + __popc(bal & ((1u << lane) - 1u));
+                s_tij[r] = (j << 16) | i;
+                s_tax[r] = ax;
+                s_tay[r] = ay;
+            }
+        }
+        __syncthreads();
+        // the long FP64 chains (state, velocity correction, collision) on as
+        // few warps as there are touched sites
+        for (int r = tid; r < s_nt; r += blockDim.x) {
+            const int i = s_tij[r] & 0xffff, j = s_tij[r] >> 16;
+            const double ax = s_tax[r], ay = s_tay[r];
             const long long s = (long long)j * L.pitch + i;
             W.force_ibm[s] = ax;
             W.force_ibm[L.S + s] = ay;
@@ -158,6 +201,7 @@ __global__ void __launch_bounds__(256) k_ibm_spread(const typename S::T* __restr
 #pragma unroll
             for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = S::save(fs[v], v);
         }
+        __syncthreads();
     }
 }
 
@@ -188,7 +232,7 @@ struct TypedPtr {
 cudaError_t launch_ibm_interp(const void* P, const LatDev& L, int t, const MarkerDev& M, double velScale,
                               cudaStream_t s, const int* t_dev) {
     if (M.n == 0) return cudaSuccess;
-    const int nb = (M.n + 127) / 128;
+    const int nb = (M.n + 3) / 4;  // one warp per marker
     TypedPtr<void> Pp{P};
     IBM_DISPATCH(k_ibm_interp, nb, 128, Pp, L, t, M, velScale, t_dev);
     return cudaGetLastError();
