@@ -343,6 +343,11 @@ int life_server_drain(LifeServer* s, double timeout_s);
 /* Stops the thread (queued requests are dropped) and frees everything. */
 int life_server_destroy(LifeServer* s);
 
+/* Self-test of the library's division by a known reciprocal (used by the
+ * FEM band solve): compares it with IEEE division on n seeded random operand
+ * pairs on the device and returns the number of results that differ. */
+int life_selftest_division(int64_t n, uint64_t seed, int64_t* mismatches);
+
 /* Parses geometry.config text with the reference's rules (leading '#' lines
  * skipped, whitespace tokens; src/Objects.cpp:338-458). Writes at most cap
  * descriptors, returns the number found in *n. */

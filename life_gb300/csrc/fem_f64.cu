@@ -465,6 +465,51 @@ __device__ void band_factor_smem(double* Bd, int nn, int kl, int ku, int W, int*
     }
 }
 
+// a / b correctly rounded (round to nearest), given y = RN(1/b): Markstein's
+// method (P. Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al.,
+// Handbook of Floating-Point Arithmetic, "Markstein's theorem"): q0 = RN(a y)
+// is within 1.5 ulp of a/b, one correction q1 = RN(q0 + RN(a - b q0) y)
+// brings it within one ulp, and then the residual a - b q1 is exact and
+// RN(q1 + (a - b q1) y) = RN(a/b). The theorem needs the intermediates in the
+// normal range, so operands outside a safe exponent window take the hardware
+// division. life_selftest_division checks this function against a / b.
+__device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
+    const int ea = (int)((unsigned long long)__double_as_longlong(a) >> 52) & 0x7ff;
+    const int eb = (int)((unsigned long long)__double_as_longlong(b) >> 52) & 0x7ff;
+    const bool a_ok = (a == 0.0) || (ea > 200 && ea < 1800);
+    const bool b_ok = eb > 200 && eb < 1800;
+    if (!(a_ok && b_ok && (a == 0.0 || (ea - eb > -700 && ea - eb < 700)))) return a / b;
+    const double q0 = a * y;
+    const double r0 = fma(-b, q0, a);
+    const double q1 = fma(r0, y, q0);
+    const double r1 = fma(-b, q1, a);
+    return fma(r1, y, q1);
+}
+
+__global__ void k_selftest_division(long long n, unsigned long long seed, unsigned long long* bad) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        // splitmix64 streams for the two operands; exponents over a wide range
+        unsigned long long z = seed + 0x9e3779b97f4a7c15ull * (unsigned long long)(2 * q + 1);
+        auto mix = [](unsigned long long x) {
+            x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+            x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+            return x ^ (x >> 31);
+        };
+        const unsigned long long u = mix(z), v = mix(z + 0x9e3779b97f4a7c15ull);
+        const unsigned long long w = mix(z ^ 0x5851f42d4c957f2dull);
+        // exponent spread: mostly near 1, sometimes anywhere in the normal range
+        const int span = (w & 7) == 0 ? 2000 : 80;
+        const long long xa = (long long)(1023 + (long long)((w >> 8) % span) - span / 2);
+        const long long xb = (long long)(1023 + (long long)((w >> 24) % span) - span / 2);
+        const unsigned long long ba = (u & 0x800fffffffffffffull) | ((unsigned long long)(xa < 1 ? 1 : (xa > 2046 ? 2046 : xa)) << 52);
+        const unsigned long long bb = (v & 0x800fffffffffffffull) | ((unsigned long long)(xb < 1 ? 1 : (xb > 2046 ? 2046 : xb)) << 52);
+        const double a = __longlong_as_double((long long)ba), b = __longlong_as_double((long long)bb);
+        const double ref = a / b;
+        const double got = div_rn_recip(a, b, __drcp_rn(b));
+        if (__double_as_longlong(ref) != __double_as_longlong(got) && !(ref != ref && got != got)) atomicAdd(bad, 1ull);
+    }
+}
+
 __device__ __forceinline__ void named_bar(int id, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
@@ -490,7 +535,7 @@ __device__ __forceinline__ void named_bar(int id, int nthreads) {
 // and barrier 2 after every step but the last; warp 2 calls barrier 1 nn
 // times. The k-th calls pair up, so every barrier completes. Needs at least
 // 128 threads; with fewer, warp 0 does everything.
-__device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* piv, double* y) {
+__device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* piv, double* y, double* rcp) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (blockDim.x < 128) {
         if (warp == 0) {
@@ -541,6 +586,7 @@ __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* 
             const double oj1 = __shfl_sync(0xffffffffu, rj, 1);  // old M(j, j+1)
             const double op1 = __shfl_sync(0xffffffffu, rp, 1);  // old M(jp, j+1)
             const double r = __shfl_sync(0xffffffffu, rc, src);
+            if (lane == 0) rcp[j] = r;  // RN(1 / U(j,j)) for the forward solve
             __syncwarp();
             // post-swap values
             const double a = (swapped && j + lane == jp) ? v0 : v;
@@ -607,7 +653,7 @@ __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* 
             named_bar(1, 128);
             const int owner = k & 31;
             const double tk = __shfl_sync(0xffffffffu, t, owner);
-            const double yk = tk / bd(Bd, W, kl, k, k);
+            const double yk = div_rn_recip(tk, bd(Bd, W, kl, k, k), rcp[k]);
             if (lane == owner) {
                 y[k] = yk;
                 t = k + 32 < nn ? y[k + 32] : 0.0;
@@ -838,7 +884,7 @@ __device__ bool epsilon_fast(const FsiDev& F, const MarkerDev& M, int m0, int di
     }
     __syncthreads();
     const int kl = s_kl, ku = s_ku, W = 2 * kl + ku + 1;
-    if (kl < 32 && kl + ku < 32 && (long long)dim * W + 2 * dim <= band_doubles) {
+    if (kl < 32 && kl + ku < 32 && (long long)dim * W + 3 * dim + 1 <= band_doubles) {
         double* Bd = band;
         double* y = Bd + (size_t)dim * W;
         int* sp = reinterpret_cast<int*>(y + dim);
@@ -851,7 +897,7 @@ __device__ bool epsilon_fast(const FsiDev& F, const MarkerDev& M, int m0, int di
             if (pp >= 0) bd(Bd, W, kl, pp % dim, pp / dim) = cval[c];
         }
         __syncthreads();
-        if (threadIdx.x < 128) band_lu_forward(Bd, dim, kl, ku, W, sp, y);
+        if (threadIdx.x < 128) band_lu_forward(Bd, dim, kl, ku, W, sp, y, reinterpret_cast<double*>(fp + dim));
         __syncthreads();
         if (threadIdx.x < 32) band_solve_back(Bd, dim, kl, W, sp, fp, y);
         __syncthreads();
@@ -897,7 +943,7 @@ __device__ void epsilon_range(const FsiDev& F, const MarkerDev& M, int m0, int d
     }
     __syncthreads();
     const int kl = s_kl, ku = s_ku, W = 2 * kl + ku + 1;
-    const long long need = (long long)dim * W + dim + dim;  // band, y, two int arrays
+    const long long need = (long long)dim * W + 3 * dim + 1;  // band, y, two int arrays, reciprocals
     if (smem && kl < 32 && need <= smem_doubles) {
         double* Bd = smem;
         double* y = Bd + (size_t)dim * W;
@@ -914,7 +960,7 @@ __device__ void epsilon_range(const FsiDev& F, const MarkerDev& M, int m0, int d
         }
         __syncthreads();
         if (kl + ku < 32) {
-            if (threadIdx.x < 128) band_lu_forward(Bd, dim, kl, ku, W, sp, y);
+            if (threadIdx.x < 128) band_lu_forward(Bd, dim, kl, ku, W, sp, y, reinterpret_cast<double*>(fp + dim));
             __syncthreads();
             if (threadIdx.x < 32) band_solve_back(Bd, dim, kl, W, sp, fp, y);
         } else if (threadIdx.x < 32) {
@@ -972,6 +1018,7 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
     double* sY = sV + n;               // [nn] right-hand side / solution
     int* sPiv = reinterpret_cast<int*>(sY + nn);
     int* sFp = sPiv + nn;
+    double* sRcp = reinterpret_cast<double*>(sFp + nn);  // [nn] pivot reciprocals
     {
         double* U = vec(B, V_U);
         double* Ud = vec(B, V_Udot);
@@ -1122,7 +1169,7 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
         }
         __syncthreads();
         // delU = solveLAPACK(K, F, bcDOFs) (src/Utils.cpp:288-311)
-        if (threadIdx.x < 128) band_lu_forward(sBd, nn, 5, 5, KW, sPiv, sY);
+        if (threadIdx.x < 128) band_lu_forward(sBd, nn, 5, 5, KW, sPiv, sY, sRcp);
         __syncthreads();
         if (threadIdx.x < 32) band_solve_back(sBd, nn, 5, KW, sPiv, sFp, sY);
         __syncthreads();
@@ -1282,7 +1329,7 @@ __global__ void k_fsi_begin(FsiDev F, int t, const int* t_dev, int t_off) {
 
 size_t fem_dynamic_smem(int n, int bc) {
     const int nn = n - bc;
-    return sizeof(double) * ((size_t)nn * 16 + (size_t)n * 22 + n + nn) + sizeof(int) * 2 * (size_t)nn;
+    return sizeof(double) * ((size_t)nn * 17 + (size_t)n * 22 + n + nn) + sizeof(int) * 2 * (size_t)nn;
 }
 
 // The opt-in shared-memory size is an attribute of the kernel, shared by every
@@ -1325,3 +1372,20 @@ cudaError_t launch_fsi_subiteration(const FsiDev& F, const MarkerDev& M, const v
 }
 
 }  // namespace life
+
+extern "C" int life_selftest_division(int64_t n, uint64_t seed, int64_t* mismatches) {
+    if (n <= 0 || !mismatches) return life::set_error(LIFE_ERR_INVALID, "bad arguments");
+    unsigned long long* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        life::k_selftest_division<<<152 * 8, 256>>>((long long)n, (unsigned long long)seed, d);
+        e = cudaGetLastError();
+    }
+    unsigned long long h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) return life::cuda_fail(e, "life_selftest_division");
+    *mismatches = (int64_t)h;
+    return LIFE_OK;
+}

@@ -48,6 +48,7 @@ SIGNATURES = {
     "life_case_set_fem": (C.c_int, [C.c_void_p, C.c_int32] + [_dp] * 12),
     "life_case_set_relax": (C.c_int, [C.c_void_p, C.c_double]),
     "life_case_get_fem0": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp]),
+    "life_selftest_division": (C.c_int, [C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
     "life_case_max_velocity": (C.c_int, [C.c_void_p, _dp, _ip]),
     "life_case_total_force": (C.c_int, [C.c_void_p, _dp, _dp]),
     "life_parse_geometry": (C.c_int, [C.c_char_p, C.c_void_p, C.c_int32, _ip]),
