@@ -291,6 +291,11 @@ def run_workload(args, world, rank):
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
+    if args.workload == "accuracy":
+        out = {"workload": "accuracy", **accuracy_leg(args.steps, max(args.steps // 25, 50))}
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        return 0
     make = cylinder_params if args.workload == "cylinder" else filament_params
     out = {"workload": args.workload}
     for prec, tag in ((PREC_F64, "fp64"), (PREC_F32, "fp32")):
@@ -311,16 +316,108 @@ def run_workload(args, world, rank):
     return 0
 
 
-def ensemble_leg(steps: int, warmup: int, n_cases: int = 64, tile=None, sequential: bool = True) -> dict:
+def _upward_crossings(t, y):
+    """Times at which y - mean(y) crosses zero upwards (linear interpolation)."""
+    import numpy as np
+    y = np.asarray(y) - float(np.mean(y))
+    k = np.flatnonzero((y[:-1] < 0.0) & (y[1:] >= 0.0))
+    return [t[i] + (t[i + 1] - t[i]) * (-y[i]) / (y[i + 1] - y[i]) for i in k]
+
+
+def cylinder_forces(precision: int, steps: int, every: int = 25) -> dict:
+    """Drag and lift coefficients of the 1000 x 400 cylinder over `steps`
+    steps: C = F / (0.5 rho U^2 D) with F the total force on the body as
+    ObjectsClass::writeTotalForces forms it (src/Objects.cpp:518-528),
+    sampled every `every` steps. Statistics over the second half: mean Cd,
+    lift amplitude (half the peak-to-peak), shedding period from the upward
+    zero crossings of Cl."""
+    import numpy as np
+    from life_gb300.lib import Case
+    p, b = cylinder_params(precision)
+    nd = 0.5 * 1.0 * 0.04 ** 2 * 40.0
+    ts, cd, cl = [], [], []
+    with Case(p, b) as c:
+        while c.t < steps:
+            c.step(min(every, steps - c.t))
+            fx, fy = c.total_force()
+            ts.append(c.t)
+            cd.append(fx / nd)
+            cl.append(fy / nd)
+    ts, cd, cl = np.array(ts, dtype=float), np.array(cd), np.array(cl)
+    h = len(ts) // 2
+    up = _upward_crossings(ts[h:], cl[h:])
+    period = float(np.mean(np.diff(up))) if len(up) >= 2 else None
+    return {"t": ts, "cd": cd, "cl": cl, "cd_mean": float(cd[h:].mean()),
+            "cl_amp": float(0.5 * (cl[h:].max() - cl[h:].min())), "period_steps": period}
+
+
+def filament_tip(precision: int, steps: int, every: int = 50) -> dict:
+    """Transverse tip displacement (y of the last FEM node minus its
+    undeformed y, over L) of the 1200 x 400 filament, sampled every `every`
+    steps."""
+    import numpy as np
+    from life_gb300.lib import Case
+    p, b = filament_params(precision)
+    L = b[0].length
+    ys = []
+    with Case(p, b) as c:
+        while c.t < steps:
+            c.step(min(every, steps - c.t))
+            fm = c.fem(0)
+            ys.append((fm["pos"][-1, 1] - fm["pos0"][-1, 1]) / L)
+    return {"tip": np.array(ys)}
+
+
+def accuracy_leg(cyl_steps: int = 50000, fil_steps: int = 2000) -> dict:
+    """FP32 shifted populations against the FP64 form (bit-identical to the
+    reference) on the two immersed-body workloads: cylinder drag, lift and
+    shedding period after cyl_steps steps; filament tip displacement over
+    fil_steps steps (FEM, epsilon and Aitken in FP64 in both)."""
+    import numpy as np
+    out = {"cylinder_steps": cyl_steps}
+    t0 = time.perf_counter()
+    r = {tag: cylinder_forces(prec, cyl_steps) for prec, tag in ((0, "fp64"), (1, "fp32"))}
+    for tag in ("fp64", "fp32"):
+        out[f"cylinder_{tag}_cd"] = round(r[tag]["cd_mean"], 6)
+        out[f"cylinder_{tag}_cl_amp"] = round(r[tag]["cl_amp"], 6)
+        per = r[tag]["period_steps"]
+        out[f"cylinder_{tag}_shedding_period_steps"] = None if per is None else round(per, 1)
+        out[f"cylinder_{tag}_strouhal"] = None if per is None else round(40.0 / (0.04 * per), 5)
+    a, b = r["fp64"], r["fp32"]
+    out["cylinder_cd_rel_err"] = abs(b["cd_mean"] - a["cd_mean"]) / abs(a["cd_mean"])
+    out["cylinder_cl_amp_rel_err"] = (abs(b["cl_amp"] - a["cl_amp"]) / a["cl_amp"]) if a["cl_amp"] > 0 else None
+    if a["period_steps"] and b["period_steps"]:
+        out["cylinder_period_rel_err"] = abs(b["period_steps"] - a["period_steps"]) / a["period_steps"]
+    # pointwise, relative to the lift amplitude (drag: to its mean)
+    out["cylinder_cd_series_max_rel_err"] = float(np.abs(b["cd"] - a["cd"]).max() / abs(a["cd_mean"]))
+    if a["cl_amp"] > 0:
+        out["cylinder_cl_series_max_err_over_amp"] = float(np.abs(b["cl"] - a["cl"]).max() / a["cl_amp"])
+    out["filament_steps"] = fil_steps
+    f64, f32 = filament_tip(0, fil_steps)["tip"], filament_tip(1, fil_steps)["tip"]
+    out["filament_fp64_tip_over_L_final"] = round(float(f64[-1]), 6)
+    out["filament_fp64_tip_over_L_range"] = [round(float(f64.min()), 6), round(float(f64.max()), 6)]
+    out["filament_tip_max_err_over_L"] = float(np.abs(f32 - f64).max())
+    span = float(f64.max() - f64.min())
+    out["filament_tip_max_err_over_swing"] = float(np.abs(f32 - f64).max() / span) if span > 0 else None
+    out["seconds"] = round(time.perf_counter() - t0, 1)
+    return out
+
+
+def ensemble_leg(steps: int, warmup: int, n_cases: int = 64, tile=None, sequential: bool = True,
+                 fp16_steps: int = None, seq_steps: int = None) -> dict:
     """The 64-case batched ensemble (uneven lattices, cylinders or filament
-    rows, BGK/CM, Re 50-300): batched FP32 and FP16 (one persistent interior
-    launch and one replayed graph per batch step, autotuned tiles) against the
-    same cases stepped one after another through life_case_step in FP64 and
-    FP32. MLUPS = sum of lattice sites x steps / device time."""
+    rows, BGK/CM, Re 50-300): batched FP32 over `steps` steps and FP16 over
+    `fp16_steps` (one persistent interior launch and one replayed graph per
+    batch step, autotuned tiles) against the same cases stepped one after
+    another through life_case_step in FP64 and FP32 over `seq_steps` steps
+    each (a bounded sample). MLUPS = sum of lattice sites x steps / device
+    time."""
     from life_gb300.ensemble import ensemble_cases, sites
     from life_gb300.lib import Batch, Case
     out = {}
+    nsteps = {1: steps, 2: steps if fp16_steps is None else fp16_steps}
     for prec, tag in ((1, "fp32"), (2, "fp16")):
+        steps = nsteps[prec]
         cs = ensemble_cases(n=n_cases, precision=prec)
         with Batch(cs) as B:
             B.step(warmup)
@@ -332,6 +429,7 @@ def ensemble_leg(steps: int, warmup: int, n_cases: int = 64, tile=None, sequenti
             B.step(warmup)
             tot, kn = B.bench_steps(steps)
             inf = B.info()
+            out[f"batched_{tag}_steps"] = steps
             out[f"batched_{tag}_mlups"] = round(inf.sites * steps / (tot * 1e-3) / 1e6, 1)
             out[f"batched_{tag}_ms_per_step"] = round(tot / steps, 4)
             out[f"batched_{tag}_interior_ms"] = round(B.interior_ms(10), 4)
@@ -344,17 +442,34 @@ def ensemble_leg(steps: int, warmup: int, n_cases: int = 64, tile=None, sequenti
     out["bodies"] = sum(len(b) for _, b in cs)
     if not sequential:
         return out
-    for prec, tag in ((0, "fp64"), (1, "fp32")):
-        cs = ensemble_cases(n=n_cases, precision=prec)
-        n_ss, ms_tot = 0, 0.0
-        k = max(10, steps // 5)
-        for p, b in cs:
-            with Case(p, b) as c:
+    # sequential per-case runs; the FP32 and FP16 states are compared with the
+    # FP64 state after the same steps (a case in a batch is bit-identical to
+    # the case alone, so this is the batched forms' error too)
+    import numpy as np
+    import dataclasses
+    k = seq_steps if seq_steps else max(10, nsteps[1] // 5)
+    n_ss, ms = 0, {0: 0.0, 1: 0.0}
+    err = {1: 0.0, 2: 0.0}
+    for p, b in ensemble_cases(n=n_cases, precision=0):
+        u = {}
+        for prec in (0, 1, 2):
+            with Case(dataclasses.replace(p, precision=prec), b) as c:
                 c.step(warmup)
-                tt, _, _ = c.bench_steps(k)
-            ms_tot += tt
-            n_ss += p.Nx * p.Ny * k
-        out[f"sequential_{tag}_mlups"] = round(n_ss / (ms_tot * 1e-3) / 1e6, 1)
+                if prec in ms:
+                    tt, _, _ = c.bench_steps(k)
+                    ms[prec] += tt
+                else:
+                    c.step(k)
+                u[prec] = c.fields(("u",))["u"]
+        n_ss += p.Nx * p.Ny * k
+        umax = float(np.abs(u[0]).max())
+        for prec in (1, 2):
+            err[prec] = max(err[prec], float(np.abs(u[prec] - u[0]).max()) / umax)
+    for prec, tag in ((0, "fp64"), (1, "fp32")):
+        out[f"sequential_{tag}_mlups"] = round(n_ss / (ms[prec] * 1e-3) / 1e6, 1)
+    out["fp32_velocity_rel_err_max_over_cases"] = err[1]
+    out["fp16_velocity_rel_err_max_over_cases"] = err[2]
+    out["error_after_steps"] = warmup + k
     out["batched_fp32_over_sequential_fp64"] = round(out["batched_fp32_mlups"] / out["sequential_fp64_mlups"], 2)
     out["batched_fp32_over_sequential_fp32"] = round(out["batched_fp32_mlups"] / out["sequential_fp32_mlups"], 2)
     return out
@@ -517,8 +632,13 @@ def run_gb300(args, world, rank, local):
             extras[f"filament_1200x400_bgk_{tag}_ms_per_step"] = round(tt / 50, 3)
             extras["filament_subiterations_last_step"] = st.last_subits
             del cf
+        # ---- FP32 vs FP64 on the immersed-body workloads: drag, lift,
+        # shedding period, filament tip displacement
+        extras["accuracy"] = accuracy_leg()
         # ---- 64-case batched ensemble
-        extras["ensemble"] = ensemble_leg(100, args.warmup)
+        # (FP32 over the configured 10,000 steps; FP16 storage over 100, since
+        # it does not carry long FSI runs)
+        extras["ensemble"] = ensemble_leg(10000, args.warmup, fp16_steps=100, seq_steps=20)
         # ---- serving: Poisson stream of canopy requests
         extras["serving"] = serving_leg()
 
@@ -576,6 +696,11 @@ def run_gb300(args, world, rank, local):
             line["fp32_vs_fp64"] = {"fp32_over_fp64_mlups": extras["fp32_over_fp64"],
                                     "fp32_velocity_rel_err": extras["fp32_velocity_rel_err"],
                                     "fp16_velocity_rel_err": extras["fp16_velocity_rel_err"]}
+            ac = extras.get("accuracy", {})
+            for key in ("cylinder_cd_rel_err", "cylinder_cl_amp_rel_err", "cylinder_period_rel_err",
+                        "filament_tip_max_err_over_L"):
+                if key in ac:
+                    line["fp32_vs_fp64"][key] = ac[key]
         if "serving" in extras:
             sv = extras["serving"]
             line["latency"] = {"p50_s": sv["latency_s_p50"], "p95_s": sv["latency_s_p95"],
@@ -599,9 +724,11 @@ def main():
     ap.add_argument("--tile", default="", help="ensemble: fixed tile WxH instead of the autotuner")
     ap.add_argument("--batch-only", action="store_true", help="ensemble: skip the sequential per-case runs")
     ap.add_argument("--step-scale", type=float, default=0.02, help="serve: fraction of each request's steps")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "cylinder", "filament", "ensemble", "serve"],
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "cylinder", "filament", "ensemble", "serve", "accuracy"],
                     help="cavity: the headline line; cylinder/filament: timing of one IBM case; "
-                         "ensemble: the 64-case batch against sequential per-case runs")
+                         "ensemble: the 64-case batch against sequential per-case runs; "
+                         "serve: the Poisson request stream; accuracy: FP32 vs FP64 cylinder "
+                         "Cd/Cl/shedding period over --steps steps and filament tip displacement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -60,3 +60,26 @@ def test_fp32_interior_matches_fp64_one_step_from_same_state():
         q.step(1)
         ua, uq = a.fields(("u",))["u"], q.fields(("u",))["u"]
     assert np.abs(ua - uq).max() / np.abs(ua).max() < 2e-6
+
+
+def test_fp32_body_forces_and_tip_vs_fp64():
+    """The immersed-body observables the FP32 form is stated for: drag and
+    lift of the 1000 x 400 rigid cylinder (central moments, D = 40, Re = 100)
+    over 4000 steps, and the tip displacement of the 1200 x 400 clamped
+    filament (80 corotational elements, FEM/epsilon/Aitken in FP64) over 600
+    steps, both against the FP64 form (bit-identical to the reference).
+    Tolerances: Cd within 1e-3 relative at every sample, Cl within 1e-3 of
+    the mean drag, tip within 1e-6 L (measured over 50,000 and 2,000 steps:
+    7.9e-4, 3.5e-3 of the lift amplitude, 8.2e-8 L)."""
+    import bench
+    r = {prec: bench.cylinder_forces(prec, 4000, every=100) for prec in (0, PREC_F32)}
+    a, q = r[0], r[PREC_F32]
+    assert len(a["cd"]) == 40
+    cd_scale = float(np.abs(a["cd"]).mean())
+    assert cd_scale > 0.5
+    assert np.abs(q["cd"] - a["cd"]).max() <= 1e-3 * cd_scale
+    assert np.abs(q["cl"] - a["cl"]).max() <= 1e-3 * cd_scale
+    t64 = bench.filament_tip(0, 600, every=100)["tip"]
+    t32 = bench.filament_tip(PREC_F32, 600, every=100)["tip"]
+    assert abs(t64[0]) > 1e-3  # the seeded deflection is visible
+    assert np.abs(t32 - t64).max() <= 1e-6
