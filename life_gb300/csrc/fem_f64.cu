@@ -514,15 +514,35 @@ __device__ __forceinline__ void named_bar(int id, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
+// First maximal |v| over the lanes with `valid` (LAPACK idamax: a NaN in
+// lane 0 wins, later NaNs never do), as the lane index. Magnitudes are
+// compared as bit patterns, which order like the values for non-negative
+// doubles. Whole warp.
+__device__ __forceinline__ int pick_pivot(double v, bool valid, int lane) {
+    unsigned long long key = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    if (key > 0x7ff0000000000000ull) key = lane == 0 ? ~0ull : 0ull;
+    const unsigned kh = (unsigned)(key >> 32), klo = (unsigned)key;
+    const unsigned mh = __reduce_max_sync(0xffffffffu, valid ? kh : 0u);
+    const bool c1 = valid && kh == mh;
+    const unsigned ml = __reduce_max_sync(0xffffffffu, c1 ? klo : 0u);
+    return __ffs(__ballot_sync(0xffffffffu, c1 && klo == ml)) - 1;
+}
+
 // Band LU of M and the forward half of the transposed solve (U^T y = b, y in
 // place), pipelined over warps 0-3 of the CTA; kl <= 31 and kl + ku <= 31.
 // The operations are those of band_factor_smem followed by the row-ordered
-// forward substitution; only who does them, and when, differs:
-//   warp 0: column j's pivot, the row swap, the scaling and the step-j update
-//           of column j+1, then barrier 1. Column j+1's candidates are then
-//           already in its registers (the rows it just updated, plus one row
-//           no earlier step touched), so the reciprocal of the next pivot
-//           candidates starts before the barrier;
+// forward substitution; only who does them, and when, differs. The critical
+// path is warp 0's chain per column: reciprocal of the pivot, multipliers,
+// update of the next column's candidates. Everything else runs beside it:
+//   warp 0: step j's row swap, the scaling and the step-j update of column
+//           j+1, barrier 1, then the reciprocals of column j+1's candidates
+//           (each lane its own; the pivot's is kept, the same correctly
+//           rounded 1/pivot as a division after the choice). Column j+1's
+//           candidates are already in its registers (the rows it just
+//           updated, plus one row no earlier step touched);
+//   warp 3: after barrier 1, the choice of column j+1's pivot from the same
+//           candidates, which are final in shared memory by then, handed to
+//           warp 0 in s_src through barrier 2;
 //   warps 1, 3: after barrier 1, the step-j update of columns j+2..kmax,
 //           split between them, then barrier 2 (which warp 0 waits on before
 //           the swap of step j+1, the first thing to touch those rows again);
@@ -536,6 +556,7 @@ __device__ __forceinline__ void named_bar(int id, int nthreads) {
 // times. The k-th calls pair up, so every barrier completes. Needs at least
 // 128 threads; with fewer, warp 0 does everything.
 __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* piv, double* y, double* rcp) {
+    __shared__ int s_src;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (blockDim.x < 128) {
         if (warp == 0) {
@@ -552,19 +573,17 @@ __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* 
     }
     if (warp == 0) {
         // lane l holds the pivot candidate M(j+l, j) and its reciprocal
-        double v = lane <= (kl < nn - 1 ? kl : nn - 1) ? bd(Bd, W, kl, lane, 0) : 0.0;
+        const int imax0 = kl < nn - 1 ? kl : nn - 1;
+        double v = lane <= imax0 ? bd(Bd, W, kl, lane, 0) : 0.0;
         double rc = __drcp_rn(v);
+        int src = pick_pivot(v, lane <= imax0, lane);
         for (int j = 0; j < nn; j++) {
             const int imax = j + kl < nn - 1 ? j + kl : nn - 1;
             const int kmax = j + kl + ku < nn - 1 ? j + kl + ku : nn - 1;
-            const bool valid = j + lane <= imax;
-            unsigned long long key = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
-            if (key > 0x7ff0000000000000ull) key = lane == 0 ? ~0ull : 0ull;
-            const unsigned kh = (unsigned)(key >> 32), klo = (unsigned)key;
-            const unsigned mh = __reduce_max_sync(0xffffffffu, valid ? kh : 0u);
-            const bool c1 = valid && kh == mh;
-            const unsigned ml = __reduce_max_sync(0xffffffffu, c1 ? klo : 0u);
-            const int src = __ffs(__ballot_sync(0xffffffffu, c1 && klo == ml)) - 1;
+            if (j > 0) {
+                named_bar(2, 96);
+                src = s_src;
+            }
             const int jp = j + src;
             const double pv = __shfl_sync(0xffffffffu, v, src);
             const double v0 = __shfl_sync(0xffffffffu, v, 0);
@@ -572,7 +591,6 @@ __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* 
             // pivot != 0 (NaN counts as non-zero), tested on the bits
             const bool nz = ((unsigned long long)__double_as_longlong(pv) << 1) != 0ull;
             const bool swapped = nz && jp != j;
-            if (j > 0) named_bar(2, 96);
             const int c = j + lane;
             double rj = 0.0, rp = 0.0;
             if (c <= kmax) {
@@ -587,7 +605,6 @@ __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* 
             const double op1 = __shfl_sync(0xffffffffu, rp, 1);  // old M(jp, j+1)
             const double r = __shfl_sync(0xffffffffu, rc, src);
             if (lane == 0) rcp[j] = r;  // RN(1 / U(j,j)) for the forward solve
-            __syncwarp();
             // post-swap values
             const double a = (swapped && j + lane == jp) ? v0 : v;
             const double u1 = swapped ? op1 : oj1;
@@ -596,6 +613,15 @@ __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* 
             double nx = 0.0;
             // x + L * (-u1), written as the identical x - L * u1
             if (mrow && early) nx = x - L * u1;
+            if (swapped && c <= kmax) {
+                bd(Bd, W, kl, j, c) = rp;
+                if (c >= j + 2) bd(Bd, W, kl, jp, c) = rj;
+            }
+            if (mrow) {
+                bd(Bd, W, kl, j + lane, j) = L;
+                if (early) bd(Bd, W, kl, j + lane, j + 1) = nx;
+            }
+            named_bar(1, 128);
             // column j+1's candidates: rows j+1..imax were just updated (lane
             // l+1 holds row j+1+l); row j+1+kl, if it exists, is untouched
             if (j + 1 < nn) {
@@ -607,15 +633,6 @@ __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* 
                 v = nv;
                 rc = __drcp_rn(v);
             }
-            if (swapped && c <= kmax) {
-                bd(Bd, W, kl, j, c) = rp;
-                if (c >= j + 2) bd(Bd, W, kl, jp, c) = rj;
-            }
-            if (mrow) {
-                bd(Bd, W, kl, j + lane, j) = L;
-                if (early) bd(Bd, W, kl, j + lane, j + 1) = nx;
-            }
-            named_bar(1, 128);
         }
     } else if (warp == 1 || warp == 3) {
         // entry q of the kl x (kl+ku-1) block of a full step, kept in registers
@@ -627,6 +644,15 @@ __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* 
             const int imax = j + kl < nn - 1 ? j + kl : nn - 1;
             const int kmax = j + kl + ku < nn - 1 ? j + kl + ku : nn - 1;
             const int rows = imax - j, cols = kmax - j - 1;
+            if (warp == 3 && j + 1 < nn) {
+                // column j+1's pivot: rows j+1..imax hold warp 0's updated
+                // values, row j+1+kl its untouched one
+                const int imax1 = j + 1 + kl < nn - 1 ? j + 1 + kl : nn - 1;
+                const int row = j + 1 + lane;
+                const double cv = row <= imax1 ? bd(Bd, W, kl, row, j + 1) : 0.0;
+                const int sp = pick_pivot(cv, row <= imax1, lane);
+                if (lane == 0) s_src = sp;
+            }
             if (rows == kl && cols == fc && rows * cols <= 128) {
                 // bd(i,k) + bd(i,j) * (-bd(j,k)), written as the identical
                 // bd(i,k) - bd(i,j) * bd(j,k)
