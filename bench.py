@@ -573,8 +573,14 @@ def run_gb300(args, world, rank, local):
     sites = n * n
     hbm, hbm_kind = peaks()
 
-    # ---- headline: FP32 shifted populations
-    c32 = Case(cavity_params(n, PREC_F32))
+    # ---- headline: FP32 shifted populations (--storage selects another form
+    # for a headline-only run, e.g. to profile that form's kernel)
+    form = {"fp32": (PREC_F32, 4, "f32", "fp32 shifted populations (f - w)"),
+            "fp16": (PREC_F16, 2, "f16", "fp16 scaled shifted populations ((f - w) / s_v)"),
+            "fp64": (PREC_F64, 8, "f64", "fp64 populations (reference arithmetic)")}[args.storage]
+    if args.storage != "fp32" and not args.quick:
+        raise SystemExit("--storage other than fp32 needs --quick (the extras compare the forms themselves)")
+    c32 = Case(cavity_params(n, form[0]))
     c32.step(args.warmup)
     c32.sync()
     barrier(world)
@@ -585,7 +591,7 @@ def run_gb300(args, world, rank, local):
     clocks = clk.summary()
     ms_step = tot_ms / args.steps
     value = world * sites * args.steps / (tot_ms * 1e-3) / 1e6
-    bytes_per_site = 18 * 4
+    bytes_per_site = 18 * form[1]
     achieved = bytes_per_site * sites / (inner_ms * 1e-3) / 1e9
 
     extras = {}
@@ -645,7 +651,7 @@ def run_gb300(args, world, rank, local):
     # ---- end to end through the C-ABI: create from params (host), K steps,
     # read the velocity field back to host memory
     t0 = time.perf_counter()
-    ce = Case(cavity_params(n, PREC_F32))
+    ce = Case(cavity_params(n, form[0]))
     ce.step(args.steps)
     u = ce.fields(("u",))["u"]
     e2e_s = time.perf_counter() - t0
@@ -656,7 +662,7 @@ def run_gb300(args, world, rank, local):
 
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "roofline_traffic.json")
-    if os.path.exists(tpath):
+    if os.path.exists(tpath) and args.storage == "fp32":
         with open(tpath) as fh:
             tr = json.load(fh)
         traffic = round(float(tr["dram_bytes_per_site"]) * sites)
@@ -674,15 +680,16 @@ def run_gb300(args, world, rank, local):
         line = {
             "metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32",
+            "vs_baseline": None, "dtype": form[2],
             "data": "synthetic (analytic initial state of the cavity)",
             "config": {"workload": f"lid_driven_cavity_{n}x{n}_d2q9_bgk", "lattice": [n, n], "collision": "BGK",
-                       "storage": "fp32 shifted populations (f - w)", "lid_velocity": 0.1, "tau": 0.5768,
-                       "parallelism": f"replicas{world}", "l2": "state 1.2 GB > L2 (no flush needed)"},
+                       "storage": form[3], "lid_velocity": 0.1, "tau": 0.5768,
+                       "parallelism": f"replicas{world}", "l2": f"state {2 * 9 * form[1] * sites / 1e9:.2f} GB > L2 (no flush needed)"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                          "frac": round(achieved / hbm, 4), "traffic": traffic,
                          "peak_source": f"{hbm_kind} hbm_gbs",
-                         "kernel": "k_step_lowp<BGK,F32> (boundary perimeter + interior, one launch per step)",
+                         "kernel": ("k_interior_f64<BGK> + k_perimeter" if args.storage == "fp64" else
+                                    f"k_step_lowp<BGK,{form[2].upper()}> (boundary perimeter + interior, one launch per step)"),
                          "algorithmic_bytes_per_site": bytes_per_site, "kernel_ms": round(inner_ms, 4)},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e, 1), "unit": "MLUPS", "h2d_bytes_per_step": round(h2d / args.steps),
@@ -719,6 +726,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nx", type=int, default=4096)
     ap.add_argument("--quick", action="store_true", help="headline measurement only")
+    ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16", "fp64"],
+                    help="population storage of the headline case (other than fp32 only with --quick)")
     ap.add_argument("--requests", type=int, default=24, help="serve: requests in the stream")
     ap.add_argument("--cases", type=int, default=64, help="ensemble: cases in the batch")
     ap.add_argument("--tile", default="", help="ensemble: fixed tile WxH instead of the autotuner")

@@ -56,22 +56,29 @@ __device__ __forceinline__ float cdot(int v, float a, float b) {
     return cx == 0 ? yb : xa + yb;
 }
 
-template <bool CM>
+// FORCED = false: the force of this step is zero everywhere (no gravity, no
+// Womersley term), so every forcing term is an exact zero and is not formed.
+template <bool CM, bool FORCED>
 __device__ __forceinline__ void collide_dev32(const float g[9], float dr, float rho, float mx, float my, float ux,
                                               float uy, float Gx, float Gy, float omega, float gs[9]) {
     if (!CM) {
         const float usq15 = 1.5f * fmaf(ux, ux, uy * uy);
-        const float uF = fmaf(ux, Gx, uy * Gy);
+        const float uF = FORCED ? fmaf(ux, Gx, uy * Gy) : 0.0f;
         const float fo = fmaf(-0.5f, omega, 1.0f);
 #pragma unroll
         for (int v = 0; v < 9; v++) {
             const float w = wgt_f(v);
             const float cu = cdot(v, ux, uy);
-            const float cF = cdot(v, Gx, Gy);
             const float inner = fmaf(4.5f * cu, cu, fmaf(3.0f, cu, -usq15));
             const float geq = w * fmaf(rho, inner, dr);
-            const float Fv = (3.0f * w) * fmaf(3.0f * cu, cF, cF - uF);
-            gs[v] = fmaf(fo, Fv, fmaf(omega, geq - g[v], g[v]));
+            const float a = fmaf(omega, geq - g[v], g[v]);
+            if (FORCED) {
+                const float cF = cdot(v, Gx, Gy);
+                const float Fv = (3.0f * w) * fmaf(3.0f * cu, cF, cF - uF);
+                gs[v] = fmaf(fo, Fv, a);
+            } else {
+                gs[v] = a;
+            }
         }
     } else {
         // raw second moments of the deviations
@@ -81,6 +88,7 @@ __device__ __forceinline__ void collide_dev32(const float g[9], float dr, float 
         const float k4 = om1 * fmaf(ux * ux - uy * uy, rho, fmaf(2.0f * uy, my, fmaf(-2.0f * ux, mx, dxxyy)));
         const float k5 = om1 * fmaf(ux * uy, rho, fmaf(-ux, my, fmaf(-uy, mx, gxy)));
         const float k1 = 0.5f * Gx, k2 = 0.5f * Gy, k7 = Gx * (1.0f / 6.0f), k6 = Gy * (1.0f / 6.0f);
+        (void)k1; (void)k2; (void)k6; (void)k7;
         float ex[3], wx[3], dx[3], ey[3], wy[3], dy[3];
         e1d(ux, ex, wx, dx);
         e1d(uy, ey, wy, dy);
@@ -120,21 +128,26 @@ __device__ __forceinline__ void collide_dev32(const float g[9], float dr, float 
             const float E = ex[a] * ey[b];
             const float D = fmaf(dx[a], dy[b], fmaf(wx[a], dy[b], dx[a] * wy[b]));
             float acc = fmaf(dr, E, D);
-            acc = fmaf(T1[v], k1, acc);
-            acc = fmaf(T2[v], k2, acc);
+            if (FORCED) {
+                acc = fmaf(T1[v], k1, acc);
+                acc = fmaf(T2[v], k2, acc);
+            }
             acc = fmaf(T4[v], k4, acc);
             acc = fmaf(T5[v], k5, acc);
-            acc = fmaf(T6[v], k6, acc);
-            gs[v] = fmaf(T7[v], k7, acc);
+            if (FORCED) {
+                acc = fmaf(T6[v], k6, acc);
+                acc = fmaf(T7[v], k7, acc);
+            }
+            gs[v] = acc;
         }
     }
 }
 
 // One interior site, reduced-precision storage. Sites on a boundary-condition
 // wall are left to the perimeter kernel.
-template <bool CM, class S>
-__device__ __forceinline__ void interior_site_lowp(const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
-                                                   const LatDev& L, int t, int i, int j) {
+template <bool CM, bool FORCED, class S>
+__device__ __forceinline__ void interior_site_lowp_f(const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
+                                                     const LatDev& L, int t, int i, int j) {
     if (site_type(L, i, j) != LIFE_FLUID) return;
     const bool edge = (i == 0) | (i == L.Nx - 1) | (j == 0) | (j == L.Ny - 1);
     float g[9];
@@ -152,24 +165,39 @@ __device__ __forceinline__ void interior_site_lowp(const typename S::T* __restri
             g[v] = S::dev(A[(size_t)v * L.S + (size_t)sj * L.pitch + si], v);
         }
     }
-    float Fxd, Fyd, Gxd, Gyd;
-    force_xy_at_f(L, t, Fxd, Fyd);
-    force_xy_at_f(L, t + 1, Gxd, Gyd);
+    float Fxd = 0.0f, Fyd = 0.0f, Gxd = 0.0f, Gyd = 0.0f;
+    if (FORCED) {
+        force_xy_at_f(L, t, Fxd, Fyd);
+        force_xy_at_f(L, t + 1, Gxd, Gyd);
+    }
     const float dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
     const float rho = 1.0f + dr;
     const float mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
     const float my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
-    const float inv = 1.0f / rho;
-    const float ux = fmaf(0.5f, Fxd, mx) * inv, uy = fmaf(0.5f, Fyd, my) * inv;
+    const float inv = __frcp_rn(rho);  // = 1.0f / rho, correctly rounded
+    const float ux = (FORCED ? fmaf(0.5f, Fxd, mx) : mx) * inv, uy = (FORCED ? fmaf(0.5f, Fyd, my) : my) * inv;
     if (L.convective && i >= L.Nx - 3) {
         const int c = i - (L.Nx - 3);
         L.outlet_u[((size_t)c * L.Ny + j) * 2 + 0] = ux;
         L.outlet_u[((size_t)c * L.Ny + j) * 2 + 1] = uy;
     }
     float gs[9];
-    collide_dev32<CM>(g, dr, rho, mx, my, ux, uy, Gxd, Gyd, L.omega_f, gs);
+    collide_dev32<CM, FORCED>(g, dr, rho, mx, my, ux, uy, Gxd, Gyd, L.omega_f, gs);
 #pragma unroll
     for (int v = 0; v < 9; v++) B[(size_t)v * L.S + base] = S::put(gs[v], v);
+}
+
+// Whether step forces exist at all for this case (a value every thread of a
+// launch shares): a Womersley pressure gradient or a non-zero gravity.
+__device__ __forceinline__ bool lattice_forced(const LatDev& L) {
+    return L.womersley || L.Fx0_f != 0.0f || L.Fy0_f != 0.0f;
+}
+
+template <bool CM, class S>
+__device__ __forceinline__ void interior_site_lowp(const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
+                                                   const LatDev& L, int t, int i, int j) {
+    if (lattice_forced(L)) interior_site_lowp_f<CM, true, S>(A, B, L, t, i, j);
+    else interior_site_lowp_f<CM, false, S>(A, B, L, t, i, j);
 }
 
 template <bool CM, class S>
@@ -253,16 +281,21 @@ __device__ __noinline__ void perimeter_site_call(const typename S::T* __restrict
 // perimeter starts at once and finishes under the interior's time. The
 // launch bound keeps the interior's register budget (and occupancy); the
 // perimeter path spills to local memory instead.
+// The interior block index b splits into row j = b / bx and column block
+// b - j bx; with bx_m != 0 the quotient is __umulhi(b, bx_m), which the host
+// has checked to be exact for every b of the launch.
 template <bool CM, class S>
 __global__ void __launch_bounds__(256, 6) k_step_lowp(const typename S::T* __restrict__ A,
-                                                      typename S::T* __restrict__ B, LatDev L, int t, int pb, int bx) {
+                                                      typename S::T* __restrict__ B, LatDev L, int t, int pb, int bx,
+                                                      unsigned bx_m) {
     t = step_t(L, t);
     if ((int)blockIdx.x < pb) {
         perimeter_site_call<CM, S>(A, B, L, t, blockIdx.x * blockDim.x + threadIdx.x);
         return;
     }
-    const int b = blockIdx.x - pb;
-    const int i = (b % bx) * blockDim.x + threadIdx.x, j = b / bx;
+    const unsigned b = blockIdx.x - pb;
+    const int j = bx_m ? (int)__umulhi(b, bx_m) : (int)(b / (unsigned)bx);
+    const int i = (int)(b - (unsigned)j * (unsigned)bx) * blockDim.x + threadIdx.x;
     if (i >= L.Nx) return;
     interior_site_lowp<CM, S>(A, B, L, t, i, j);
 }
@@ -271,12 +304,18 @@ cudaError_t launch_step_lowp(const void* A, void* B, const LatDev& L, int t, cud
     const int n = 2 * L.Nx + 2 * (L.Ny - 2);
     const int pb = (n + 255) / 256, bx = (L.Nx + 255) / 256;
     const unsigned grid = (unsigned)(pb + bx * L.Ny);
+    // m = floor(2^32 / bx) + 1 gives floor(b / bx) = umulhi(b, m) exactly
+    // when b (m bx - 2^32) < 2^32 for the largest b; else divide
+    const unsigned long long m = (1ull << 32) / (unsigned long long)bx + 1ull;
+    const unsigned long long bmax = (unsigned long long)bx * (unsigned long long)L.Ny;
+    const unsigned bx_m = (m < (1ull << 32) && bmax * (m * (unsigned long long)bx - (1ull << 32)) < (1ull << 32))
+                              ? (unsigned)m : 0u;
     if (L.prec == LIFE_PREC_F32) {
-        if (L.cm) k_step_lowp<true, StoreF32><<<grid, 256, 0, s>>>((const float*)A, (float*)B, L, t, pb, bx);
-        else k_step_lowp<false, StoreF32><<<grid, 256, 0, s>>>((const float*)A, (float*)B, L, t, pb, bx);
+        if (L.cm) k_step_lowp<true, StoreF32><<<grid, 256, 0, s>>>((const float*)A, (float*)B, L, t, pb, bx, bx_m);
+        else k_step_lowp<false, StoreF32><<<grid, 256, 0, s>>>((const float*)A, (float*)B, L, t, pb, bx, bx_m);
     } else {
-        if (L.cm) k_step_lowp<true, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t, pb, bx);
-        else k_step_lowp<false, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t, pb, bx);
+        if (L.cm) k_step_lowp<true, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t, pb, bx, bx_m);
+        else k_step_lowp<false, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t, pb, bx, bx_m);
     }
     return cudaGetLastError();
 }
