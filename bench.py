@@ -613,13 +613,20 @@ def run_gb300(args, world, rank, local):
         done = args.warmup + args.steps
         c64.step(done - c64.t)
         c16.step(done - c16.t)
-        u64 = c64.fields(("u",))["u"]
-        umax = np.abs(u64).max()
+        ref = c64.fields(("rho", "u", "f"))
+        umax = np.abs(ref["u"]).max()
         for name, c in (("fp32", c32), ("fp16", c16)):
-            u = c.fields(("u",))["u"]
-            extras[f"{name}_velocity_rel_err"] = float(np.abs(u - u64).max() / umax)
+            got = c.fields(("rho", "u", "f"))
+            extras[f"{name}_velocity_rel_err"] = float(np.abs(got["u"] - ref["u"]).max() / umax)
+            # the other error measures: L2 (relative to the FP64 field's
+            # norm) of u and f, max-relative of f, max of rho - rho64
+            extras[f"{name}_velocity_l2_rel_err"] = float(np.linalg.norm(got["u"] - ref["u"]) / np.linalg.norm(ref["u"]))
+            extras[f"{name}_f_max_rel_err"] = float(np.abs(got["f"] - ref["f"]).max() / np.abs(ref["f"]).max())
+            extras[f"{name}_f_l2_rel_err"] = float(np.linalg.norm(got["f"] - ref["f"]) / np.linalg.norm(ref["f"]))
+            extras[f"{name}_rho_max_abs_err"] = float(np.abs(got["rho"] - ref["rho"]).max())
+            del got
         extras["error_after_steps"] = done
-        del c64, c16, u64
+        del c64, c16, ref
         # ---- rigid cylinder channel (1000 x 400, CM, IBM) and flexible
         # filament channel (1200 x 400, BGK, FEM), FP64 and FP32
         for prec, tag in ((PREC_F64, "fp64"), (PREC_F32, "fp32")):
@@ -702,6 +709,8 @@ def run_gb300(args, world, rank, local):
         if "fp64_mlups" in extras:
             line["fp32_vs_fp64"] = {"fp32_over_fp64_mlups": extras["fp32_over_fp64"],
                                     "fp32_velocity_rel_err": extras["fp32_velocity_rel_err"],
+                                    "fp32_velocity_l2_rel_err": extras["fp32_velocity_l2_rel_err"],
+                                    "fp32_f_max_rel_err": extras["fp32_f_max_rel_err"],
                                     "fp16_velocity_rel_err": extras["fp16_velocity_rel_err"]}
             ac = extras.get("accuracy", {})
             for key in ("cylinder_cd_rel_err", "cylinder_cl_amp_rel_err", "cylinder_period_rel_err",

@@ -7,6 +7,7 @@ namespace life {
 
 // Inverse central-moment transform (De Rosis 2019), term order as in the
 // reference (src/Grid.cpp:109-223); FP64 parity depends on that order.
+template <bool UNF>
 __device__ __forceinline__ void collide_cm(const double f[9], double rho, double ux, double uy, double Fx, double Fy,
                            double omega, double cs, double fs[9]) {
     double k4Pre = 0.0, k5Pre = 0.0;
@@ -30,7 +31,7 @@ __device__ __forceinline__ void collide_cm(const double f[9], double rho, double
     // The force moments k1, k2, k6, k7 are exact zeros when Fx = Fy = 0 (a
     // value the whole launch shares); their terms are then not formed, and
     // every other term is added in the reference's order.
-    const bool forced = Fx != 0.0 || Fy != 0.0;
+    const bool forced = !UNF && (Fx != 0.0 || Fy != 0.0);
     {
         double a = (X2 * Y2 - X2 - Y2 + 1.0) * k0;
         if (forced) a = a + ((2.0 * ux * Y2 - 2.0 * ux) * k1);

@@ -142,6 +142,22 @@ __device__ __forceinline__ void macroscopic(const double f[9], double Fx, double
     uy = (my + 0.5 * Fy) / r;
 }
 
+// macroscopic() for a zero force: m + 0.5 * (+-0) is m itself, since the
+// momentum sums start at +0 and a round-to-nearest sum is -0 only when both
+// of its terms are, so they are never -0.
+__device__ __forceinline__ void macroscopic_unforced(const double f[9], double& rho, double& ux, double& uy) {
+    double r = 0.0, mx = 0.0, my = 0.0;
+#pragma unroll
+    for (int v = 0; v < 9; v++) {
+        r = r + f[v];
+        mx = add_c(mx, cx_of(v), f[v]);
+        my = add_c(my, cy_of(v), f[v]);
+    }
+    rho = r;
+    ux = mx / r;
+    uy = my / r;
+}
+
 // IBMNodeClass::updateMacroscopic form (src/IBMNode.cpp:113-122): the IBM
 // force enters the velocity at support sites.
 __device__ __forceinline__ void macroscopic_ibm(const double f[9], double Fx, double Fy, double Ix,
@@ -193,18 +209,46 @@ __device__ __forceinline__ double lattice_force(int v, double ux, double uy, dou
 
 // BGK collision (src/Grid.cpp:236-244).
 // With no force at all (Fx = Fy = 0, a value the whole launch shares) the
-// forcing term is an exact zero added to a nonzero sum, so it is not formed.
+// forcing term is an exact zero added to a nonzero sum, so it is not formed;
+// UNF = true states that at compile time (no comparison at run time).
+// The equilibria are those of equilibrium<false>, value for value, with the
+// products that opposite directions share formed once: for c_w = -c_v,
+// c_w.u = -(c_v.u) and 3 (c_w.u) = -(3 c_v.u) exactly (negation commutes
+// with round-to-nearest), and 1 + 3 c.u adds the same operands either way (a
+// zero of either sign gives 1); the diagonal term 9 cx cy ux uy is
+// (9 ux) uy or its negative.
+template <bool UNF = false>
 __device__ __forceinline__ void collide_bgk(const double f[9], double rho, double ux, double uy, double Fx,
                                             double Fy, double omega, double fs[9]) {
-    const bool forced = Fx != 0.0 || Fy != 0.0;
+    const bool forced = !UNF && (Fx != 0.0 || Fy != 0.0);
+    const double px = 3.0 * ux, py = 3.0 * uy;
+    const double pa = 3.0 * (ux + uy), pb = 3.0 * (ux - uy);
+    const double d9 = 9.0 * ux * uy;
+    const double X2 = LSQ(ux), Y2 = LSQ(uy);
+    const double h00 = 4.5 * (X2 * (0.0 - 1.0 / 3.0) + Y2 * (0.0 - 1.0 / 3.0));
+    const double h10 = 4.5 * (X2 * (1.0 - 1.0 / 3.0) + Y2 * (0.0 - 1.0 / 3.0));
+    const double h01 = 4.5 * (X2 * (0.0 - 1.0 / 3.0) + Y2 * (1.0 - 1.0 / 3.0));
+    const double h11 = 4.5 * (X2 * (1.0 - 1.0 / 3.0) + Y2 * (1.0 - 1.0 / 3.0));
+    const double r0 = rho * (4.0 / 9.0), r1 = rho * (1.0 / 9.0), r2 = rho * (1.0 / 36.0);
+    double feq[9];
+    feq[0] = r0 * (1.0 + h00);
+    feq[1] = r1 * ((1.0 + px) + h10);
+    feq[2] = r1 * ((1.0 + -px) + h10);
+    feq[3] = r1 * ((1.0 + py) + h01);
+    feq[4] = r1 * ((1.0 + -py) + h01);
+    feq[5] = r2 * (((1.0 + pa) + h11) + d9);
+    feq[6] = r2 * (((1.0 + -pa) + h11) + d9);
+    feq[7] = r2 * (((1.0 + pb) + h11) + -d9);
+    feq[8] = r2 * (((1.0 + -pb) + h11) + -d9);
 #pragma unroll
     for (int v = 0; v < 9; v++) {
-        const double a = f[v] + omega * (equilibrium<false>(v, rho, ux, uy) - f[v]);
+        const double a = f[v] + omega * (feq[v] - f[v]);
         fs[v] = forced ? a + (1.0 - 0.5 * omega) * lattice_force(v, ux, uy, Fx, Fy) : a;
     }
 }
 
 // Central-moments collision (De Rosis 2019; src/Grid.cpp:106-233), in collide_cm.cuh.
+template <bool UNF = false>
 __device__ __forceinline__ void collide_cm(const double f[9], double rho, double ux, double uy, double Fx,
                                            double Fy, double omega, double cs, double fs[9]);
 
@@ -218,6 +262,14 @@ __device__ __forceinline__ void force_xy_at_f(const LatDev& L, int t, float& Fx,
         Fx = L.Fx0_f;
         Fy = L.Fy0_f;
     }
+}
+
+// Whether this case has a step force at all (a value every thread of a
+// launch shares): a Womersley pressure gradient or a gravity that is not
+// +-0, tested on the bits (no FP64 comparison).
+__device__ __forceinline__ bool lattice_forced_d(const LatDev& L) {
+    return L.womersley || ((unsigned long long)__double_as_longlong(L.Fx0) << 1) != 0ull ||
+           ((unsigned long long)__double_as_longlong(L.Fy0) << 1) != 0ull;
 }
 
 // Step index of a launch: its argument, or the device counter in a graph.
@@ -350,11 +402,11 @@ __device__ __forceinline__ void site_state(const typename S::T* __restrict__ P, 
     macroscopic(f, Fx, Fy, rho, ux, uy);
 }
 
-template <bool CM>
+template <bool CM, bool UNF = false>
 __device__ __forceinline__ void collide(const double f[9], double rho, double ux, double uy, double Fx, double Fy,
                                         double omega, double cs, double fs[9]) {
-    if (CM) collide_cm(f, rho, ux, uy, Fx, Fy, omega, cs, fs);
-    else collide_bgk(f, rho, ux, uy, Fx, Fy, omega, fs);
+    if (CM) collide_cm<UNF>(f, rho, ux, uy, Fx, Fy, omega, cs, fs);
+    else collide_bgk<UNF>(f, rho, ux, uy, Fx, Fy, omega, fs);
 }
 
 // Outlet side outputs of step t: final u of the last three columns and the

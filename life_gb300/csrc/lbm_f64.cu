@@ -57,10 +57,22 @@ __device__ __forceinline__ void interior_site_f64(const double* __restrict__ A, 
 #pragma unroll
         for (int v = 0; v < 9; v++) f[v] = A[(size_t)v * L.S + base - cx_of(v) - (long long)cy_of(v) * L.pitch];
     }
-    force_xy_at(L, t, Fx, Fy);
-    macroscopic(f, Fx, Fy, rho, ux, uy);
-    outlet_outputs(L, i, j, f, ux, uy);
-    store_collided<CM, StoreF64>(B, L, t + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
+    if (lattice_forced_d(L)) {
+        force_xy_at(L, t, Fx, Fy);
+        macroscopic(f, Fx, Fy, rho, ux, uy);
+        outlet_outputs(L, i, j, f, ux, uy);
+        store_collided<CM, StoreF64>(B, L, t + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
+    } else {
+        // zero force at every step: the velocity without the force half-term
+        // (the same value) and no forcing terms in the collision
+        macroscopic_unforced(f, rho, ux, uy);
+        outlet_outputs(L, i, j, f, ux, uy);
+        double fs[9];
+        collide<CM, true>(f, rho, ux, uy, 0.0, 0.0, L.omega, L.cs, fs);
+        const size_t s = (size_t)j * L.pitch + i;
+#pragma unroll
+        for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = fs[v];
+    }
 }
 
 template <bool CM>
