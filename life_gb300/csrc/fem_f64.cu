@@ -691,6 +691,27 @@ __device__ void band_lu_forward(double* Bd, int nn, int kl, int ku, int W, int* 
     }
 }
 
+// The forward half of the transposed solve alone (U^T y = b, y in place) on
+// factors band_lu_forward produced earlier: warp 2's part of that routine
+// without the pipeline, the same operations in the same order. One warp.
+__device__ void band_forward_only(const double* Bd_, int nn, int kl, int ku, int W, double* y, const double* rcp) {
+    double* Bd = const_cast<double*>(Bd_);
+    const int lane = threadIdx.x & 31, w = kl + ku;
+    double t = lane < nn ? y[lane] : 0.0;
+    for (int k = 0; k < nn; k++) {
+        const int owner = k & 31;
+        const double tk = __shfl_sync(0xffffffffu, t, owner);
+        const double yk = div_rn_recip(tk, bd(Bd, W, kl, k, k), rcp[k]);
+        if (lane == owner) {
+            y[k] = yk;
+            t = k + 32 < nn ? y[k + 32] : 0.0;
+        }
+        const int rr = k + 1 + ((lane - k - 1) & 31);
+        if (rr <= k + w && rr < nn) t = t - bd(Bd, W, kl, k, rr) * yk;
+    }
+    __syncwarp();
+}
+
 // Backward half of the transposed solve (L^T), one warp, after
 // band_lu_forward: lane l forms the product of the multiplier stored in band
 // row i+1+l with y at its final row Fp[i+1+l] (Fp: nn ints of scratch) and
@@ -1045,6 +1066,19 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
     int* sPiv = reinterpret_cast<int*>(sY + nn);
     int* sFp = sPiv + nn;
     double* sRcp = reinterpret_cast<double*>(sFp + nn);  // [nn] pivot reciprocals
+    // Every subiteration restarts from U_n (U = U_n, Udot = Udot_n, ...), so
+    // the first Newton iteration of every subiteration of a step builds the
+    // same element matrices, internal force F, K_eff = K + a0 M and M v with
+    // v = a0 (U_n - U) + a2 Udot + a3 Udotdot; only the load R differs.
+    // Subiteration 0 keeps that iteration's LU factors, F and M v; the later
+    // subiterations form F_eff = (R - F) + M v from them and solve with the
+    // kept factors (the same factorisation of the same matrix).
+    const bool reuse = F.s->subIt > 0;
+    double* cBd = B.lu_cache;
+    double* cRcp = cBd + (size_t)nn * KW;
+    double* cF = cRcp + nn;
+    double* cMv = cF + n;
+    int* cPiv = reinterpret_cast<int*>(cMv + n);
     {
         double* U = vec(B, V_U);
         double* Ud = vec(B, V_Udot);
@@ -1102,103 +1136,136 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
     if (threadIdx.x == 0) s_it = 0;
     __syncthreads();
     do {
-        // buildGlobalMatrices (src/FEMBody.cpp:90-109)
-        for (int e = threadIdx.x; e < B.nEl; e += blockDim.x) {
-            const double* el = B.el + (size_t)e * EL_STRIDE;
-            const double L = el[EL_L], L0 = el[EL_L0], E = el[EL_E], A = el[EL_A], I = el[EL_I];
-            const double c = el[EL_COS], s = el[EL_SIN], ang = el[EL_ANG];
-            const double u = (DSQ(L) - DSQ(L0)) / (L + L0);
-            const double th1 = shift_angle_d(B.node[e * 6 + 5] - ang);
-            const double th2 = shift_angle_d(B.node[(e + 1) * 6 + 5] - ang);
-            const double F0 = (E * A / L0) * u;
-            const double M1 = (2 * E * I / L0) * (2.0 * th1 + th2);
-            const double M2 = (2 * E * I / L0) * (th1 + 2.0 * th2);
-            double Fl[6];
-            Fl[0] = -F0;
-            Fl[1] = (1.0 / L0) * (M1 + M2);
-            Fl[2] = M1;
-            Fl[3] = F0;
-            Fl[4] = -(1.0 / L0) * (M1 + M2);
-            Fl[5] = M2;
-            double* sc = B.elscr + (size_t)e * ES_STRIDE;
-            tt_vec(Fl, c, s, sc + ES_F);
-            tt_a_t(el + EL_M, c, s, sc + ES_M);
-            double G[36], G2[36], KNL[36];
-            tt_a_t(el + EL_KL, c, s, G);
-            const double Fa = -Fl[0], V0 = Fl[4];
-#pragma unroll
-            for (int q = 0; q < 36; q++) KNL[q] = 0.0;
-            KNL[0 * 6 + 1] = -V0 / L0;
-            KNL[0 * 6 + 4] = V0 / L0;
-            KNL[1 * 6 + 0] = -V0 / L0;
-            KNL[1 * 6 + 1] = Fa / L0;
-            KNL[1 * 6 + 3] = V0 / L0;
-            KNL[1 * 6 + 4] = -Fa / L0;
-            KNL[3 * 6 + 1] = V0 / L0;
-            KNL[3 * 6 + 4] = -V0 / L0;
-            KNL[4 * 6 + 0] = V0 / L0;
-            KNL[4 * 6 + 1] = -Fa / L0;
-            KNL[4 * 6 + 3] = -V0 / L0;
-            KNL[4 * 6 + 4] = Fa / L0;
-            tt_a_t(KNL, c, s, G2);
-#pragma unroll
-            for (int q = 0; q < 36; q++) sc[ES_K + q] = G[q] + G2[q];
-        }
-        __syncthreads();
-        // Ordered assembly of M, K (band |r-c| <= 5) and F, then setNewmark
-        // (src/FEMBody.cpp:112-126): K_eff = K + a0*M goes straight into the
-        // shared-memory band of the LU's view M(i,j) = K_eff[bc+j][bc+i].
-        {
+        const bool first = s_it == 0;
+        if (first && reuse) {
+            // the kept factors and vectors of this step's first iteration
             double* Fv = vec(B, V_F);
-            for (int q = threadIdx.x; q < nn * KW; q += blockDim.x) sBd[q] = 0.0;
-            for (int p = threadIdx.x; p < n * 11; p += blockDim.x) {
-                const int r = p / 11, cc = r - 5 + p % 11;
-                if (cc < 0 || cc >= n) continue;
-                double am = 0.0, ak = 0.0;
-                const int lo = (r > cc ? r : cc), hi = (r < cc ? r : cc);
-                for (int e = (lo / 3 - 1 < 0 ? 0 : lo / 3 - 1); e <= hi / 3 && e < B.nEl; e++) {
-                    const int li = r - 3 * e, lj = cc - 3 * e;
-                    if (li < 0 || li > 5 || lj < 0 || lj > 5) continue;
-                    const double* sc = B.elscr + (size_t)e * ES_STRIDE;
-                    am += sc[ES_M + li * 6 + lj];
-                    ak += sc[ES_K + li * 6 + lj];
-                }
-                sMb[p] = am;
-                sKe[p] = ak;
-            }
-            for (int r = threadIdx.x; r < n; r += blockDim.x) {
-                double af = 0.0;
-                for (int e = (r / 3 - 1 < 0 ? 0 : r / 3 - 1); e <= r / 3 && e < B.nEl; e++)
-                    af += B.elscr[(size_t)e * ES_STRIDE + ES_F + (r - 3 * e)];
-                Fv[r] = af;
-            }
-            const double* U = vec(B, V_U);
-            const double* Un = vec(B, V_Un);
-            const double* Ud = vec(B, V_Udot);
-            const double* Udd = vec(B, V_Udotdot);
-            for (int i = threadIdx.x; i < n; i += blockDim.x) sV[i] = a0 * (Un[i] - U[i]) + a2 * Ud[i] + a3 * Udd[i];
-            __syncthreads();
             const double* Rv = vec(B, V_R);
+            for (int q = threadIdx.x; q < nn * KW; q += blockDim.x) sBd[q] = cBd[q];
+            for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+                sPiv[i] = cPiv[i];
+                sRcp[i] = cRcp[i];
+            }
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                double mv = 0.0;
-                for (int j = (i - 5 < 0 ? 0 : i - 5); j <= i + 5 && j < n; j++) mv += sMb[i * 11 + (j - i + 5)] * sV[j];
-                const double fe = Rv[i] - Fv[i] + mv;
+                const double fe = Rv[i] - cF[i] + cMv[i];
                 Fv[i] = fe;
                 if (i >= B.bc) sY[i - B.bc] = fe;
             }
-            for (int p = threadIdx.x; p < n * 11; p += blockDim.x) {
-                const int r = p / 11, cc = r - 5 + p % 11;
-                if (cc < B.bc || cc >= n || r < B.bc) continue;
-                const double keff = sKe[p] + a0 * sMb[p];
-                bd(sBd, KW, 5, cc - B.bc, r - B.bc) = keff;
+            __syncthreads();
+            if (threadIdx.x < 32) band_forward_only(sBd, nn, 5, 5, KW, sY, sRcp);
+            __syncthreads();
+            if (threadIdx.x < 32) band_solve_back(sBd, nn, 5, KW, sPiv, sFp, sY);
+            __syncthreads();
+        } else {
+            // buildGlobalMatrices (src/FEMBody.cpp:90-109)
+            for (int e = threadIdx.x; e < B.nEl; e += blockDim.x) {
+                const double* el = B.el + (size_t)e * EL_STRIDE;
+                const double L = el[EL_L], L0 = el[EL_L0], E = el[EL_E], A = el[EL_A], I = el[EL_I];
+                const double c = el[EL_COS], s = el[EL_SIN], ang = el[EL_ANG];
+                const double u = (DSQ(L) - DSQ(L0)) / (L + L0);
+                const double th1 = shift_angle_d(B.node[e * 6 + 5] - ang);
+                const double th2 = shift_angle_d(B.node[(e + 1) * 6 + 5] - ang);
+                const double F0 = (E * A / L0) * u;
+                const double M1 = (2 * E * I / L0) * (2.0 * th1 + th2);
+                const double M2 = (2 * E * I / L0) * (th1 + 2.0 * th2);
+                double Fl[6];
+                Fl[0] = -F0;
+                Fl[1] = (1.0 / L0) * (M1 + M2);
+                Fl[2] = M1;
+                Fl[3] = F0;
+                Fl[4] = -(1.0 / L0) * (M1 + M2);
+                Fl[5] = M2;
+                double* sc = B.elscr + (size_t)e * ES_STRIDE;
+                tt_vec(Fl, c, s, sc + ES_F);
+                tt_a_t(el + EL_M, c, s, sc + ES_M);
+                double G[36], G2[36], KNL[36];
+                tt_a_t(el + EL_KL, c, s, G);
+                const double Fa = -Fl[0], V0 = Fl[4];
+    #pragma unroll
+                for (int q = 0; q < 36; q++) KNL[q] = 0.0;
+                KNL[0 * 6 + 1] = -V0 / L0;
+                KNL[0 * 6 + 4] = V0 / L0;
+                KNL[1 * 6 + 0] = -V0 / L0;
+                KNL[1 * 6 + 1] = Fa / L0;
+                KNL[1 * 6 + 3] = V0 / L0;
+                KNL[1 * 6 + 4] = -Fa / L0;
+                KNL[3 * 6 + 1] = V0 / L0;
+                KNL[3 * 6 + 4] = -V0 / L0;
+                KNL[4 * 6 + 0] = V0 / L0;
+                KNL[4 * 6 + 1] = -Fa / L0;
+                KNL[4 * 6 + 3] = -V0 / L0;
+                KNL[4 * 6 + 4] = Fa / L0;
+                tt_a_t(KNL, c, s, G2);
+    #pragma unroll
+                for (int q = 0; q < 36; q++) sc[ES_K + q] = G[q] + G2[q];
             }
+            __syncthreads();
+            // Ordered assembly of M, K (band |r-c| <= 5) and F, then setNewmark
+            // (src/FEMBody.cpp:112-126): K_eff = K + a0*M goes straight into the
+            // shared-memory band of the LU's view M(i,j) = K_eff[bc+j][bc+i].
+            {
+                double* Fv = vec(B, V_F);
+                for (int q = threadIdx.x; q < nn * KW; q += blockDim.x) sBd[q] = 0.0;
+                for (int p = threadIdx.x; p < n * 11; p += blockDim.x) {
+                    const int r = p / 11, cc = r - 5 + p % 11;
+                    if (cc < 0 || cc >= n) continue;
+                    double am = 0.0, ak = 0.0;
+                    const int lo = (r > cc ? r : cc), hi = (r < cc ? r : cc);
+                    for (int e = (lo / 3 - 1 < 0 ? 0 : lo / 3 - 1); e <= hi / 3 && e < B.nEl; e++) {
+                        const int li = r - 3 * e, lj = cc - 3 * e;
+                        if (li < 0 || li > 5 || lj < 0 || lj > 5) continue;
+                        const double* sc = B.elscr + (size_t)e * ES_STRIDE;
+                        am += sc[ES_M + li * 6 + lj];
+                        ak += sc[ES_K + li * 6 + lj];
+                    }
+                    sMb[p] = am;
+                    sKe[p] = ak;
+                }
+                for (int r = threadIdx.x; r < n; r += blockDim.x) {
+                    double af = 0.0;
+                    for (int e = (r / 3 - 1 < 0 ? 0 : r / 3 - 1); e <= r / 3 && e < B.nEl; e++)
+                        af += B.elscr[(size_t)e * ES_STRIDE + ES_F + (r - 3 * e)];
+                    Fv[r] = af;
+                }
+                const double* U = vec(B, V_U);
+                const double* Un = vec(B, V_Un);
+                const double* Ud = vec(B, V_Udot);
+                const double* Udd = vec(B, V_Udotdot);
+                for (int i = threadIdx.x; i < n; i += blockDim.x) sV[i] = a0 * (Un[i] - U[i]) + a2 * Ud[i] + a3 * Udd[i];
+                __syncthreads();
+                const double* Rv = vec(B, V_R);
+                for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                    double mv = 0.0;
+                    for (int j = (i - 5 < 0 ? 0 : i - 5); j <= i + 5 && j < n; j++) mv += sMb[i * 11 + (j - i + 5)] * sV[j];
+                    if (first) {
+                        cF[i] = Fv[i];
+                        cMv[i] = mv;
+                    }
+                    const double fe = Rv[i] - Fv[i] + mv;
+                    Fv[i] = fe;
+                    if (i >= B.bc) sY[i - B.bc] = fe;
+                }
+                for (int p = threadIdx.x; p < n * 11; p += blockDim.x) {
+                    const int r = p / 11, cc = r - 5 + p % 11;
+                    if (cc < B.bc || cc >= n || r < B.bc) continue;
+                    const double keff = sKe[p] + a0 * sMb[p];
+                    bd(sBd, KW, 5, cc - B.bc, r - B.bc) = keff;
+                }
+            }
+            __syncthreads();
+            // delU = solveLAPACK(K, F, bcDOFs) (src/Utils.cpp:288-311)
+            if (threadIdx.x < 128) band_lu_forward(sBd, nn, 5, 5, KW, sPiv, sY, sRcp);
+            __syncthreads();
+            if (first) {
+                for (int q = threadIdx.x; q < nn * KW; q += blockDim.x) cBd[q] = sBd[q];
+                for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+                    cPiv[i] = sPiv[i];
+                    cRcp[i] = sRcp[i];
+                }
+            }
+            if (threadIdx.x < 32) band_solve_back(sBd, nn, 5, KW, sPiv, sFp, sY);
+            __syncthreads();
         }
-        __syncthreads();
-        // delU = solveLAPACK(K, F, bcDOFs) (src/Utils.cpp:288-311)
-        if (threadIdx.x < 128) band_lu_forward(sBd, nn, 5, 5, KW, sPiv, sY, sRcp);
-        __syncthreads();
-        if (threadIdx.x < 32) band_solve_back(sBd, nn, 5, KW, sPiv, sFp, sY);
-        __syncthreads();
         {
             double* dU = vec(B, V_delU);
             for (int i = threadIdx.x; i < n; i += blockDim.x) dU[i] = i < B.bc ? 0.0 : sY[i - B.bc];

@@ -156,8 +156,8 @@ int setup_fem(LifeCase* c) {
         }
         fStart[f.nEl] = (int)fNode.size();
         D.nfmap = (int)fNode.size();
-        if ((rc = upload(c, &D.pool, pool)) || (rc = fallocT(c, &D.K, (size_t)n * n)) ||
-            (rc = fallocT(c, &D.M, (size_t)n * n)) || (rc = upload(c, &D.node, node)) || (rc = upload(c, &D.el, el)) ||
+        if ((rc = upload(c, &D.pool, pool)) || (rc = fallocT(c, &D.lu_cache, fem_cache_doubles(n, D.bc))) ||
+            (rc = upload(c, &D.node, node)) || (rc = upload(c, &D.el, el)) ||
             (rc = fallocT(c, &D.elscr, (size_t)f.nEl * ES_STRIDE)) || (rc = upload(c, &D.fmapStart, fStart)) ||
             (rc = upload(c, &D.fmapEl, fEl)) || (rc = upload(c, &D.fmapNode, fNode)) || (rc = upload(c, &D.fmapZ, fZ)) ||
             (rc = fallocT(c, &D.rgscr, (size_t)D.nfmap * 6)) || (rc = upload(c, &D.mapEl, f.mapEl)) ||
@@ -165,7 +165,6 @@ int setup_fem(LifeCase* c) {
             (rc = fallocT(c, &D.lmax, (size_t)n)) || (rc = fallocT(c, &D.epsA, (size_t)D.nMark * D.nMark)) ||
             (rc = fallocT(c, &D.epsB, (size_t)D.nMark)))
             return rc;
-        CK(cudaMemset(D.M, 0, sizeof(double) * n * n));
         H->bodies.push_back(D);
         H->hostBody.push_back((int)b);
     }
