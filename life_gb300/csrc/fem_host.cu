@@ -38,16 +38,7 @@ struct FemHost {
         if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
     } while (0)
 
-static int falloc(LifeCase* c, void** p, size_t bytes) {
-    cudaError_t e = cudaMalloc(p, bytes ? bytes : 8);
-    if (e != cudaSuccess) {
-        *p = nullptr;
-        return set_error(LIFE_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    }
-    c->allocs.push_back(*p);
-    c->dev_bytes += bytes;
-    return LIFE_OK;
-}
+static int falloc(LifeCase* c, void** p, size_t bytes) { return case_dev_alloc(c, p, bytes); }
 template <class T>
 static int fallocT(LifeCase* c, T** p, size_t n) {
     return falloc(c, (void**)p, sizeof(T) * n);

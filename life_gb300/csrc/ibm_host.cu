@@ -20,16 +20,7 @@ using namespace life;
         if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
     } while (0)
 
-static int alloc_track(LifeCase* c, void** p, size_t bytes) {
-    cudaError_t e = cudaMalloc(p, bytes ? bytes : 8);
-    if (e != cudaSuccess) {
-        *p = nullptr;
-        return set_error(LIFE_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    }
-    c->allocs.push_back(*p);
-    c->dev_bytes += bytes;
-    return LIFE_OK;
-}
+static int alloc_track(LifeCase* c, void** p, size_t bytes) { return case_dev_alloc(c, p, bytes); }
 template <class T>
 static int alloc_t(LifeCase* c, T** p, size_t n) {
     return alloc_track(c, (void**)p, sizeof(T) * n);

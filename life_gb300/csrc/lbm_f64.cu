@@ -25,19 +25,43 @@ namespace life {
 // initial velocity, f = feq; then the collision of step t0+1.
 template <bool CM, class S>
 __global__ void k_init(typename S::T* __restrict__ B, LatDev L, int t0) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-    if (i >= L.Nx) return;
-    double ux, uy;
-    if (L.init_mode == 0) { ux = 0.0; uy = 0.0; }
-    else if (L.init_mode == 1) { ux = L.u_in[j * 2]; uy = L.u_in[j * 2 + 1]; }
-    else { ux = L.u0x; uy = L.u0y; }
-    if (site_type(L, i, j) == LIFE_WALL) { ux = 0.0; uy = 0.0; }
-    const double rho = 1.0;
-    double f[9];
+    // Every site of row j starts from the equilibrium at rho = 1 of one of two
+    // velocities: the row's (uniform, or the inlet profile at j) or zero at a
+    // wall site. Two threads form the two variants' populations and their
+    // collision for the first step (store_collided's arithmetic) once; every
+    // site then stores its variant.
+    __shared__ typename S::T s_out[2][9];
+    __shared__ double s_f[2][9];
+    __shared__ double s_u[2][2];
+    const int j = blockIdx.y;
+    if (threadIdx.x < 2) {
+        const int w = threadIdx.x;
+        double ux, uy;
+        if (w == 1 || L.init_mode == 0) { ux = 0.0; uy = 0.0; }
+        else if (L.init_mode == 1) { ux = L.u_in[j * 2]; uy = L.u_in[j * 2 + 1]; }
+        else { ux = L.u0x; uy = L.u0y; }
+        const double rho = 1.0;
+        double f[9], fs[9], Fx, Fy;
 #pragma unroll
-    for (int v = 0; v < 9; v++) f[v] = equilibrium<CM>(v, rho, ux, uy);
-    outlet_outputs(L, i, j, f, ux, uy);
-    store_collided<CM, S>(B, L, t0 + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
+        for (int v = 0; v < 9; v++) f[v] = equilibrium<CM>(v, rho, ux, uy);
+        force_xy_at(L, t0 + 1, Fx, Fy);
+        collide<CM>(f, rho, ux, uy, Fx + 0.0, Fy + 0.0, L.omega, L.cs, fs);
+#pragma unroll
+        for (int v = 0; v < 9; v++) {
+            s_out[w][v] = S::save(fs[v], v);
+            s_f[w][v] = f[v];
+        }
+        s_u[w][0] = ux;
+        s_u[w][1] = uy;
+    }
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= L.Nx) return;
+    const int w = site_type(L, i, j) == LIFE_WALL ? 1 : 0;
+    outlet_outputs(L, i, j, s_f[w], s_u[w][0], s_u[w][1]);
+    const size_t s = (size_t)j * L.pitch + i;
+#pragma unroll
+    for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = s_out[w][v];
 }
 
 // One time step, interior sites, FP64: S_t from P_t (A), then P_{t+1} into B.

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -46,17 +47,87 @@ int cuda_fail(cudaError_t e, const char* where) {
 extern "C" int life_abi_version(void) { return LIFE_ABI_VERSION; }
 extern "C" const char* life_last_error(void) { return g_err.c_str(); }
 
-static int dev_alloc(LifeCase* c, void** p, size_t bytes) {
-    cudaError_t e = cudaMalloc(p, bytes);
+// The large buffers of a case (population planes, force fields: 1 MiB and
+// up) come from the device's stream-ordered memory pool, set to keep what is
+// freed: a case created after another was destroyed (a served request, a
+// batch rebuilt) reuses that memory instead of mapping new pages. Allocation
+// and release are ordered on one allocation stream per device; each
+// allocation is complete before it is handed out, and a case's memory is
+// released only after every stream that used it has drained. The many small buffers (per-body arrays) use cudaMalloc,
+// which needs no synchronisation per allocation; so do devices without
+// memory pools.
+namespace {
+struct DevicePool {
+    bool init = false, pooled = false;
+    cudaStream_t s = nullptr;
+};
+DevicePool g_pools[64];
+std::mutex g_pool_mu;
+
+DevicePool* device_pool(int dev) {
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    DevicePool& P = g_pools[dev];
+    if (!P.init) {
+        P.init = true;
+        int ok = 0;
+        if (cudaDeviceGetAttribute(&ok, cudaDevAttrMemoryPoolsSupported, dev) == cudaSuccess && ok) {
+            cudaMemPool_t pool;
+            unsigned long long keep = ~0ull;
+            if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess &&
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) == cudaSuccess &&
+                cudaStreamCreateWithFlags(&P.s, cudaStreamNonBlocking) == cudaSuccess)
+                P.pooled = true;
+        }
+        cudaGetLastError();
+    }
+    return &P;
+}
+}  // namespace
+
+int life::case_dev_alloc(LifeCase* c, void** p, size_t bytes) {
+    if (!bytes) bytes = 8;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    DevicePool* P = device_pool(dev);
+    cudaError_t e;
+    const bool pooled = P && P->pooled && bytes >= (1u << 20);
+    if (pooled) {
+        e = cudaMallocAsync(p, bytes, P->s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(P->s);
+    } else {
+        e = cudaMalloc(p, bytes);
+    }
     if (e != cudaSuccess) {
         *p = nullptr;
+        cudaGetLastError();
         return set_error(e == cudaErrorMemoryAllocation ? LIFE_ERR_NOMEM : LIFE_ERR_CUDA,
-                         std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+                         std::string("device allocation (") + std::to_string(bytes) + " bytes): " +
+                             cudaGetErrorString(e));
     }
     c->allocs.push_back(*p);
+    c->alloc_pooled.push_back(pooled ? 1 : 0);
     c->dev_bytes += bytes;
     return LIFE_OK;
 }
+
+// Called with the case's device current and every stream that used the
+// case's memory idle.
+void life::case_dev_free_all(LifeCase* c) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    DevicePool* P = device_pool(dev);
+    for (size_t k = 0; k < c->allocs.size(); k++) {
+        void* p = c->allocs[k];
+        if (!p) continue;
+        if (c->alloc_pooled[k] && P && P->pooled) cudaFreeAsync(p, P->s);
+        else cudaFree(p);
+    }
+    c->allocs.clear();
+    c->alloc_pooled.clear();
+}
+
+static int dev_alloc(LifeCase* c, void** p, size_t bytes) { return case_dev_alloc(c, p, bytes); }
 
 template <class T>
 static int dev_alloc_t(LifeCase* c, T** p, size_t count) {
@@ -174,12 +245,16 @@ static void free_case(LifeCase* c) {
     int prev = -1;
     cudaGetDevice(&prev);
     if (c->device >= 0) cudaSetDevice(c->device);
-    if (c->stream) cudaStreamSynchronize(c->stream);
-    free_fem(c);
-    for (void* p : c->allocs)
-        if (p) cudaFree(p);
-    if (c->side) cudaStreamSynchronize(c->side);
+    // the case's own streams drain before its memory returns to the pool. A
+    // batch that steps the case (a user batch, a server group) synchronises
+    // its stream before it lets go of its cases, so no other work can still
+    // use the memory. (No device-wide synchronisation: another thread may be
+    // capturing a graph.)
+    for (cudaStream_t s : {c->stream, c->side, c->aux})
+        if (s) cudaStreamSynchronize(s);
     if (c->self_batch) batch_free(c->self_batch);
+    free_fem(c);
+    case_dev_free_all(c);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->ev_out) cudaEventDestroy(c->ev_out);

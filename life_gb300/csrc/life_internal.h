@@ -29,6 +29,10 @@ struct FemHost;  // fem_host.cu
 
 int set_error(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* where);
+// Device memory of a case, tracked in c->allocs and c->dev_bytes and
+// released by the case's destruction (case_dev_free_all).
+int case_dev_alloc(LifeCase* c, void** p, size_t bytes);
+void case_dev_free_all(LifeCase* c);
 
 }  // namespace life
 
@@ -69,6 +73,7 @@ struct LifeCase {
     bool host_steps = false;
     size_t dev_bytes = 0;
     std::vector<void*> allocs;
+    std::vector<char> alloc_pooled;  // allocs[k] came from the memory pool
     // immersed bodies
     life::Grid0 g0{};
     life::HObjects obj;

@@ -172,13 +172,24 @@ class Case:
     def sync(self) -> None:
         _check(lib().life_case_sync(self._h))
 
-    def fields(self, which=("rho", "u", "f", "force_ibm")) -> Dict[str, np.ndarray]:
+    def fields(self, which=("rho", "u", "f", "force_ibm"), out: Optional[Dict[str, np.ndarray]] = None
+               ) -> Dict[str, np.ndarray]:
+        """The fields of `which` in the reference layout. `out` may hold
+        caller-owned arrays to fill (C-contiguous float64 of the right shape),
+        as a host program reuses its own buffers from step to step."""
         n = self.params.Nx * self.params.Ny
+        shapes = {"rho": (n,), "u": (n, 2), "f": (n, 9), "force_ibm": (n, 2)}
+        given = out or {}
+        for k, a in given.items():
+            if k not in shapes or a.shape != shapes[k] or a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError(f"out[{k!r}] must be a C-contiguous float64 array of shape {shapes.get(k)}")
         out = {}
-        rho = np.empty(n) if "rho" in which else None
-        u = np.empty((n, 2)) if "u" in which else None
-        f = np.empty((n, 9)) if "f" in which else None
-        fi = np.empty((n, 2)) if "force_ibm" in which else None
+
+        def buf(k):
+            if k not in which:
+                return None
+            return given[k] if k in given else np.empty(shapes[k])
+        rho, u, f, fi = buf("rho"), buf("u"), buf("f"), buf("force_ibm")
         _check(lib().life_case_get_fields(self._h, _p(rho), _p(u), _p(f), _p(fi)))
         for k, v in (("rho", rho), ("u", u), ("f", f), ("force_ibm", fi)):
             if v is not None:
