@@ -110,3 +110,24 @@ def test_max_velocity_matches_fields():
         u = c.fields(("u",))["u"]
     assert not nan
     assert m == np.sqrt(u[:, 0] ** 2 + u[:, 1] ** 2).max()
+
+
+def test_fields_into_caller_buffers():
+    """fields(out=...) fills the caller's arrays with exactly what the
+    allocating call returns, and rejects arrays of the wrong shape or type."""
+    from life_gb300.lib import Case
+    p, b = CASES["cylinder_rigid_cm"]
+    with Case(p, b) as c:
+        c.step(11)
+        ref = c.fields()
+        n = p.Nx * p.Ny
+        out = {"rho": np.full(n, np.nan), "u": np.full((n, 2), np.nan), "f": np.full((n, 9), np.nan),
+               "force_ibm": np.full((n, 2), np.nan)}
+        got = c.fields(out=out)
+        for key in ("rho", "u", "f", "force_ibm"):
+            assert got[key] is out[key]
+            assert np.array_equal(out[key], ref[key]), key
+        with pytest.raises(ValueError):
+            c.fields(("u",), out={"u": np.zeros((n, 3))})
+        with pytest.raises(ValueError):
+            c.fields(("u",), out={"u": np.zeros((n, 2), dtype=np.float32)})
