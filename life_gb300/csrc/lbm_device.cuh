@@ -47,6 +47,19 @@ __device__ __forceinline__ float h16_scale(int v) { return v == 0 ? 0.5f : (v < 
 __device__ __forceinline__ float h16_inv(int v) { return v == 0 ? 2.0f : (v < 5 ? 8.0f : 32.0f); }
 __device__ __forceinline__ float wgt_f(int v) { return v == 0 ? 4.0f / 9.0f : (v < 5 ? 1.0f / 9.0f : 1.0f / 36.0f); }
 
+// float -> double, the exact value. On GB300 the hardware conversion issues
+// to the narrow FP64 pipe; for normal floats the double's fields are the
+// float's, rebiased, so integer operations give the same bits. Zeros,
+// subnormals, infinities and NaNs take the hardware conversion.
+__device__ __forceinline__ double f2d(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;
+    return __longlong_as_double((long long)(((unsigned long long)(b >> 31) << 63) |
+                                            ((unsigned long long)(e + (1023u - 127u)) << 52) |
+                                            ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+
 struct StoreF64 {
     using T = double;
     static constexpr int prec = LIFE_PREC_F64;
@@ -56,7 +69,7 @@ struct StoreF64 {
 struct StoreF32 {
     using T = float;
     static constexpr int prec = LIFE_PREC_F32;
-    __device__ static __forceinline__ double load(T x, int v) { return (double)x + wgt(v); }
+    __device__ static __forceinline__ double load(T x, int v) { return f2d(x) + wgt(v); }
     __device__ static __forceinline__ T save(double f, int v) { return (float)(f - wgt(v)); }
     __device__ static __forceinline__ float dev(T x, int) { return x; }      // g_v
     __device__ static __forceinline__ T put(float g, int) { return g; }
@@ -65,7 +78,7 @@ struct StoreF16 {
     using T = __half;
     static constexpr int prec = LIFE_PREC_F16;
     __device__ static __forceinline__ double load(T x, int v) {
-        return (double)(__half2float(x) * h16_scale(v)) + wgt(v);
+        return f2d(__half2float(x) * h16_scale(v)) + wgt(v);
     }
     __device__ static __forceinline__ T save(double f, int v) {
         return __float2half_rn((float)(f - wgt(v)) * h16_inv(v));

@@ -188,9 +188,12 @@ __global__ void k_state(typename S::T* __restrict__ B, LatDev L, int t, const do
 // GridClass::writeRestart dumps, src/Grid.cpp:1191-1222).
 template <bool CM, class S>
 __global__ void k_export(const typename S::T* __restrict__ P, LatDev L, int t, double* __restrict__ rho_out,
-                             double* __restrict__ u_out, double* __restrict__ f_out, double* __restrict__ fibm_out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-    if (i >= L.Nx) return;
+                             double* __restrict__ u_out, double* __restrict__ f_out, double* __restrict__ fibm_out,
+                             int i0, int i1) {
+    // columns i0 <= i < i1 (their reference-layout rows id = i*Ny + j are
+    // one contiguous range of the output)
+    const int i = i0 + blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= i1) return;
     double f[9], rho, ux, uy;
     site_state<CM, S>(P, L, t, i, j, f, rho, ux, uy);
     double Ix = 0.0, Iy = 0.0;
@@ -326,12 +329,24 @@ cudaError_t launch_state(void* B, const LatDev& L, int t, const double* rho, con
 }
 
 cudaError_t launch_export(const void* P, const LatDev& L, int t, bool initial, double* rho, double* u, double* f,
-                          double* fibm, cudaStream_t s) {
+                          double* fibm, cudaStream_t s, int i0, int i1) {
+    if (i1 < 0) i1 = L.Nx;
     if (initial) {
         if (L.cm) k_export_init<true><<<grid_of(L), 128, 0, s>>>(L, rho, u, f, fibm);
         else k_export_init<false><<<grid_of(L), 128, 0, s>>>(L, rho, u, f, fibm);
+        return cudaGetLastError();
+    }
+    if (i1 <= i0) return cudaSuccess;
+    const dim3 g((i1 - i0 + 127) / 128, L.Ny);
+    if (L.prec == LIFE_PREC_F64) {
+        if (L.cm) k_export<true, StoreF64><<<g, 128, 0, s>>>((const double*)P, L, t, rho, u, f, fibm, i0, i1);
+        else k_export<false, StoreF64><<<g, 128, 0, s>>>((const double*)P, L, t, rho, u, f, fibm, i0, i1);
+    } else if (L.prec == LIFE_PREC_F32) {
+        if (L.cm) k_export<true, StoreF32><<<g, 128, 0, s>>>((const float*)P, L, t, rho, u, f, fibm, i0, i1);
+        else k_export<false, StoreF32><<<g, 128, 0, s>>>((const float*)P, L, t, rho, u, f, fibm, i0, i1);
     } else {
-        LIFE_DISPATCH(k_export, const, P, L, t, rho, u, f, fibm);
+        if (L.cm) k_export<true, StoreF16><<<g, 128, 0, s>>>((const __half*)P, L, t, rho, u, f, fibm, i0, i1);
+        else k_export<false, StoreF16><<<g, 128, 0, s>>>((const __half*)P, L, t, rho, u, f, fibm, i0, i1);
     }
     return cudaGetLastError();
 }

@@ -18,8 +18,10 @@ cudaError_t launch_step_lowp(const void* A, void* B, const LatDev& L, int t, cud
 cudaError_t launch_outlet(const LatDev& L, double* delU, cudaStream_t s);
 cudaError_t launch_state(void* B, const LatDev& L, int t, const double* rho, const double* u, const double* f,
                          const double* fibm, cudaStream_t s);
+// Reference-layout export of columns i0 <= i < i1 (i1 < 0: all columns;
+// the initial-state export always covers the whole lattice).
 cudaError_t launch_export(const void* P, const LatDev& L, int t, bool initial, double* rho, double* u, double* f,
-                          double* fibm, cudaStream_t s);
+                          double* fibm, cudaStream_t s, int i0 = 0, int i1 = -1);
 cudaError_t launch_maxvel(const void* P, const LatDev& L, int t, unsigned long long* out, cudaStream_t s);
 
 // One case of a batched interior launch: its lattice view and buffers for the

@@ -604,30 +604,84 @@ extern "C" int life_case_get_fields(LifeCase* c, double* rho, double* u, double*
         if (force_ibm) std::memcpy(force_ibm, c->h_fibm.data(), n * 2 * sizeof(double));
         return LIFE_OK;
     }
+    // staging buffers on the device: from the memory pool, ordered on the
+    // case's stream (kernel, copies and release all run there), else cudaMalloc
     double *d_rho = nullptr, *d_u = nullptr, *d_f = nullptr, *d_fi = nullptr;
-    auto cleanup = [&]() {
-        cudaFree(d_rho);
-        cudaFree(d_u);
-        cudaFree(d_f);
-        cudaFree(d_fi);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    DevicePool* P = device_pool(dev);
+    const bool pooled = P && P->pooled;
+    auto get = [&](double** p, size_t count) {
+        return pooled ? cudaMallocAsync((void**)p, count * sizeof(double), c->stream)
+                      : cudaMalloc((void**)p, count * sizeof(double));
     };
-    if ((rho && cudaMalloc(&d_rho, n * sizeof(double)) != cudaSuccess) ||
-        (u && cudaMalloc(&d_u, n * 2 * sizeof(double)) != cudaSuccess) ||
-        (f && cudaMalloc(&d_f, n * 9 * sizeof(double)) != cudaSuccess) ||
-        (force_ibm && cudaMalloc(&d_fi, n * 2 * sizeof(double)) != cudaSuccess)) {
+    auto cleanup = [&]() {
+        for (double* p : {d_rho, d_u, d_f, d_fi})
+            if (p) {
+                if (pooled) cudaFreeAsync(p, c->stream);
+                else cudaFree(p);
+            }
+    };
+    if ((rho && get(&d_rho, n) != cudaSuccess) || (u && get(&d_u, n * 2) != cudaSuccess) ||
+        (f && get(&d_f, n * 9) != cudaSuccess) || (force_ibm && get(&d_fi, n * 2) != cudaSuccess)) {
         cleanup();
+        cudaStreamSynchronize(c->stream);
+        cudaGetLastError();
         return set_error(LIFE_ERR_NOMEM, "no device memory for the field export");
     }
     LatDev L = lattice_view(c, c->t);
     const bool initial = (c->t == c->t_set);
-    cudaError_t e = launch_export(c->P[c->cur ^ 1], L, c->t, initial, d_rho, d_u, d_f, d_fi, c->stream);
-    if (e == cudaSuccess && rho) e = cudaMemcpyAsync(rho, d_rho, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess && u) e = cudaMemcpyAsync(u, d_u, n * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess && f) e = cudaMemcpyAsync(f, d_f, n * 9 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess && force_ibm)
-        e = cudaMemcpyAsync(force_ibm, d_fi, n * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    // Large lattices export into page-locked host buffers in column chunks,
+    // each a contiguous range of the reference layout, so the copy of chunk k
+    // (on the side stream) runs beside the export kernel of chunk k+1 (on the
+    // case's stream). Copies to pageable memory block the host and would
+    // serialise the chunks, so those take one copy per field.
+    bool locked = true;
+    for (const double* h : {(const double*)rho, (const double*)u, (const double*)f, (const double*)force_ibm}) {
+        if (!h) continue;
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, h) != cudaSuccess || a.type != cudaMemoryTypeHost) locked = false;
+    }
+    cudaGetLastError();
+    const int chunks = (!initial && locked && n >= (1u << 20)) ? 8 : 1;
+    cudaEvent_t ev = nullptr;
+    cudaError_t e = chunks > 1 ? cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) : cudaSuccess;
+    for (int k = 0; k < chunks && e == cudaSuccess; k++) {
+        const int i0 = (int)((long long)c->Nx * k / chunks), i1 = (int)((long long)c->Nx * (k + 1) / chunks);
+        const size_t o = (size_t)i0 * c->Ny, m = (size_t)(i1 - i0) * c->Ny;
+        e = launch_export(c->P[c->cur ^ 1], L, c->t, initial, d_rho, d_u, d_f, d_fi, c->stream, i0,
+                          chunks > 1 ? i1 : -1);
+        cudaStream_t cs = c->stream;
+        if (chunks > 1) {
+            if (e == cudaSuccess) e = cudaEventRecord(ev, c->stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, ev, 0);
+            cs = c->side;
+        }
+        const size_t oo = chunks > 1 ? o : 0, mm = chunks > 1 ? m : n;
+        if (e == cudaSuccess && rho)
+            e = cudaMemcpyAsync(rho + oo, d_rho + oo, mm * sizeof(double), cudaMemcpyDeviceToHost, cs);
+        if (e == cudaSuccess && u)
+            e = cudaMemcpyAsync(u + 2 * oo, d_u + 2 * oo, mm * 2 * sizeof(double), cudaMemcpyDeviceToHost, cs);
+        if (e == cudaSuccess && f)
+            e = cudaMemcpyAsync(f + 9 * oo, d_f + 9 * oo, mm * 9 * sizeof(double), cudaMemcpyDeviceToHost, cs);
+        if (e == cudaSuccess && force_ibm)
+            e = cudaMemcpyAsync(force_ibm + 2 * oo, d_fi + 2 * oo, mm * 2 * sizeof(double), cudaMemcpyDeviceToHost, cs);
+    }
+    if (chunks > 1) {
+        // the staging buffers are released on the case's stream after the copies
+        const cudaError_t ew = ev ? cudaEventRecord(ev, c->side) : cudaSuccess;
+        if (ew == cudaSuccess) {
+            cudaStreamWaitEvent(c->stream, ev, 0);
+        } else {
+            cudaStreamSynchronize(c->side);
+            if (e == cudaSuccess) e = ew;
+        }
+    }
     cleanup();
+    const cudaError_t es = cudaStreamSynchronize(c->stream);
+    if (chunks > 1) cudaStreamSynchronize(c->side);
+    if (ev) cudaEventDestroy(ev);
+    if (e == cudaSuccess) e = es;
     if (e != cudaSuccess) return cuda_fail(e, "get_fields");
     return LIFE_OK;
 }
