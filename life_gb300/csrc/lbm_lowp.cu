@@ -87,8 +87,9 @@ __device__ __forceinline__ void collide_dev32(const float g[9], float dr, float 
         const float om1 = 1.0f - omega;
         const float k4 = om1 * fmaf(ux * ux - uy * uy, rho, fmaf(2.0f * uy, my, fmaf(-2.0f * ux, mx, dxxyy)));
         const float k5 = om1 * fmaf(ux * uy, rho, fmaf(-ux, my, fmaf(-uy, mx, gxy)));
-        const float k1 = 0.5f * Gx, k2 = 0.5f * Gy, k7 = Gx * (1.0f / 6.0f), k6 = Gy * (1.0f / 6.0f);
-        (void)k1; (void)k2; (void)k6; (void)k7;
+        // force moments (exact zeros, and unused, when not FORCED)
+        const float k1 = FORCED ? 0.5f * Gx : 0.0f, k2 = FORCED ? 0.5f * Gy : 0.0f;
+        const float k7 = FORCED ? Gx * (1.0f / 6.0f) : 0.0f, k6 = FORCED ? Gy * (1.0f / 6.0f) : 0.0f;
         float ex[3], wx[3], dx[3], ey[3], wy[3], dy[3];
         e1d(ux, ex, wx, dx);
         e1d(uy, ey, wy, dy);
