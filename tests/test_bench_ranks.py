@@ -4,6 +4,7 @@ reduction takes the maximum over ranks, and rank 0 alone prints the one JSON
 line. The reference arm runs here because it times the CPU oracle."""
 import json
 import os
+import re
 import socket
 import subprocess
 import sys
@@ -44,7 +45,8 @@ import bench
 world, rank, local = bench.dist_setup()
 bench.barrier(world)
 v = bench.max_over_ranks(world, float(rank + 1) * 10.0)
-print(f"rank {rank} max {v}", flush=True)
+sys.stdout.write(f"rank {rank} max {v}\n")  # one write: the ranks share the pipe
+sys.stdout.flush()
 import torch.distributed as dist
 dist.destroy_process_group()
 """
@@ -56,5 +58,5 @@ def test_max_over_ranks_gloo(tmp_path):
     os.environ["ROOT"] = ROOT
     res = _torchrun([str(script)], timeout=300)
     assert res.returncode == 0, res.stderr[-3000:]
-    got = sorted(ln for ln in res.stdout.splitlines() if ln.startswith("rank"))
-    assert got == ["rank 0 max 20.0", "rank 1 max 20.0"], res.stdout
+    got = sorted(re.findall(r"rank (\d+) max ([0-9.]+)", res.stdout))
+    assert got == [("0", "20.0"), ("1", "20.0")], res.stdout
