@@ -61,3 +61,38 @@ def test_parse_geometry_rejects_unknown_keyword(libpath):
     from life_gb300.lib import LifeError, parse_geometry
     with pytest.raises(LifeError):
         parse_geometry("SQUARE 1 0 0 0 0 0 1\n")
+
+
+C_CLIENT = r"""
+#include <stdio.h>
+#include "life_gb300.h"
+int main(void) {
+    LifeBodyDesc b[4];
+    int32_t n = 0;
+    const char* text = "# comment\nCIRCLE 1 0 20.0 20.0 0.0 0.0 5.0\n";
+    const int rc = life_parse_geometry(text, b, 4, &n);
+    printf("abi %d rc %d n %d\n", life_abi_version(), rc, (int)n);
+    return (life_abi_version() == 1 && rc == 0 && n == 1 && b[0].radius == 5.0) ? 0 : 1;
+}
+"""
+
+
+def test_header_is_plain_c(libpath, tmp_path):
+    """The public header compiles as strict C11 (no C++ in a C-ABI) and a C
+    program links against the library and calls it (host-only calls)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no gcc")
+    src = tmp_path / "client.c"
+    src.write_text(C_CLIENT)
+    exe = tmp_path / "client"
+    libdir = os.path.dirname(libpath)
+    res = subprocess.run([gcc, "-std=c11", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I",
+                          os.path.join(ROOT, "include"), str(src), "-L", libdir, "-llife_gb300",
+                          f"-Wl,-rpath,{libdir}", "-o", str(exe)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, run.stdout + run.stderr
+    assert "abi 1 rc 0 n 1" in run.stdout
