@@ -2,7 +2,8 @@
  * TEST INFRASTRUCTURE ONLY -- CPU oracle for the LIFE hot path (FP64).
  *
  * A restatement of the LIFE reference algorithm (joconnor22/LIFE v1.0.3) in
- * plain C, used only by tests/ and bench.py's CPU-baseline leg as the checker.
+ * plain C, used only by tests/ (as the oracle the CUDA path is compared with)
+ * and by bench.py's CPU-baseline leg.
  * Every floating-point expression keeps the reference's operation order
  * (and the build disables FMA contraction) so that lattice results agree with
  * the reference binary bit for bit; each function cites the reference code it
