@@ -37,26 +37,16 @@ WORKLOAD = "lid_driven_cavity_4096x4096_d2q9_bgk"
 
 
 def cavity_params(n: int, precision: int, cm: bool = False):
-    from life_gb300.case import VELOCITY, WALL, CaseParams
-    omega = 1.0 / 0.5768
-    cs = 1.0 / (3.0 ** 0.5)
-    nu = (1.0 / omega - 0.5) * (cs * cs)
-    return CaseParams(Nx=n, Ny=n, height_p=float(n - 1), rho_p=1.0, nu_p=nu, omega=omega,
-                      wall_left=WALL, wall_right=WALL, wall_bottom=WALL, wall_top=VELOCITY,
-                      uxInlet_p=0.1, central_moments=cm, precision=precision, ref_L=float(n - 1))
+    """The lid-driven cavity (BGK, lid 0.1, tau 0.5768) on an n x n lattice."""
+    from life_gb300 import configs
+    return configs.cavity(n, precision, cm)
 
 
 def cylinder_params(precision: int):
     """Rigid cylinder channel: 1000 x 400, central moments, D = 40, inlet 0.04,
     convective outlet, Re = 100 (tau = 0.548)."""
-    from life_gb300.case import CONVECTIVE, VELOCITY, WALL, CaseParams, Circle
-    omega = 1.0 / 0.548
-    cs = 1.0 / (3.0 ** 0.5)
-    nu = (1.0 / omega - 0.5) * (cs * cs)
-    p = CaseParams(Nx=1000, Ny=400, height_p=399.0, rho_p=1.0, nu_p=nu, omega=omega,
-                   wall_left=VELOCITY, wall_right=CONVECTIVE, wall_bottom=WALL, wall_top=WALL,
-                   uxInlet_p=0.04, central_moments=True, precision=precision, ref_L=40.0)
-    return p, [Circle(x=200.0, y=200.0, radius=20.0)]
+    from life_gb300 import configs
+    return configs.cylinder(precision)
 
 
 def filament_params(precision: int):
@@ -64,15 +54,8 @@ def filament_params(precision: int):
     one filament L = 80 clamped at (300, 200), 80 corotational elements,
     EI/(rho U^2 L^3) = 0.2 (E = 3072 with H = 1), mass ratio 0.5 (rho_s = 40),
     Re = 100 on L (tau = 0.62), initial tip deflection 0.03 L."""
-    from life_gb300.case import CONVECTIVE, VELOCITY, WALL, CaseParams, Filament
-    omega = 1.0 / 0.62
-    cs = 1.0 / (3.0 ** 0.5)
-    nu = (1.0 / omega - 0.5) * (cs * cs)
-    p = CaseParams(Nx=1200, Ny=400, height_p=399.0, rho_p=1.0, nu_p=nu, omega=omega,
-                   wall_left=VELOCITY, wall_right=CONVECTIVE, wall_bottom=WALL, wall_top=WALL,
-                   uxInlet_p=0.05, precision=precision, ref_L=80.0, initial_deflect=0.03, subTol=1e-8)
-    return p, [Filament(x=300.0, y=200.0, length=80.0, height=1.0, angle_deg=0.0, flexible=True,
-                        n_elements=80, clamped=True, rho=40.0, E=3072.0)]
+    from life_gb300 import configs
+    return configs.filament(precision)
 
 
 def _pinned_array(shape):
@@ -591,6 +574,56 @@ def serving_leg(n_requests: int = 24, step_scale: float = 0.02, seed: int = 7, l
     return out
 
 
+def fp64_block(args, n: int, world: int) -> dict:
+    """The FP64 form (the reference's arithmetic, bit for bit) on the same
+    lattice: device MLUPS, its interior kernel against the FP64 rate this GPU
+    sustains (the bound) and against HBM, and its own end-to-end figure
+    through the C-ABI (create, K steps, velocity field to host)."""
+    from life_gb300.case import PREC_F64
+    from life_gb300.lib import Case, measure_fp64_rate
+    sites = n * n
+    k = args.steps
+    c = Case(cavity_params(n, PREC_F64))
+    c.step(args.warmup)
+    c.sync()
+    tot, inner, launches = c.bench_steps(k)
+    del c
+    out = {"value": round(sites * k / (tot * 1e-3) / 1e6, 1), "unit": "MLUPS", "steps": k,
+           "ms_per_step": round(tot / k, 4), "kernel_ms": round(inner, 4), "gpu_launches": launches}
+    hbm, hbm_kind = peaks()
+    gbs = 144 * sites / (inner * 1e-3) / 1e9
+    out["hbm"] = {"achieved": round(gbs, 1), "peak": hbm, "unit": "GB/s", "frac": round(gbs / hbm, 4),
+                  "peak_source": f"{hbm_kind} hbm_gbs", "algorithmic_bytes_per_site": 144}
+    rate = measure_fp64_rate()
+    fl = None
+    fpath = os.path.join(ROOT, "profiles", "interior_f64_flops.json")
+    if os.path.exists(fpath):
+        with open(fpath) as fh:
+            fl = json.load(fh)
+    roof = {"bound": "fp64", "peak": round(rate, 1), "unit": "GFLOP/s",
+            "peak_source": "measured here: life_measure_fp64_rate (independent FMA chains, all SMs)",
+            "kernel": "k_interior_f64<BGK>"}
+    if fl:
+        per = float(fl["fp64_flops_per_site"])
+        ach = per * sites / (inner * 1e-3) / 1e9
+        roof.update({"achieved": round(ach, 1), "frac": round(ach / rate, 4), "fp64_flops_per_site": per,
+                     "flops_source": fl.get("source")})
+    out["roofline"] = roof
+    # end to end through the C-ABI, as the headline's e2e
+    u = _pinned_array((sites, 2))
+    t0 = time.perf_counter()
+    ce = Case(cavity_params(n, PREC_F64))
+    ce.step(k)
+    ce.fields(("u",), out={"u": u})
+    e2e_s = time.perf_counter() - t0
+    del ce, u
+    out["e2e"] = {"value": round(world * sites * k / e2e_s / 1e6, 1), "unit": "MLUPS",
+                  "h2d_bytes_per_step": round((376 + 16 * n + 32 * (k + 2)) / k),
+                  "d2h_bytes_per_step": round(sites * 16 / k),
+                  "what": "create from params + K steps + velocity field to host, wall clock"}
+    return out
+
+
 def run_gb300(args, world, rank, local):
     import numpy as np
     from life_gb300.build import build
@@ -623,6 +656,7 @@ def run_gb300(args, world, rank, local):
     achieved = bytes_per_site * sites / (inner_ms * 1e-3) / 1e9
 
     extras = {}
+    fp64 = fp64_block(args, n, world) if args.storage == "fp32" else None
     if not args.quick:
         # ---- FP64 (reference-exact) and FP16 storage on the same lattice
         k2 = max(10, args.steps // 2)
@@ -735,6 +769,7 @@ def run_gb300(args, world, rank, local):
                     "d2h_bytes_per_step": round(d2h / args.steps),
                     "what": "create from params + K steps + velocity field to host, wall clock"},
             "gpu_launches": launches,
+            "fp64": fp64,
             "clocks": clocks,
             "extras": extras,
         }

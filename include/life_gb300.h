@@ -45,10 +45,10 @@ enum {
     LIFE_ERR_BUSY = 10          /* serving queue full / slot not ready */
 };
 
-/* eLatType (reference inc/defs.h:163); LIFE_FLUID on a wall means periodic. */
+/* eLatType (reference inc/defs.h:51); LIFE_FLUID on a wall means periodic. */
 enum { LIFE_FLUID = 0, LIFE_WALL = 1, LIFE_VELOCITY = 2, LIFE_FREESLIP = 3,
        LIFE_PRESSURE = 4, LIFE_CONVECTIVE = 5 };
-/* eProfileType (reference inc/defs.h:164); UNIFORM = PROFILE undefined. */
+/* eProfileType (reference inc/defs.h:52); UNIFORM = PROFILE undefined. */
 enum { LIFE_PROFILE_UNIFORM = -1, LIFE_PROFILE_PARABOLIC = 0, LIFE_PROFILE_SHEAR = 1,
        LIFE_PROFILE_BOUNDARY_LAYER = 2 };
 /* Population storage/arithmetic form on the GPU. */
@@ -195,7 +195,11 @@ int life_ibm_epsilon(const double* pos, const int32_t* nsupp, const int32_t* si,
  * with LIFE_ERR_INVALID. All calls share that array, so calls that overlap on
  * the GPU race; the caller must order them. The first call on each device
  * looks up the array's device address, and should come before any stream
- * capture on that device. Same arguments and result as life_ibm_epsilon. */
+ * capture on that device; the address is kept until exit, so the library must
+ * not be used on a device across a cudaDeviceReset. Unlike life_ibm_epsilon
+ * the call does not wait: it queues the solve on `stream` and returns, and
+ * eps is ready once that stream reaches this point. Same arguments and result
+ * as life_ibm_epsilon. */
 int life_ibm_epsilon_noalloc(const double* pos, const int32_t* nsupp, const int32_t* si, const int32_t* sj,
                              const double* sd, const double* ds, int32_t n, double Dx, double* eps,
                              void* stream);
@@ -234,6 +238,26 @@ int life_case_get_fem0(LifeCase* c, int32_t k, double* node_pos0, double* node_a
  * src/Objects.cpp:518-528). */
 int life_case_max_velocity(LifeCase* c, double* max_vel, int32_t* has_nan);
 int life_case_total_force(LifeCase* c, double* fx, double* fy);
+
+/* Observables recorder: the rows ObjectsClass::writeTotalForces and
+ * ObjectsClass::writeTips append every tinfo steps (src/Objects.cpp:491-594,
+ * called from Utils::writeInfo, src/Utils.cpp:120-137), gathered on the device
+ * inside the step graph, with no host synchronisation per row.
+ * life_case_record(c, every, capacity) records a row for every step t with
+ * t % every == 0 (and one for the current state at once, as the reference
+ * writes one before its first step), into a device buffer of `capacity` rows;
+ * every <= 0 removes the recorder. A row holds Fx, Fy (the reference's total
+ * force: minus the sum over markers of force * 1.0 * eps * ds * forceScale, in
+ * marker order) and, for each flexible body in body order, the x, y, vx, vy
+ * of its last marker (the reference's tip). Call it between steps.
+ * life_case_records copies the rows recorded so far (oldest first) into
+ * t[n_rows] and rows[n_rows * n_cols], and empties the buffer; rows that found
+ * it full are counted in *dropped. Fails with LIFE_ERR_INVALID when more than
+ * max_rows rows are waiting. With t and rows both NULL it only reports
+ * n_rows, n_cols and dropped and leaves the rows in place. */
+int life_case_record(LifeCase* c, int32_t every, int32_t capacity);
+int life_case_records(LifeCase* c, int32_t max_rows, int32_t* n_rows, int32_t* n_cols, int32_t* t,
+                      double* rows, int32_t* dropped);
 
 /* Measurement hook (no counterpart in the reference, which only prints an
  * MLUPS figure from wall-clock time, src/Grid.cpp:594-610): runs nsteps steps
@@ -347,6 +371,12 @@ int life_server_destroy(LifeServer* s);
  * FEM band solve): compares it with IEEE division on n seeded random operand
  * pairs on the device and returns the number of results that differ. */
 int life_selftest_division(int64_t n, uint64_t seed, int64_t* mismatches);
+
+/* Measurement helper (no counterpart in the reference): the FP64 rate this
+ * GPU sustains on independent fused multiply-add chains, in GFLOP/s (an FMA
+ * counts two). It is the roofline denominator of the FP64 lattice kernels,
+ * which the SM's FP64 unit bounds. Runs on the current device and waits. */
+int life_measure_fp64_rate(double* gflops);
 
 /* Parses geometry.config text with the reference's rules (leading '#' lines
  * skipped, whitespace tokens; src/Objects.cpp:338-458). Writes at most cap

@@ -1,7 +1,7 @@
 /*
  * Stand-in for the reference's inc/defs.h when a LIFE params.h is compiled
  * against life_params_pack.h: a params.h starts with #include "defs.h" and
- * uses these enumerations and macros (reference inc/defs.h:146-171). The
+ * uses these constants, enumerations and macros (reference inc/defs.h:34-58). The
  * enumerator values are those of the reference, so WALL_* and PROFILE
  * settings map one to one onto LIFE_FLUID..LIFE_CONVECTIVE and
  * LIFE_PROFILE_*.

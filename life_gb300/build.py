@@ -3,9 +3,10 @@
 Every translation unit is compiled for sm_103a only, in parallel, and linked
 into one shared library that exports the C-ABI of ``include/life_gb300.h``.
 
-* FP64 device code that must reproduce the reference bit for bit is compiled
-  with ``--fmad=false`` (no a*b+c contraction, as g++ on x86-64 does).
-* Reduced-precision lattice kernels are compiled with FMA contraction on.
+* Every CUDA unit is compiled with ``--fmad=false`` (no a*b+c contraction, as
+  g++ on x86-64 does), so the FP64 code shared by all storage forms rounds
+  identically everywhere; the reduced-precision kernels spell out the fused
+  multiply-adds they want with ``fmaf``.
 * Host C++ is compiled with ``-ffp-contract=off`` so start-up arithmetic is
   identical on x86-64 and aarch64 hosts.
 
@@ -47,6 +48,8 @@ UNITS: List[Tuple[str, List[str]]] = [
     ("ibm_noalloc.cu", ["--fmad=false"]),
     ("batch.cu", ["--fmad=false"]),
     ("server.cu", ["--fmad=false"]),
+    ("observe.cu", ["--fmad=false"]),
+    ("measure.cu", ["--fmad=false"]),
     ("objects.cpp", []),
 ]
 

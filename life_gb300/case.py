@@ -25,10 +25,10 @@ import tempfile
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence, Union
 
-# eLatType (reference inc/defs.h:163). eFluid on a wall means periodic.
+# eLatType (reference inc/defs.h:51). eFluid on a wall means periodic.
 FLUID, WALL, VELOCITY, FREESLIP, PRESSURE, CONVECTIVE = range(6)
 LAT_NAMES = ["eFluid", "eWall", "eVelocity", "eFreeSlip", "ePressure", "eConvective"]
-# eProfileType (reference inc/defs.h:164); None = uniform inlet (PROFILE undefined).
+# eProfileType (reference inc/defs.h:52); None = uniform inlet (PROFILE undefined).
 PARABOLIC, SHEAR, BOUNDARY_LAYER = range(3)
 PROFILE_NAMES = ["eParabolic", "eShear", "eBoundaryLayer"]
 

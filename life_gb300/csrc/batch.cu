@@ -70,7 +70,7 @@ struct LifeBatch {
     // relative to (t_base, cur_base) of each case
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     int kernel_nodes[2] = {0, 0};
-    std::vector<int> t_base, cur_base;
+    std::vector<int> t_base, cur_base, rec_gen;
     std::vector<int> ring_end;  // step tables are valid for t < ring_end[k]
     std::string status_msg;
     int status_code = 0;
@@ -235,6 +235,7 @@ static int capture_step(LifeBatch* b, int phase, cudaGraphExec_t* out, int* kern
         if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_join, 0);
         if (e == cudaSuccess && c->obj.hasIBM) e = cudaStreamWaitEvent(c->stream, c->ev_aux, 0);
         if (e == cudaSuccess && c->obj.hasIBM) rc = ibm_apply(c, tt, A, B, c->stream);
+        if (e == cudaSuccess && rc == LIFE_OK) e = launch_record(c, tt, c->stream);
         if (c->stream != bs) {
             if (e == cudaSuccess && rc == LIFE_OK) e = cudaEventRecord(c->ev_done, c->stream);
             if (e == cudaSuccess && rc == LIFE_OK) e = cudaStreamWaitEvent(bs, c->ev_done, 0);
@@ -288,9 +289,11 @@ static int build_graphs(LifeBatch* b) {
     if (int rc = upload_case_table(b)) return rc;
     b->t_base.resize(n);
     b->cur_base.resize(n);
+    b->rec_gen.resize(n);
     for (int k = 0; k < n; k++) {
         b->t_base[k] = b->cases[k]->t;
         b->cur_base[k] = b->cases[k]->cur;
+        b->rec_gen[k] = b->cases[k]->rec_gen;
     }
     int rc = LIFE_OK;
     for (int p = 0; p < 2 && rc == LIFE_OK; p++) rc = capture_step(b, p, &b->exec[p], &b->kernel_nodes[p]);
@@ -316,6 +319,7 @@ static int graph_phase(LifeBatch* b) {
     int ph = -1;
     for (size_t k = 0; k < b->cases.size(); k++) {
         const LifeCase* c = b->cases[k];
+        if (c->rec_gen != b->rec_gen[k]) return -1;  // recorder set up or removed since the capture
         const int d = (c->t - b->t_base[k]) & 1;
         if ((c->cur ^ b->cur_base[k]) != d) return -1;
         if (ph < 0) ph = d;

@@ -17,7 +17,12 @@
 // names a host-side stand-in. The device address is fetched with
 // cudaGetSymbolAddress once per device, with that device current, by the first
 // call made on it; that first call should come before any stream capture on
-// the device.
+// the device. The address is kept for the life of the process, so the library
+// must not be used on a device across a cudaDeviceReset.
+//
+// The call is stream-ordered: it queues the kernel on the caller's stream and
+// returns without waiting. eps is ready once the caller's stream has reached
+// that point (cudaStreamSynchronize, an event, or later work on the stream).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -87,7 +92,6 @@ extern "C" int life_ibm_epsilon_noalloc(const double* pos, const int32_t* nsupp,
     cudaStream_t s = (cudaStream_t)stream;
     e = launch_epsilon_markers(M, n, Dx, reinterpret_cast<double*>(base), reinterpret_cast<double*>(base + kOffB),
                                reinterpret_cast<int*>(base + kOffPiv), reinterpret_cast<int*>(base + kOffLmax), s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "life_ibm_epsilon_noalloc");
     return LIFE_OK;
 }

@@ -253,6 +253,7 @@ static void free_case(LifeCase* c) {
     for (cudaStream_t s : {c->stream, c->side, c->aux})
         if (s) cudaStreamSynchronize(s);
     if (c->self_batch) batch_free(c->self_batch);
+    free_recorder(c);
     free_fem(c);
     case_dev_free_all(c);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
@@ -479,6 +480,11 @@ static int run_steps(LifeCase* c, int nsteps, StepTiming* tm) {
             int before = c->ibm_launches;
             if ((rc = ibm_step(c, tt, A, B))) return rc;
             if (tm) tm->launches += c->ibm_launches - before;
+        }
+        if (c->rec.every > 0) {
+            e = launch_record(c, tt, c->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "observables recorder");
+            if (tm) tm->launches++;
         }
         c->cur ^= 1;
         c->t = tt;

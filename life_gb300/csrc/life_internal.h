@@ -27,6 +27,18 @@ struct FsiScalars {
 
 struct FemHost;  // fem_host.cu
 
+// Device side of the observables recorder (observe.cu): `capacity` rows of
+// `cols` doubles (Fx, Fy, then x, y, vx, vy of each flexible body's last
+// marker) and their steps; count[0] rows written, count[1] rows dropped.
+struct RecorderDev {
+    int every = 0, capacity = 0, cols = 0, n_tips = 0;
+    double force_scale = 0.0;
+    double* rows = nullptr;
+    int* t = nullptr;
+    int* count = nullptr;
+    int* tip = nullptr;  // marker index of each flexible body's last marker
+};
+
 int set_error(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* where);
 // Device memory of a case, tracked in c->allocs and c->dev_bytes and
@@ -90,6 +102,10 @@ struct LifeCase {
     const int* t_dev = nullptr;
     int t_off = 0;
     int loop_body_kernels = 0;  // kernels in one pass of a captured FSI loop body
+    // observables recorder (life_case_record); rec_gen changes whenever the
+    // recorder is set up or removed, so captured step graphs are rebuilt
+    life::RecorderDev rec{};
+    int rec_gen = 0;
 };
 
 namespace life {
@@ -103,5 +119,9 @@ int case_interior_ms(LifeCase* c, int reps, float* ms);
 // Kernel nodes of one captured step of the case (0 before the first capture).
 int case_kernels_per_step(LifeCase* c);
 void free_fem(LifeCase* c);
+// The recorder's kernel for the step ending at t (a no-op without a recorder);
+// inside a capture the step is read from c->t_dev.
+cudaError_t launch_record(const LifeCase* c, int t, cudaStream_t s);
+void free_recorder(LifeCase* c);
 int ensure_steps(LifeCase* c, int t0, int n);
 }  // namespace life

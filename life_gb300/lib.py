@@ -51,6 +51,9 @@ SIGNATURES = {
     "life_selftest_division": (C.c_int, [C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
     "life_case_max_velocity": (C.c_int, [C.c_void_p, _dp, _ip]),
     "life_case_total_force": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "life_case_record": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "life_measure_fp64_rate": (C.c_int, [_dp]),
+    "life_case_records": (C.c_int, [C.c_void_p, C.c_int32, _ip, _ip, _ip, _dp, _ip]),
     "life_parse_geometry": (C.c_int, [C.c_char_p, C.c_void_p, C.c_int32, _ip]),
     "life_case_bench_steps": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _ip]),
     "life_case_get_support": (C.c_int, [C.c_void_p, _ip, _ip, _ip, _dp]),
@@ -272,6 +275,36 @@ class Case:
         fx, fy = C.c_double(), C.c_double()
         _check(lib().life_case_total_force(self._h, C.byref(fx), C.byref(fy)))
         return fx.value, fy.value
+
+    def record(self, every: int, capacity: int = 4096) -> None:
+        """Record the total force and the flexible bodies' tips every `every`
+        steps on the device (``life_case_record``); 0 removes the recorder."""
+        _check(lib().life_case_record(self._h, int(every), int(capacity)))
+
+    def records(self, max_rows: int = 1 << 20) -> Dict[str, np.ndarray]:
+        """Rows recorded since the last call (``life_case_records``): ``t``,
+        ``force`` [n, 2], ``tip_pos`` / ``tip_vel`` [n, bodies, 2], ``dropped``."""
+        n, cols, dropped = C.c_int32(), C.c_int32(), C.c_int32()
+        _check(lib().life_case_records(self._h, 0, C.byref(n), C.byref(cols), None, None, C.byref(dropped)))
+        max_rows = max(max_rows, n.value)
+        t = np.zeros(max(max_rows, 1), dtype=np.int32)
+        rows = np.zeros((max(max_rows, 1), max(cols.value, 1)))
+        _check(lib().life_case_records(self._h, int(max_rows), C.byref(n), C.byref(cols), _p(t), _p(rows),
+                                       C.byref(dropped)))
+        k, nc = n.value, cols.value
+        rows = rows[:k, :nc]
+        nb = (nc - 2) // 4
+        tips = rows[:, 2:].reshape(k, nb, 4) if nb else np.zeros((k, 0, 4))
+        return {"t": t[:k].copy(), "force": rows[:, :2].copy(), "tip_pos": tips[:, :, :2].copy(),
+                "tip_vel": tips[:, :, 2:].copy(), "dropped": dropped.value}
+
+
+def measure_fp64_rate() -> float:
+    """FP64 GFLOP/s this GPU sustains on independent FMA chains
+    (``life_measure_fp64_rate``)."""
+    g = C.c_double()
+    _check(lib().life_measure_fp64_rate(C.byref(g)))
+    return g.value
 
 
 class Batch:

@@ -11,8 +11,8 @@ For every case in ``cases.py`` this script
    ``IBM.restart``, ``FEM.restart`` -- full-precision binary doubles) as
    ``tests/golden/<case>.npz``.
 
-It needs the reference tree (default ``/root/reference``, override with
-``LIFE_REFERENCE``) and is run by hand when the case list changes:
+It needs the reference tree (``LIFE_REFERENCE``, else a checkout named
+``reference`` beside this repository) and is run by hand when the case list changes:
 
     python tests/golden/make_golden.py [case ...]
 """
@@ -36,7 +36,7 @@ from cases import golden_cases  # noqa: E402
 from life_gb300.case import geometry_config_text  # noqa: E402
 from life_gb300.restart import read_fem_restart, read_fluid_restart, read_ibm_restart  # noqa: E402
 
-REF = os.environ.get("LIFE_REFERENCE", "/root/reference")
+REF = os.environ.get("LIFE_REFERENCE") or os.path.join(os.path.dirname(REPO), "reference")
 
 
 def params_digest(text: str) -> str:
@@ -47,7 +47,7 @@ def array_digest(a) -> str:
     return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
 
 
-def run_case(name: str, params, bodies, work: str, lapack: str = "openblas") -> dict:
+def run_case(name: str, params, bodies, work: str, lapack: str = "openblas", threads: int = 1) -> dict:
     cdir = os.path.join(work, name + lapack, "case")
     rdir = os.path.join(work, name + lapack, "run")
     os.makedirs(cdir, exist_ok=True)
@@ -62,7 +62,7 @@ def run_case(name: str, params, bodies, work: str, lapack: str = "openblas") -> 
                     f"CASE={cdir}", f"NAME=golden_{name}_{lapack}", f"REF={REF}",
                     f"LAPACK={lapack}"], check=True)
     exe = os.path.join(REPO, "oracle", "_ref", f"golden_{name}_{lapack}", "LIFE")
-    env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1")
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS="1")
     log = subprocess.run([exe], cwd=rdir, env=env, capture_output=True, text=True)
     if log.returncode != 0:
         raise RuntimeError(f"{name}: reference exited {log.returncode}\n{log.stdout[-2000:]}")
@@ -87,9 +87,11 @@ def run_case(name: str, params, bodies, work: str, lapack: str = "openblas") -> 
             out["fem_" + key] = np.concatenate([getattr(b, key) for b in fe.bodies])
         out["fem_pos0"] = np.vstack([b.pos0 for b in fe.bodies])
         out["fem_pos"] = np.vstack([b.pos for b in fe.bodies])
-    forces = os.path.join(rdir, "Results", "TotalForces.out")
-    if os.path.exists(forces):
-        out["total_forces_text"] = open(forces).read()
+    for key, fname in (("total_forces_text", "TotalForces.out"), ("tip_positions_text", "TipPositions.out"),
+                       ("tip_velocities_text", "TipVelocities.out")):
+        path = os.path.join(rdir, "Results", fname)
+        if os.path.exists(path):
+            out[key] = open(path).read()
     return out
 
 

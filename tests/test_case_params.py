@@ -9,7 +9,8 @@ import pytest
 from cases import golden_cases
 from life_gb300.case import load_params_h
 
-REF = os.environ.get("LIFE_REFERENCE", "/root/reference")
+REF = os.environ.get("LIFE_REFERENCE") or os.path.join(
+    os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "reference")
 
 
 @pytest.mark.parametrize("name", sorted(golden_cases()))

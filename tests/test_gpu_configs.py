@@ -1,0 +1,160 @@
+"""The named single-case workloads at their full stated sizes, against the
+LIFE reference's own runs (tests/golden/make_configs.py), and the device
+observables recorder against the reference's text files.
+
+* 256 x 256 BGK cavity, 20,000 steps: the GPU FP64 fields are bit-identical
+  to the reference's Fluid.restart (SHA-256 of f, rho, u); the FP32 form's
+  velocity is within 1e-5 of it (relative to max |u|).
+* 1000 x 400 central-moments cylinder, 50,000 steps: the recorder's rows,
+  formatted as ObjectsClass::writeTotalForces writes them, are the
+  reference's TotalForces.out character for character (501 lines, every 100
+  steps), and the final lattice and marker state is bit-identical.
+* 1200 x 400 flexible filament, 2,000 steps: TipPositions.out,
+  TipVelocities.out and TotalForces.out (every 10 steps) agree with the
+  reference's to the tolerances below. The flexible-body path is not
+  bit-identical to the reference: the device evaluates atan2/sin/cos with
+  its own routines, which differ from the C library's in the last bit for
+  some arguments, and the coupling amplifies such differences (the
+  reference's own results move by ~1e-11 in the marker forces when one
+  trigonometric result in a thousand changes by one unit in the last place).
+* The six small body fixtures: the recorded total force at the last step
+  matches the reference's TotalForces.out line to its 10 printed digits.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from cases import golden_cases
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from life_gb300.build import build
+    build()
+
+
+def test_config1_cavity256_fp64_bit_exact_after_20000_steps():
+    from life_gb300 import configs
+    from life_gb300.lib import Case
+    g = np.load(os.path.join(GOLD, "config1_cavity256.npz"))
+    p = configs.cavity(256, steps=20000)
+    with Case(p) as c:
+        c.step(20000)
+        assert c.t == int(g["t"]) == 20000
+        fl = c.fields(("rho", "u", "f"))
+    for key in ("f", "rho", "u"):
+        assert digest(fl[key]) == str(g["sha_" + key]), key
+    assert float(np.abs(fl["u"]).max()) == float(g["u_max"])
+
+
+def test_config1_cavity256_fp32_velocity_error():
+    from life_gb300 import configs
+    from life_gb300.case import PREC_F32
+    from life_gb300.lib import Case
+    g = np.load(os.path.join(GOLD, "config1_cavity256.npz"))
+    p = configs.cavity(256, precision=PREC_F32, steps=20000)
+    with Case(p) as c:
+        c.step(20000)
+        u = c.fields(("u",))["u"].reshape(256, 256, 2)[::8, ::8]
+    err = float(np.abs(u - g["u_sub"]).max() / float(g["u_max"]))
+    print(f"config1 FP32 velocity max error / max|u| after 20000 steps: {err:.3e}")
+    assert err <= 1e-5
+
+
+def _records_text(c, p):
+    from life_gb300.observables import tips_text, total_forces_text
+    rec = c.records()
+    assert rec["dropped"] == 0
+    Dt = c.info().Dt
+    return rec, total_forces_text(p, Dt, rec), tips_text(Dt, rec, "tip_pos"), tips_text(Dt, rec, "tip_vel")
+
+
+def test_config2_cylinder_total_forces_text_identical_over_50000_steps():
+    from life_gb300 import configs
+    from life_gb300.lib import Case
+    g = np.load(os.path.join(GOLD, "config2_cylinder.npz"))
+    p, b = configs.cylinder(steps=50000, tinfo=100)
+    with Case(p, b) as c:
+        c.record(100, capacity=1024)
+        c.step(50000)
+        rec, forces, _, _ = _records_text(c, p)
+        fl, mk = c.fields(), c.markers()
+    assert len(rec["t"]) == 501 and rec["t"][-1] == 50000
+    ref = str(g["total_forces_text"])
+    assert forces == ref, next((a, b) for a, b in zip(forces.split("\n"), ref.split("\n")) if a != b)
+    got = dict(f=fl["f"], rho=fl["rho"], u=fl["u"], force_ibm=fl["force_ibm"], ibm_pos=mk["pos"],
+               ibm_vel=mk["vel"], ibm_force=mk["force"])
+    for key, arr in got.items():
+        assert digest(arr) == str(g["sha_" + key]), key
+
+
+def test_config3_filament_tips_and_forces_over_2000_steps():
+    from life_gb300 import configs
+    from life_gb300.lib import Case
+    from life_gb300.observables import parse_table
+    g = np.load(os.path.join(GOLD, "config3_filament.npz"))
+    p, b = configs.filament(steps=2000, tinfo=10)
+    with Case(p, b) as c:
+        c.record(10, capacity=1024)
+        c.step(2000)
+        rec, forces, tpos, tvel = _records_text(c, p)
+        mk, fm = c.markers(), c.fem(0)
+    assert len(rec["t"]) == 201 and rec["t"][-1] == 2000
+    errs = {}
+    for name, got, key in (("tip_pos", tpos, "tip_positions_text"), ("tip_vel", tvel, "tip_velocities_text"),
+                           ("force", forces, "total_forces_text")):
+        a, r = parse_table(got), parse_table(str(g[key]))
+        assert a.shape == r.shape
+        assert np.array_equal(a[:, 0], r[:, 0])
+        # per column, relative to the column's largest magnitude
+        scale = np.abs(r[:, 2:]).max(axis=0)
+        errs[name] = float((np.abs(a[:, 2:] - r[:, 2:]) / scale).max())
+    # full-precision final state
+    errs["fem_pos"] = float(np.abs(fm["pos"] - g["fem_pos"]).max() / np.abs(g["fem_pos"]).max())
+    errs["fem_U"] = float(np.abs(fm["U"] - g["fem_U"]).max() / np.abs(g["fem_U"]).max())
+    errs["marker_pos"] = float(np.abs(mk["pos"] - g["ibm_pos"]).max() / np.abs(g["ibm_pos"]).max())
+    errs["marker_force"] = float(np.abs(mk["force"] - g["ibm_force"]).max() / np.abs(g["ibm_force"]).max())
+    print("config3 GPU FP64 vs reference:", {k: f"{v:.2e}" for k, v in errs.items()})
+    # tip positions print 10 significant digits (1e-7 at x ~ 380): the text
+    # agrees to its last printed digit; FEM node positions to 1e-12
+    assert errs["tip_pos"] <= 2e-10
+    assert errs["fem_pos"] <= 1e-12 and errs["marker_pos"] <= 1e-12
+    assert errs["fem_U"] <= 1e-9
+    assert errs["tip_vel"] <= 1e-8 and errs["force"] <= 1e-8
+    assert errs["marker_force"] <= 1e-8
+
+
+BODY_CASES = [k for k, (_, b) in golden_cases().items() if b]
+
+
+@pytest.mark.parametrize("name", BODY_CASES)
+def test_recorded_total_force_matches_reference_text(name):
+    from life_gb300.lib import Case
+    from life_gb300.observables import parse_table
+    p, b = golden_cases()[name]
+    g = np.load(os.path.join(GOLD, f"{name}.npz"))
+    with Case(p, b) as c:
+        c.record(p.nSteps, capacity=8)
+        c.step(p.nSteps)
+        rec, forces, _, _ = _records_text(c, p)
+        fx, fy = c.total_force()
+    a, r = parse_table(forces), parse_table(str(g["total_forces_text"]))
+    assert a.shape == r.shape == (2, 6)
+    assert np.array_equal(a[:, :2], r[:, :2])
+    # the reference prints 10 significant digits; its LAPACK (OpenBLAS) and
+    # the device's textbook LU round differently, so allow one printed unit
+    tol = 1e-9 * np.abs(r[:, 2:])
+    assert np.all(np.abs(a[:, 2:] - r[:, 2:]) <= tol), (a, r)
+    # the device recorder and the host-side sum of life_case_total_force
+    # agree bit for bit
+    assert rec["force"][-1, 0] == fx and rec["force"][-1, 1] == fy
