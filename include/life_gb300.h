@@ -372,6 +372,11 @@ int life_server_destroy(LifeServer* s);
  * pairs on the device and returns the number of results that differ. */
 int life_selftest_division(int64_t n, uint64_t seed, int64_t* mismatches);
 
+/* Self-test of the device's correctly rounded trigonometry (the FEM element
+ * angle and rotation): evaluates op 0 = sin(x), 1 = cos(x), 2 = atan2(y, x)
+ * on the device for n host operands and writes the results to out[n]. */
+int life_selftest_trig(int32_t op, int64_t n, const double* x, const double* y, double* out);
+
 /* Measurement helper (no counterpart in the reference): the FP64 rate this
  * GPU sustains on independent fused multiply-add chains, in GFLOP/s (an FMA
  * counts two). It is the roofline denominator of the FP64 lattice kernels,

@@ -23,6 +23,7 @@
 #include <atomic>
 
 #include "band_lu.h"
+#include "crtrig.h"
 #include "fem_kernels.h"
 
 namespace life {
@@ -98,14 +99,18 @@ __device__ void update_fem_values(FemBodyDev& B) {
         const double* n1 = B.node + (e + 1) * 6;
         const double ev0 = n1[2] - n0[2], ev1 = n1[3] - n0[3];
         double* el = B.el + (size_t)e * EL_STRIDE;
-        const double ang = atan2(ev1, ev0);
+        // correctly rounded trigonometry (crtrig.h): the same bits on every
+        // device and on a host checker
+        const double ang = life_cr_atan2(ev1, ev0);
         double dd = 0.0;
         dd += ev0 * ev0;
         dd += ev1 * ev1;
         el[EL_ANG] = ang;
         el[EL_L] = sqrt(dd);
-        el[EL_COS] = cos(ang);
-        el[EL_SIN] = sin(ang);
+        double sa, ca;
+        life_cr_sincos(ang, &sa, &ca);
+        el[EL_COS] = ca;
+        el[EL_SIN] = sa;
     }
     __syncthreads();
 }
@@ -1346,8 +1351,10 @@ __global__ void k_fem_element_trig(double* el, int nEl) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nEl) return;
     const double ang = el[(size_t)e * EL_STRIDE + EL_ANG];
-    el[(size_t)e * EL_STRIDE + EL_COS] = cos(ang);
-    el[(size_t)e * EL_STRIDE + EL_SIN] = sin(ang);
+    double sa, ca;
+    life_cr_sincos(ang, &sa, &ca);
+    el[(size_t)e * EL_STRIDE + EL_COS] = ca;
+    el[(size_t)e * EL_STRIDE + EL_SIN] = sa;
 }
 
 cudaError_t launch_fem_element_trig(double* el, int nEl, cudaStream_t s) {
@@ -1465,6 +1472,42 @@ cudaError_t launch_fsi_subiteration(const FsiDev& F, const MarkerDev& M, const v
 }
 
 }  // namespace life
+
+namespace {
+__global__ void k_selftest_trig(int op, long long n, const double* x, const double* y, double* out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double s, c;
+        if (op == 2) {
+            out[i] = life_cr_atan2(y[i], x[i]);
+        } else {
+            life_cr_sincos(x[i], &s, &c);
+            out[i] = op == 0 ? s : c;
+        }
+    }
+}
+}  // namespace
+
+extern "C" int life_selftest_trig(int32_t op, int64_t n, const double* x, const double* y, double* out) {
+    if (op < 0 || op > 2 || n <= 0 || !x || !out || (op == 2 && !y))
+        return life::set_error(LIFE_ERR_INVALID, "bad arguments");
+    double *dx = nullptr, *dy = nullptr, *dout = nullptr;
+    const size_t bytes = sizeof(double) * (size_t)n;
+    cudaError_t e = cudaMalloc(&dx, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&dout, bytes);
+    if (e == cudaSuccess && op == 2) e = cudaMalloc(&dy, bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && op == 2) e = cudaMemcpy(dy, y, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_selftest_trig<<<152 * 4, 256>>>(op, (long long)n, dx, dy, dout);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(dx);
+    cudaFree(dy);
+    cudaFree(dout);
+    if (e != cudaSuccess) return life::cuda_fail(e, "life_selftest_trig");
+    return LIFE_OK;
+}
 
 extern "C" int life_selftest_division(int64_t n, uint64_t seed, int64_t* mismatches) {
     if (n <= 0 || !mismatches) return life::set_error(LIFE_ERR_INVALID, "bad arguments");

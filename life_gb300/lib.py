@@ -53,6 +53,7 @@ SIGNATURES = {
     "life_case_total_force": (C.c_int, [C.c_void_p, _dp, _dp]),
     "life_case_record": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "life_measure_fp64_rate": (C.c_int, [_dp]),
+    "life_selftest_trig": (C.c_int, [C.c_int32, C.c_int64, _dp, _dp, _dp]),
     "life_case_records": (C.c_int, [C.c_void_p, C.c_int32, _ip, _ip, _ip, _dp, _ip]),
     "life_parse_geometry": (C.c_int, [C.c_char_p, C.c_void_p, C.c_int32, _ip]),
     "life_case_bench_steps": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp, _ip]),

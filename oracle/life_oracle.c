@@ -27,6 +27,28 @@
 #define M_PI 3.14159265358979323846
 #endif
 
+/* Trigonometry of the per-step element update (element angle and rotation).
+ * The default build calls the C library, as the reference does. Built with
+ * -DLIFE_ORACLE_CR_TRIG (liblife_oracle_cr.so) it calls the correctly rounded
+ * routines the GPU uses instead (life_gb300/csrc/crtrig.h, checked against
+ * 300-bit arithmetic by tests/test_crtrig.py), so the device's remaining
+ * arithmetic can be compared with this restatement bit for bit. Start-up
+ * (the static pre-deflection, body construction) always uses the C library,
+ * as the GPU path's host start-up does. */
+#ifdef LIFE_ORACLE_CR_TRIG
+#include "crtrig.h"
+static double step_atan2(double y, double x) { return life_cr_atan2(y, x); }
+static double step_sin(double x) { return life_cr_sin(x); }
+static double step_cos(double x) { return life_cr_cos(x); }
+double oracle_cr_sin(double x) { return life_cr_sin(x); }
+double oracle_cr_cos(double x) { return life_cr_cos(x); }
+double oracle_cr_atan2(double y, double x) { return life_cr_atan2(y, x); }
+#else
+static double step_atan2(double y, double x) { return atan2(y, x); }
+static double step_sin(double x) { return sin(x); }
+static double step_cos(double x) { return cos(x); }
+#endif
+
 #define NV 9
 #define SUPP 9
 
@@ -725,10 +747,12 @@ static void mat6_vec(double r[6], const double A[6][6], const double v[6]) {
 }
 
 /* FEMElementClass::setElementTransform (src/FEMElement.cpp:255-262) */
-static void el_transform(Element* e) {
-    e->T[0][0] = e->T[1][1] = e->T[3][3] = e->T[4][4] = cos(e->angle);
-    e->T[0][1] = e->T[3][4] = sin(e->angle);
-    e->T[1][0] = e->T[4][3] = -sin(e->angle);
+static void el_transform(Element* e, int in_step) {
+    const double ca = in_step ? step_cos(e->angle) : cos(e->angle);
+    const double sa = in_step ? step_sin(e->angle) : sin(e->angle);
+    e->T[0][0] = e->T[1][1] = e->T[3][3] = e->T[4][4] = ca;
+    e->T[0][1] = e->T[3][4] = sa;
+    e->T[1][0] = e->T[4][3] = -sa;
     e->T[2][2] = e->T[5][5] = 1.0;
 }
 
@@ -783,7 +807,7 @@ static void assemble_mat(const Element* e, const double loc[6][6], double* glob,
 }
 
 /* FEMBodyClass::updateFEMValues (src/FEMBody.cpp:198-223) */
-static void fem_update_values(FemBody* fb) {
+static void fem_update_values(FemBody* fb, int in_step) {
     for (int n = 0; n < fb->nNodes; n++) {
         for (int d = 0; d < 2; d++) fb->pos[n][d] = fb->pos0[n][d] + fb->U[n * 3 + d];
         fb->anglen[n] = fb->angle0n[n] + fb->U[n * 3 + 2];
@@ -792,9 +816,9 @@ static void fem_update_values(FemBody* fb) {
         Element* e = &fb->el[k];
         double ev[2] = {fb->pos[e->node[1]][0] - fb->pos[e->node[0]][0],
                         fb->pos[e->node[1]][1] - fb->pos[e->node[0]][1]};
-        e->angle = atan2(ev[1], ev[0]);
+        e->angle = in_step ? step_atan2(ev[1], ev[0]) : atan2(ev[1], ev[0]);
         e->L = sqrt(dot(ev, ev, 2));
-        el_transform(e);
+        el_transform(e, in_step);
     }
 }
 
@@ -973,7 +997,7 @@ static int fem_nr_dynamic(OracleCase* c, FemBody* fb) {
     int rc = oracle_solve(n, fb->K, fb->F, fb->bcDOFs, fb->delU);
     if (rc) return rc;
     for (int i = 0; i < n; i++) fb->U[i] = fb->U[i] + fb->delU[i];
-    fem_update_values(fb);
+    fem_update_values(fb, 1);
     return LIFE_OK;
 }
 
@@ -988,7 +1012,7 @@ static int fem_dynamic(OracleCase* c, Body* b) {
     memcpy(fb->U, fb->U_n, sizeof(double) * n);
     memcpy(fb->Udot, fb->Udot_n, sizeof(double) * n);
     memcpy(fb->Udotdot, fb->Udotdot_n, sizeof(double) * n);
-    fem_update_values(fb);
+    fem_update_values(fb, 1);
     memset(fb->R, 0, sizeof(double) * n);
     for (int k = 0; k < fb->nEl; k++) el_load(c, b, fb, &fb->el[k]);
     fb->itNR = 0;
@@ -1027,7 +1051,7 @@ static void fem_predictor(OracleCase* c, Body* b) {
         for (int i = 0; i < n; i++) fb->U[i] = 2.0 * fb->U_n[i] - fb->U_nm1[i];
     else if (c->t == 1)
         memcpy(fb->U, fb->U_n, sizeof(double) * n);
-    fem_update_values(fb);
+    fem_update_values(fb, 1);
     fem_finish_newmark(c, fb);
     fem_update_ibm(c, b);
     SWAPP(fb->U_km1, fb->U);
@@ -1067,7 +1091,7 @@ static int fem_initial_deflection(OracleCase* c, Body* b) {
             int rc = oracle_solve(n, fb->K, rhs, fb->bcDOFs, fb->delU);
             if (rc) { free(rhs); return rc; }
             for (int i = 0; i < n; i++) fb->U[i] = fb->U[i] + fb->delU[i];
-            fem_update_values(fb);
+            fem_update_values(fb, 0);
             fb->resNR = nr_residual(c, fb);
             fb->itNR++;
         } while (fb->resNR > TOL && fb->itNR < 20);
@@ -1132,7 +1156,7 @@ static int recompute_object_vals(OracleCase* c) {
                 FemBody* fb = c->b[ib].fem;
                 for (int i = 0; i < fb->bodyDOFs; i++)
                     fb->U[i] = fb->U_km1[i] + c->relax * (fb->U[i] - fb->U_km1[i]);
-                fem_update_values(fb);
+                fem_update_values(fb, 1);
                 fem_finish_newmark(c, fb);
                 fem_update_ibm(c, &c->b[ib]);
                 SWAPP(fb->U_km1, fb->U);
@@ -1286,7 +1310,7 @@ static FemBody* build_fem(OracleCase* c, const double pos[2], const LifeBodyDesc
         e->node[1] = i + 1;
         for (int a = 0; a < 2; a++)
             for (int k = 0; k < 3; k++) e->DOFs[a * 3 + k] = (i + a) * 3 + k;
-        el_transform(e);
+        el_transform(e, 0);
         el_local(e);
     }
     fem_node_mapping(fb, nIBM, fb->nNodes);

@@ -19,7 +19,8 @@ from life_gb300.case import CaseParams
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liblife_oracle.so")
-_lib = None
+CR_LIB_PATH = os.path.join(HERE, "_build", "liblife_oracle_cr.so")
+_libs: Dict[str, C.CDLL] = {}
 _lock = threading.Lock()
 
 
@@ -28,13 +29,16 @@ def build() -> str:
     return LIB_PATH
 
 
-def lib() -> C.CDLL:
-    global _lib
+def lib(trig: str = "libm") -> C.CDLL:
+    """The oracle library. trig="libm" is the restatement pinned to the
+    reference (C library trigonometry); trig="cr" is the same restatement
+    with the GPU's correctly rounded per-step trigonometry."""
     with _lock:
-        if _lib is None:
-            if not os.path.exists(LIB_PATH):
+        if trig not in _libs:
+            path = LIB_PATH if trig == "libm" else CR_LIB_PATH
+            if not os.path.exists(path):
                 build()
-            L = C.CDLL(LIB_PATH)
+            L = C.CDLL(path)
             dp = C.POINTER(C.c_double)
             ip = C.POINTER(C.c_int)
             L.oracle_last_error.restype = C.c_char_p
@@ -52,8 +56,14 @@ def lib() -> C.CDLL:
             L.oracle_get_relax.argtypes = [C.c_void_p, dp, ip, dp]
             L.oracle_solve.argtypes = [C.c_int, dp, dp, C.c_int, dp]
             L.oracle_get_nr.argtypes = [C.c_void_p, C.c_int, ip, dp]
-            _lib = L
-    return _lib
+            if trig == "cr":
+                for name in ("oracle_cr_sin", "oracle_cr_cos"):
+                    getattr(L, name).argtypes = [C.c_double]
+                    getattr(L, name).restype = C.c_double
+                L.oracle_cr_atan2.argtypes = [C.c_double, C.c_double]
+                L.oracle_cr_atan2.restype = C.c_double
+            _libs[trig] = L
+    return _libs[trig]
 
 
 def _dp(a: Optional[np.ndarray]):
@@ -77,8 +87,8 @@ class OracleError(RuntimeError):
 class Oracle:
     """A LIFE case run by the CPU oracle (reference layout, FP64)."""
 
-    def __init__(self, params: CaseParams, bodies: Sequence = ()):
-        L = lib()
+    def __init__(self, params: CaseParams, bodies: Sequence = (), trig: str = "libm"):
+        self._L = L = lib(trig)
         self.params = params
         ps = params_struct(params)
         bs = body_structs(bodies)
@@ -93,43 +103,43 @@ class Oracle:
 
     def close(self) -> None:
         if getattr(self, "_h", None):
-            lib().oracle_destroy(self._h)
+            self._L.oracle_destroy(self._h)
             self._h = None
 
     __del__ = close
 
     @property
     def t(self) -> int:
-        return lib().oracle_time(self._h)
+        return self._L.oracle_time(self._h)
 
     def step(self, n: int = 1) -> None:
-        rc = lib().oracle_step(self._h, int(n))
+        rc = self._L.oracle_step(self._h, int(n))
         if rc:
-            raise OracleError(rc, lib().oracle_last_error().decode())
+            raise OracleError(rc, self._L.oracle_last_error().decode())
 
     def fields(self) -> Dict[str, np.ndarray]:
         n = self.params.Nx * self.params.Ny
         rho, u = np.empty(n), np.empty((n, 2))
         f, fibm = np.empty((n, 9)), np.empty((n, 2))
-        lib().oracle_get_fields(self._h, _dp(rho), _dp(u), _dp(f), _dp(fibm))
+        self._L.oracle_get_fields(self._h, _dp(rho), _dp(u), _dp(f), _dp(fibm))
         return dict(rho=rho, u=u, f=f, force_ibm=fibm)
 
     def set_fields(self, t: int, rho, u, f, force_ibm) -> None:
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (rho, u, f, force_ibm)]
-        lib().oracle_set_fields(self._h, int(t), *[_dp(a) for a in arrs])
+        self._L.oracle_set_fields(self._h, int(t), *[_dp(a) for a in arrs])
 
     def markers(self) -> Dict[str, np.ndarray]:
         n = self.n_markers
         pos, vel, force = np.empty((n, 2)), np.empty((n, 2)), np.empty((n, 2))
         eps, ds = np.empty(n), np.empty(n)
         bidx = np.empty(n, dtype=np.int32)
-        lib().oracle_get_markers(self._h, _dp(pos), _dp(vel), _dp(force), _dp(eps), _dp(ds), _ip(bidx))
+        self._L.oracle_get_markers(self._h, _dp(pos), _dp(vel), _dp(force), _dp(eps), _dp(ds), _ip(bidx))
         return dict(pos=pos, vel=vel, force=force, epsilon=eps, ds=ds, body=bidx)
 
     def bodies(self) -> Dict[str, np.ndarray]:
         nb = self.n_bodies
         out = {k: np.empty(nb, dtype=np.int32) for k in ("ids", "flexible", "n_markers", "n_fem_nodes")}
-        lib().oracle_get_bodies(self._h, *[_ip(out[k]) for k in ("ids", "flexible", "n_markers", "n_fem_nodes")])
+        self._L.oracle_get_bodies(self._h, *[_ip(out[k]) for k in ("ids", "flexible", "n_markers", "n_fem_nodes")])
         return out
 
     def fem(self, k: int) -> Dict[str, np.ndarray]:
@@ -139,20 +149,20 @@ class Oracle:
         out = {key: np.empty(dofs) for key in keys}
         out["el_L"], out["el_angle"] = np.empty(nn - 1), np.empty(nn - 1)
         out["pos"], out["angle"] = np.empty((nn, 2)), np.empty(nn)
-        rc = lib().oracle_get_fem(self._h, k, *[_dp(out[key]) for key in keys], _dp(out["el_L"]),
+        rc = self._L.oracle_get_fem(self._h, k, *[_dp(out[key]) for key in keys], _dp(out["el_L"]),
                                   _dp(out["el_angle"]), _dp(out["pos"]), _dp(out["angle"]))
         if rc:
-            raise OracleError(rc, lib().oracle_last_error().decode())
+            raise OracleError(rc, self._L.oracle_last_error().decode())
         return out
 
     def nr(self, k: int = 0):
         it, res = C.c_int(), C.c_double()
-        lib().oracle_get_nr(self._h, k, C.byref(it), C.byref(res))
+        self._L.oracle_get_nr(self._h, k, C.byref(it), C.byref(res))
         return it.value, res.value
 
     def relax(self):
         r, s, res = C.c_double(), C.c_int(), C.c_double()
-        lib().oracle_get_relax(self._h, C.byref(r), C.byref(s), C.byref(res))
+        self._L.oracle_get_relax(self._h, C.byref(r), C.byref(s), C.byref(res))
         return r.value, s.value, res.value
 
 

@@ -1,15 +1,25 @@
 """Flexible bodies (corotational FEM + Newmark + Aitken FSI) on the GPU.
 
 Start-up (static pre-deflection, support, ds, epsilon) runs on the host with
-the textbook-order LU and must equal the oracle bit for bit. Time stepping
-runs the FEM on the device in FP64; its trigonometric functions (atan2, sin,
-cos) are CUDA's, which can differ from the C library's in the last bit, and
-the Aitken factor (a ratio of differences of successive iterates) magnifies
-such differences, so parity after N steps is a tolerance:
-  lattice fields  <= 1e-11 relative, IBM forces <= 1e-9 relative,
-  marker / FEM node positions <= 1e-11 absolute (lattice units).
-(measured worst cases on these fixtures: 2.3e-12, 2.1e-11, well below 1e-12).
-The reference's own dumps (OpenBLAS LU) are held to the same bounds.
+the textbook-order LU and must equal the oracle bit for bit.
+
+Time stepping runs the FEM on the device in FP64. Its element angles and
+rotations use correctly rounded atan2/sin/cos (crtrig.h). The oracle built
+with the same routines (trig="cr") must then equal the GPU bit for bit after
+N steps: every other operation of the flexible-body path is the reference's,
+in the reference's order.
+
+Against the reference's own arithmetic (the C library's trigonometry: the
+default oracle, pinned to the textbook-LAPACK reference build, and the
+reference's OpenBLAS dumps) the run is a tolerance. The C library's results
+are not all correctly rounded (about one in a thousand sin/cos/atan2 results
+on [-pi, pi] is one unit in the last place away), and the coupling amplifies
+such differences: in the oracle alone, changing one trigonometric result in a
+thousand by one unit moves the marker forces by ~1e-11 relative, the lattice
+velocity by ~1e-12 and node positions by ~1e-16. The bounds asserted:
+  populations <= 1e-12, velocity and density <= 1e-11 (relative to max),
+  marker and FEM node positions <= 1e-12 (relative to max),
+  IBM and marker forces <= 1e-9 (relative to max).
 """
 import os
 
@@ -51,6 +61,28 @@ def test_startup_state_bit_exact(name):
 
 
 @pytest.mark.parametrize("name", FLEX)
+def test_fsi_run_bit_exact_vs_oracle_with_same_trigonometry(name):
+    from life_gb300.lib import Case
+    from oracle.pyoracle import Oracle
+    p, b = CASES[name]
+    o = Oracle(p, b, trig="cr")
+    o.step(p.nSteps)
+    with Case(p, b) as c:
+        c.step(p.nSteps)
+        fl, mk = c.fields(), c.markers()
+        fem = [c.fem(k) for k in range(c.n_flex)]
+    fo, mo = o.fields(), o.markers()
+    for key in ("f", "rho", "u", "force_ibm"):
+        assert np.array_equal(fl[key], fo[key]), (key, rel(fl[key], fo[key]))
+    for key in ("pos", "vel", "force", "epsilon", "ds"):
+        assert np.array_equal(mk[key], mo[key]), (key, rel(mk[key], mo[key]))
+    for k in range(len(fem)):
+        fk = o.fem(k)
+        for key in ("U", "Udot", "Udotdot", "pos", "el_angle"):
+            assert np.array_equal(fem[k][key], fk[key]), (k, key, rel(fem[k][key], fk[key]))
+
+
+@pytest.mark.parametrize("name", FLEX)
 def test_fsi_run_matches_oracle_and_reference(name):
     from life_gb300.lib import Case
     from oracle.pyoracle import Oracle
@@ -66,20 +98,19 @@ def test_fsi_run_matches_oracle_and_reference(name):
     fo, mo = o.fields(), o.markers()
     femo = [o.fem(k) for k in range(o.n_flex)]
     report = {}
-    for ref_name, F, Mk, FE in (("oracle", fo, mo, femo),
-                                ("reference", g, {"force": g["ibm_force"], "pos": g["ibm_pos"]}, None)):
-        for key in ("f", "rho", "u"):
+    for ref_name, F, Mk in (("oracle", fo, mo), ("reference", g, {"force": g["ibm_force"], "pos": g["ibm_pos"]})):
+        for key, bound in (("f", 1e-12), ("rho", 1e-11), ("u", 1e-11), ("force_ibm", 1e-9)):
             report[(ref_name, key)] = rel(fl[key], F[key])
-            assert report[(ref_name, key)] < 1e-11, (ref_name, key, report[(ref_name, key)])
-        report[(ref_name, "force_ibm")] = rel(fl["force_ibm"], F["force_ibm"])
-        assert report[(ref_name, "force_ibm")] < 1e-9
+            assert report[(ref_name, key)] <= bound, (ref_name, key, report[(ref_name, key)])
         report[(ref_name, "marker_force")] = rel(mk["force"], Mk["force"])
-        assert report[(ref_name, "marker_force")] < 1e-9
-        assert np.abs(mk["pos"] - Mk["pos"]).max() < 1e-11
+        assert report[(ref_name, "marker_force")] <= 1e-9
+        report[(ref_name, "marker_pos")] = rel(mk["pos"], Mk["pos"])
+        assert report[(ref_name, "marker_pos")] <= 1e-12
     pos = np.vstack([x["pos"] for x in fem])
-    assert np.abs(pos - g["fem_pos"]).max() < 1e-11
+    report[("reference", "fem_pos")] = rel(pos, g["fem_pos"])
+    assert report[("reference", "fem_pos")] <= 1e-12
     for k in range(len(fem)):
-        assert np.abs(fem[k]["pos"] - femo[k]["pos"]).max() < 1e-11
+        assert rel(fem[k]["pos"], femo[k]["pos"]) <= 1e-12
     assert st.code == 0
     print(name, {f"{a}:{b}": f"{v:.2e}" for (a, b), v in report.items()}, "subits", st.last_subits)
 
