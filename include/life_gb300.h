@@ -170,6 +170,21 @@ int life_case_get_markers(LifeCase* c, double* pos, double* vel, double* force,
 int life_case_get_bodies(LifeCase* c, int32_t* ids, int32_t* flexible, int32_t* n_markers,
                          int32_t* n_fem_nodes);
 
+/* Body shapes and marker lists, as ObjectsClass::writeVTK walks them
+ * (src/Objects.cpp:738-830): kind[n_bodies] (LIFE_BODY_CIRCLE or
+ * LIFE_BODY_FILAMENT; a circle's outline is closed) and, body after body, the
+ * global index of each of the body's markers in its node order
+ * (marker_index[n_markers]). Either pointer may be NULL. */
+int life_case_get_body_nodes(LifeCase* c, int32_t* kind, int32_t* marker_index);
+
+/* The arrays GridClass::writeVTK writes to Results/VTK/Fluid.<t>.vti
+ * (src/Grid.cpp:790-913) for the current state, in VTK point order (x
+ * fastest: point j*Nx + i): density[Nx*Ny] = rho*Drho, pressure[Nx*Ny] =
+ * ref_P + (rho - rho_p/Drho) c_s^2 Dm / (Dx Dt^2) and velocity[Nx*Ny*3] =
+ * (ux, uy, 0) Dx/Dt, each with the reference's operation order. Formed on
+ * the device, in the device's own site order; any pointer may be NULL. */
+int life_case_get_vtk_fields(LifeCase* c, double* density, double* pressure, double* velocity);
+
 /* Support table of every marker (IBMNodeClass::supp, reference
  * inc/IBMNode.h:69-70): count nsupp[n], lattice indices si/sj[n*9] and delta
  * weights sd[n*9], as findSupport left them (src/IBMNode.cpp:139-179). */

@@ -126,7 +126,7 @@ def body_structs(bodies: Sequence) -> "C.Array":
         d.number, d.id = int(b.number), int(b.ID)
         d.x, d.y, d.dx, d.dy = float(b.x), float(b.y), float(b.dx), float(b.dy)
         if isinstance(b, Circle):
-            d.kind = 0
+            d.kind = 0  # CIRCLE_KIND
             d.radius = float(b.radius)
         elif isinstance(b, Filament):
             d.kind = 1

@@ -32,6 +32,9 @@ LAT_NAMES = ["eFluid", "eWall", "eVelocity", "eFreeSlip", "ePressure", "eConvect
 PARABOLIC, SHEAR, BOUNDARY_LAYER = range(3)
 PROFILE_NAMES = ["eParabolic", "eShear", "eBoundaryLayer"]
 
+# geometry.config keywords (LifeBodyDesc.kind, LIFE_BODY_CIRCLE / _FILAMENT).
+CIRCLE_KIND, FILAMENT_KIND = 0, 1
+
 # Storage/arithmetic forms of the lattice populations on the GPU.
 PREC_F64, PREC_F32, PREC_F16 = 0, 1, 2
 PREC_NAMES = {"f64": PREC_F64, "f32": PREC_F32, "f16": PREC_F16}
@@ -70,6 +73,9 @@ class CaseParams:
     uni_epsilon: bool = False
     ordered: bool = True
     initial_deflect: Optional[float] = None
+    # output switches of params.h (VTK files; the FEM file too with vtk_fem)
+    vtk: bool = False
+    vtk_fem: bool = False
     nSteps: int = 100
     tinfo: int = 100
     tVTK: int = 100
@@ -134,6 +140,8 @@ class CaseParams:
         s.append(d("UNI_EPSILON", self.uni_epsilon))
         s.append(d("ORDERED", self.ordered))
         s.append(d("INITIAL_DEFLECT", self.initial_deflect is not None, self.initial_deflect))
+        s.append(d("VTK", self.vtk))
+        s.append(d("VTK_FEM", self.vtk_fem))
         s.append("#define FORCES\n#define TIPS\n")
         s.append(f"const int Nx = {int(self.Nx)};\nconst int Ny = {int(self.Ny)};\n")
         for name in ("height_p", "rho_p", "nu_p", "ux0_p", "uy0_p", "gravityX", "gravityY",

@@ -185,6 +185,20 @@ extern "C" int life_case_get_bodies(LifeCase* c, int32_t* ids, int32_t* flexible
     return LIFE_OK;
 }
 
+extern "C" int life_case_get_body_nodes(LifeCase* c, int32_t* kind, int32_t* marker_index) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    size_t q = 0;
+    for (size_t k = 0; k < c->obj.b.size(); k++) {
+        const HBody& b = c->obj.b[k];
+        if (kind) kind[k] = b.kind;
+        for (int m : b.nodes) {
+            if (marker_index) marker_index[q] = m;
+            q++;
+        }
+    }
+    return LIFE_OK;
+}
+
 // ObjectsClass::writeTotalForces (src/Objects.cpp:517-528): sequential sum
 // over markers, in lattice units scaled to newtons.
 extern "C" int life_case_total_force(LifeCase* c, double* fx, double* fy) {

@@ -215,6 +215,46 @@ __global__ void k_export(const typename S::T* __restrict__ P, LatDev L, int t, d
     if (fibm_out) { fibm_out[id * 2] = Ix; fibm_out[id * 2 + 1] = Iy; }
 }
 
+// The arrays GridClass::writeVTK writes (src/Grid.cpp:860-893), in VTK point
+// order (x fastest, the device's own order): density rho*Drho, pressure
+// ref_P + (rho - rho_p/Drho) c_s^2 Dm / (Dx Dt^2) and velocity u Dx/Dt with a
+// zero third component, each in the reference's operation order. `initial`
+// selects the state before the first step (as k_export_init).
+template <bool CM, class S>
+__global__ void k_export_vti(const typename S::T* __restrict__ P, LatDev L, int t, int initial, VtiScale V,
+                             double* __restrict__ dens, double* __restrict__ pres, double* __restrict__ vel) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= L.Nx) return;
+    double rho, ux, uy;
+    if (initial) {
+        rho = 1.0;
+        if (L.init_mode == 0) { ux = 0.0; uy = 0.0; }
+        else if (L.init_mode == 1) { ux = L.u_in[j * 2]; uy = L.u_in[j * 2 + 1]; }
+        else { ux = L.u0x; uy = L.u0y; }
+        if (site_type(L, i, j) == LIFE_WALL) { ux = 0.0; uy = 0.0; }
+    } else {
+        double f[9];
+        site_state<CM, S>(P, L, t, i, j, f, rho, ux, uy);
+        if (L.force_ibm) {
+            const size_t s = (size_t)j * L.pitch + i;
+            const double Ix = L.force_ibm[s], Iy = L.force_ibm[L.S + s];
+            if (Ix != 0.0 || Iy != 0.0) {
+                double Fx, Fy;
+                force_xy_at(L, t, Fx, Fy);
+                macroscopic_ibm(f, Fx, Fy, Ix, Iy, rho, ux, uy);
+            }
+        }
+    }
+    const size_t id = (size_t)j * L.Nx + i;
+    if (dens) dens[id] = rho * V.Drho;
+    if (pres) pres[id] = V.ref_P + (rho - V.rho_p / V.Drho) * (V.cs * V.cs) * V.Dm / (V.Dx * (V.Dt * V.Dt));
+    if (vel) {
+        vel[id * 3] = ux * (V.Dx / V.Dt);
+        vel[id * 3 + 1] = uy * (V.Dx / V.Dt);
+        vel[id * 3 + 2] = 0.0;
+    }
+}
+
 // Initial state (before any step) in reference layout.
 template <bool CM>
 __global__ void k_export_init(LatDev L, double* __restrict__ rho_out, double* __restrict__ u_out,
@@ -348,6 +388,12 @@ cudaError_t launch_export(const void* P, const LatDev& L, int t, bool initial, d
         if (L.cm) k_export<true, StoreF16><<<g, 128, 0, s>>>((const __half*)P, L, t, rho, u, f, fibm, i0, i1);
         else k_export<false, StoreF16><<<g, 128, 0, s>>>((const __half*)P, L, t, rho, u, f, fibm, i0, i1);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export_vti(const void* P, const LatDev& L, int t, bool initial, const VtiScale& V, double* dens,
+                              double* pres, double* vel, cudaStream_t s) {
+    LIFE_DISPATCH(k_export_vti, const, P, L, t, initial ? 1 : 0, V, dens, pres, vel);
     return cudaGetLastError();
 }
 

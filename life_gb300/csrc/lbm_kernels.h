@@ -22,6 +22,14 @@ cudaError_t launch_state(void* B, const LatDev& L, int t, const double* rho, con
 // the initial-state export always covers the whole lattice).
 cudaError_t launch_export(const void* P, const LatDev& L, int t, bool initial, double* rho, double* u, double* f,
                           double* fibm, cudaStream_t s, int i0 = 0, int i1 = -1);
+// Scalars of GridClass::writeVTK's conversions (src/Grid.cpp:860-893).
+struct VtiScale {
+    double Drho, ref_P, rho_p, cs, Dm, Dx, Dt;
+};
+// VTK-order (x fastest) density, pressure and 3-component velocity of the
+// state after step t (initial: the state before the first step).
+cudaError_t launch_export_vti(const void* P, const LatDev& L, int t, bool initial, const VtiScale& V, double* dens,
+                              double* pres, double* vel, cudaStream_t s);
 cudaError_t launch_maxvel(const void* P, const LatDev& L, int t, unsigned long long* out, cudaStream_t s);
 
 // One case of a batched interior launch: its lattice view and buffers for the

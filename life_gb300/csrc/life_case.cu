@@ -692,6 +692,51 @@ extern "C" int life_case_get_fields(LifeCase* c, double* rho, double* u, double*
     return LIFE_OK;
 }
 
+extern "C" int life_case_get_vtk_fields(LifeCase* c, double* density, double* pressure, double* velocity) {
+    if (!c) return set_error(LIFE_ERR_INVALID, "case is NULL");
+    const size_t n = (size_t)c->Nx * c->Ny;
+    VtiScale V{c->Drho, c->p.ref_P, c->p.rho_p, c->cs, c->Dm, c->Dx, c->Dt};
+    if (c->t == c->t_set && c->host_state) {
+        // a loaded restart state, before any step: the same conversions on
+        // the host arrays (reference layout id = i*Ny + j)
+        for (int j = 0; j < c->Ny; j++)
+            for (int i = 0; i < c->Nx; i++) {
+                const size_t id = (size_t)i * c->Ny + j, o = (size_t)j * c->Nx + i;
+                const double rho = c->h_rho[id];
+                if (density) density[o] = rho * V.Drho;
+                if (pressure)
+                    pressure[o] = V.ref_P + (rho - V.rho_p / V.Drho) * (V.cs * V.cs) * V.Dm / (V.Dx * (V.Dt * V.Dt));
+                if (velocity) {
+                    velocity[o * 3] = c->h_u[id * 2] * (V.Dx / V.Dt);
+                    velocity[o * 3 + 1] = c->h_u[id * 2 + 1] * (V.Dx / V.Dt);
+                    velocity[o * 3 + 2] = 0.0;
+                }
+            }
+        return LIFE_OK;
+    }
+    double *d_dens = nullptr, *d_pres = nullptr, *d_vel = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (density) e = cudaMallocAsync((void**)&d_dens, n * sizeof(double), c->stream);
+    if (e == cudaSuccess && pressure) e = cudaMallocAsync((void**)&d_pres, n * sizeof(double), c->stream);
+    if (e == cudaSuccess && velocity) e = cudaMallocAsync((void**)&d_vel, 3 * n * sizeof(double), c->stream);
+    if (e == cudaSuccess) {
+        const LatDev L = lattice_view(c, c->t);
+        e = launch_export_vti(c->P[c->cur ^ 1], L, c->t, c->t == c->t_set, V, d_dens, d_pres, d_vel, c->stream);
+    }
+    if (e == cudaSuccess && density)
+        e = cudaMemcpyAsync(density, d_dens, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && pressure)
+        e = cudaMemcpyAsync(pressure, d_pres, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && velocity)
+        e = cudaMemcpyAsync(velocity, d_vel, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    for (double* p : {d_dens, d_pres, d_vel})
+        if (p) cudaFreeAsync(p, c->stream);
+    const cudaError_t es = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = es;
+    if (e != cudaSuccess) return cuda_fail(e, "life_case_get_vtk_fields");
+    return LIFE_OK;
+}
+
 extern "C" int life_case_set_fields(LifeCase* c, int32_t t, const double* rho, const double* u, const double* f,
                                     const double* force_ibm) {
     if (!c || !rho || !u || !f) return set_error(LIFE_ERR_INVALID, "NULL argument");

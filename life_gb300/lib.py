@@ -52,6 +52,8 @@ SIGNATURES = {
     "life_case_max_velocity": (C.c_int, [C.c_void_p, _dp, _ip]),
     "life_case_total_force": (C.c_int, [C.c_void_p, _dp, _dp]),
     "life_case_record": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "life_case_get_body_nodes": (C.c_int, [C.c_void_p, _ip, _ip]),
+    "life_case_get_vtk_fields": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
     "life_measure_fp64_rate": (C.c_int, [_dp]),
     "life_selftest_trig": (C.c_int, [C.c_int32, C.c_int64, _dp, _dp, _dp]),
     "life_case_records": (C.c_int, [C.c_void_p, C.c_int32, _ip, _ip, _ip, _dp, _ip]),
@@ -271,6 +273,24 @@ class Case:
         tot, inner, launches = C.c_double(), C.c_double(), C.c_int32()
         _check(lib().life_case_bench_steps(self._h, int(n), C.byref(tot), C.byref(inner), C.byref(launches)))
         return tot.value, inner.value, launches.value
+
+    def vtk_fields(self):
+        """(density, pressure, velocity[.., 3]) as GridClass::writeVTK writes
+        them, in VTK point order (``life_case_get_vtk_fields``)."""
+        i = self.info()
+        n = i.Nx * i.Ny
+        dens, pres, vel = np.empty(n), np.empty(n), np.empty((n, 3))
+        _check(lib().life_case_get_vtk_fields(self._h, _p(dens), _p(pres), _p(vel)))
+        return dens, pres, vel
+
+    def body_nodes(self):
+        """(kind per body, global marker index of each body's markers in body
+        order) (``life_case_get_body_nodes``)."""
+        i = self.info()
+        kind = np.zeros(max(i.n_bodies, 1), dtype=np.int32)
+        idx = np.zeros(max(i.n_markers, 1), dtype=np.int32)
+        _check(lib().life_case_get_body_nodes(self._h, _p(kind), _p(idx)))
+        return kind[:i.n_bodies], idx[:i.n_markers]
 
     def total_force(self):
         fx, fy = C.c_double(), C.c_double()

@@ -87,6 +87,9 @@ def run_case(name: str, params, bodies, work: str, lapack: str = "openblas", thr
             out["fem_" + key] = np.concatenate([getattr(b, key) for b in fe.bodies])
         out["fem_pos0"] = np.vstack([b.pos0 for b in fe.bodies])
         out["fem_pos"] = np.vstack([b.pos for b in fe.bodies])
+    vdir = os.path.join(rdir, "Results", "VTK")
+    if os.path.isdir(vdir):
+        out["vtk_files"] = {name: open(os.path.join(vdir, name), "rb").read() for name in sorted(os.listdir(vdir))}
     for key, fname in (("total_forces_text", "TotalForces.out"), ("tip_positions_text", "TipPositions.out"),
                        ("tip_velocities_text", "TipVelocities.out")):
         path = os.path.join(rdir, "Results", fname)
