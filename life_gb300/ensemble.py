@@ -52,7 +52,8 @@ def filament_modulus(stiffness: float, u: float, length: float, height: float = 
 
 
 def ensemble_cases(n: int = 64, seed: int = 20260101, precision: int = 0, u_in: float = 0.04,
-                   mass_ratio: float = 10.0, stiffness=(1e-2, 1e-1)) -> List[Tuple[CaseParams, list]]:
+                   mass_ratio: float = 10.0, stiffness=(1e-2, 1e-1),
+                   thickness: float = THICKNESS) -> List[Tuple[CaseParams, list]]:
     """The batched-ensemble workload: n channel cases, inlet u_in on the left
     (ramped in over 400 steps), convective outlet, no-slip top and bottom.
 
@@ -107,9 +108,10 @@ def ensemble_cases(n: int = 64, seed: int = 20260101, precision: int = 0, u_in: 
                 x = x0 + col * 2.5 * lmax
                 y = H * (row + 1) / (nrows + 1)
                 L = lengths[k]
-                bodies.append(Filament(x=round(x, 3), y=round(y, 3), length=float(L), height=THICKNESS,
+                bodies.append(Filament(x=round(x, 3), y=round(y, 3), length=float(L), height=thickness,
                                        angle_deg=0.0, flexible=True, n_elements=L, clamped=True,
-                                       rho=mass_ratio * L / THICKNESS, E=filament_modulus(stiff[k], u_in, L), ID=k))
+                                       rho=mass_ratio * L / thickness,
+                                       E=filament_modulus(stiff[k], u_in, L, thickness), ID=k))
             lref = float(max(b.length for b in bodies))
         tau, _ = _tau_for(u_in, lref, re)
         kw = dict(wall_left=VELOCITY, wall_right=CONVECTIVE, wall_bottom=WALL, wall_top=WALL,
@@ -119,7 +121,7 @@ def ensemble_cases(n: int = 64, seed: int = 20260101, precision: int = 0, u_in: 
 
 
 def canopy_case(rng: np.random.Generator, precision: int = 1, mass_ratio: float = 10.0,
-                stiffness=(1e-2, 1e-1)) -> Tuple[CaseParams, list, int]:
+                stiffness=(1e-2, 1e-1), thickness: float = THICKNESS) -> Tuple[CaseParams, list, int]:
     """One serving request: a canopy of 8-32 stalks clamped on the bottom wall
     (angle 90 degrees), evenly spaced, length 20-40 lattice units with 20
     corotational elements each, bending stiffness log-uniform over
@@ -141,9 +143,9 @@ def canopy_case(rng: np.random.Generator, precision: int = 1, mass_ratio: float 
     if gap < 4.0:
         m = max(1, int((x1 - x0) // 4.0) + 1)
         gap = (x1 - x0) / max(m - 1, 1)
-    bodies = [Filament(x=round(x0 + k * gap, 3), y=0.0, length=lengths[k], height=THICKNESS, angle_deg=90.0,
-                       flexible=True, n_elements=20, clamped=True, rho=mass_ratio * lengths[k] / THICKNESS,
-                       E=filament_modulus(stiff[k], u, lengths[k]), ID=k) for k in range(m)]
+    bodies = [Filament(x=round(x0 + k * gap, 3), y=0.0, length=lengths[k], height=thickness, angle_deg=90.0,
+                       flexible=True, n_elements=20, clamped=True, rho=mass_ratio * lengths[k] / thickness,
+                       E=filament_modulus(stiff[k], u, lengths[k], thickness), ID=k) for k in range(m)]
     tau, _ = _tau_for(u, lmax, 100.0)
     from .case import FREESLIP
     p = _lattice(W, H, tau, precision, wall_left=VELOCITY, wall_right=CONVECTIVE, wall_bottom=WALL,
