@@ -404,17 +404,22 @@ def accuracy_leg(cyl_steps: int = 50000, fil_steps: int = 2000) -> dict:
 
 
 def ensemble_leg(steps: int, warmup: int, n_cases: int = 64, tile=None, sequential: bool = True,
-                 fp16_steps: int = None, seq_steps: int = None) -> dict:
+                 fp16_steps: int = None, seq_steps: int = None, long_error: bool = False) -> dict:
     """The 64-case batched ensemble (uneven lattices, cylinders or filament
     rows, BGK/CM, Re 50-300): batched FP32 over `steps` steps and FP16 over
     `fp16_steps` (one persistent interior launch and one replayed graph per
     batch step, autotuned tiles) against the same cases stepped one after
     another through life_case_step in FP64 and FP32 over `seq_steps` steps
     each (a bounded sample). MLUPS = sum of lattice sites x steps / device
-    time."""
+    time. With long_error, the same cases are also run as an FP64 batch for
+    the FP32 batch's whole length and every case's final velocity field is
+    compared: the FP32 error after the configured run, not a short sample."""
+    import numpy as np
     from life_gb300.ensemble import ensemble_cases, sites
     from life_gb300.lib import Batch, Case
     out = {}
+    u32 = {}
+    total32 = 0
     nsteps = {1: steps, 2: steps if fp16_steps is None else fp16_steps}
     for prec, tag in ((1, "fp32"), (2, "fp16")):
         steps = nsteps[prec]
@@ -436,6 +441,22 @@ def ensemble_leg(steps: int, warmup: int, n_cases: int = 64, tile=None, sequenti
             out[f"batched_{tag}_tile"] = [w, h]
             out[f"batched_{tag}_kernel_nodes_per_step"] = kn
             out[f"batched_{tag}_device_gb"] = round(inf.device_bytes / 1e9, 3)
+            if prec == 1 and long_error:
+                total32 = B.case(0).t
+                u32 = {k: B.case(k).fields(("u",))["u"] for k in range(len(cs))}
+    if long_error:
+        # the FP64 batch (the reference's arithmetic) over the same steps
+        t0 = time.perf_counter()
+        errs = []
+        with Batch(ensemble_cases(n=n_cases, precision=0)) as B:
+            B.step(total32)
+            for k in range(n_cases):
+                u64 = B.case(k).fields(("u",))["u"]
+                errs.append(float(np.abs(u32[k] - u64).max() / np.abs(u64).max()))
+        out["fp32_velocity_rel_err_after_full_run"] = {
+            "steps": total32, "max_over_cases": max(errs), "median_over_cases": float(np.median(errs)),
+            "cases_above_1e-5": int(sum(e > 1e-5 for e in errs)), "fp64_batch_seconds": round(time.perf_counter() - t0, 1)}
+        del u32
     cs = ensemble_cases(n=n_cases)
     out["cases"] = len(cs)
     out["sites"] = sites(cs)
@@ -475,7 +496,8 @@ def ensemble_leg(steps: int, warmup: int, n_cases: int = 64, tile=None, sequenti
     return out
 
 
-def serving_leg(n_requests: int = 24, step_scale: float = 0.02, seed: int = 7, load: float = 0.8) -> dict:
+def serving_leg(n_requests: int = 24, step_scale: float = 0.25, seed: int = 7, load: float = 0.8,
+                error_samples: int = 4) -> dict:
     """Serving: a seeded Poisson stream of canopy requests (8-32 stalks of 20
     elements, 512-4096 x 256-1024 lattices, FP32 lattice / FP64 FEM) against
     a 160 GB admission budget, continuous batching on one GB300.
@@ -485,7 +507,11 @@ def serving_leg(n_requests: int = 24, step_scale: float = 0.02, seed: int = 7, l
     2. stream: arrivals at rate load x capacity / mean request work, each
        request released as soon as it finishes; latency = finish - submit;
     3. baseline: the same kind of request solved alone in FP64 through
-       life_case_step, one after another (bounded sample of steps).
+       life_case_step, one after another (bounded sample of steps);
+    4. error: the `error_samples` requests with the least work are taken from
+       the server when they finish and compared with the same request solved
+       alone in FP64 (the reference's arithmetic) for the same steps: max
+       |u - u64| / max |u64| per request.
     Step counts are the request's 2000-20000 steps times step_scale."""
     import numpy as np
     from life_gb300.ensemble import canopy_case
@@ -518,6 +544,8 @@ def serving_leg(n_requests: int = 24, step_scale: float = 0.02, seed: int = 7, l
     # 2. Poisson stream at `load` of capacity
     lam = load * cap / float(np.mean(work))
     gaps = rng.exponential(1.0 / lam, size=n_requests)
+    sampled = set(sorted(range(n_requests), key=lambda k: work[k])[:error_samples])
+    u_served = {}
     with Server(hbm_budget=budget, steps_per_round=100) as S:
         t0 = time.perf_counter()
         ids = []
@@ -530,7 +558,7 @@ def serving_leg(n_requests: int = 24, step_scale: float = 0.02, seed: int = 7, l
                 time.sleep(min(dt, 0.01))
             ids.append(S.submit(p, b, s))
         lat, infos, done_work = [], [], 0
-        for i, w in zip(ids, work):
+        for k, (i, w) in enumerate(zip(ids, work)):
             try:
                 S.wait(i, timeout=7200)
             except LifeError:
@@ -540,7 +568,11 @@ def serving_leg(n_requests: int = 24, step_scale: float = 0.02, seed: int = 7, l
             if inf.state == REQ_DONE:
                 lat.append(inf.done_s - inf.submit_s)
                 done_work += w
-            S.release(i)
+            if k in sampled and inf.state == REQ_DONE:
+                with S.take(i) as c:
+                    u_served[k] = c.fields(("u",))["u"]
+            else:
+                S.release(i)
         st = S.stats()
     span = max(i.done_s for i in infos) - min(i.submit_s for i in infos)
     lat = np.array(lat if lat else [float("nan")])
@@ -567,6 +599,18 @@ def serving_leg(n_requests: int = 24, step_scale: float = 0.02, seed: int = 7, l
         ms_tot += tt
         n_ss += p.Nx * p.Ny * k
     out["sequential_fp64_mlups"] = round(n_ss / (ms_tot * 1e-3) / 1e6, 1)
+    # 4. served FP32 result against the request solved alone in FP64
+    import dataclasses
+    errs = {}
+    for k, u in u_served.items():
+        p, b, s = reqs[k]
+        with Case(dataclasses.replace(p, precision=0), b) as c:
+            c.step(s)
+            u64 = c.fields(("u",))["u"]
+        errs[k] = float(np.abs(u - u64).max() / np.abs(u64).max())
+    out["served_fp32_velocity_rel_err_vs_fp64_solo"] = {
+        "requests": sorted(errs), "steps": [reqs[k][2] for k in sorted(errs)],
+        "errors": [errs[k] for k in sorted(errs)], "max": max(errs.values()) if errs else None}
     out["aggregate_over_sequential_fp64"] = round(out["aggregate_mlups"] / out["sequential_fp64_mlups"], 2)
     # under an open (Poisson) stream the aggregate follows the arrival rate;
     # the capacity is what the server sustains
@@ -717,7 +761,7 @@ def run_gb300(args, world, rank, local):
         # ---- 64-case batched ensemble
         # (FP32 over the configured 10,000 steps; FP16 storage over 100, since
         # it does not carry long FSI runs)
-        extras["ensemble"] = ensemble_leg(10000, args.warmup, fp16_steps=100, seq_steps=20)
+        extras["ensemble"] = ensemble_leg(10000, args.warmup, fp16_steps=100, seq_steps=20, long_error=True)
         # ---- serving: Poisson stream of canopy requests
         extras["serving"] = serving_leg()
 
@@ -812,7 +856,7 @@ def main():
     ap.add_argument("--cases", type=int, default=64, help="ensemble: cases in the batch")
     ap.add_argument("--tile", default="", help="ensemble: fixed tile WxH instead of the autotuner")
     ap.add_argument("--batch-only", action="store_true", help="ensemble: skip the sequential per-case runs")
-    ap.add_argument("--step-scale", type=float, default=0.02, help="serve: fraction of each request's steps")
+    ap.add_argument("--step-scale", type=float, default=0.25, help="serve: fraction of each request's steps")
     ap.add_argument("--workload", default="cavity", choices=["cavity", "cylinder", "filament", "ensemble", "serve", "accuracy"],
                     help="cavity: the headline line; cylinder/filament: timing of one IBM case; "
                          "ensemble: the 64-case batch against sequential per-case runs; "

@@ -25,15 +25,51 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+#include <cstring>
+
 #include "collide_cm.cuh"
 #include "lbm_device.cuh"
 #include "lbm_kernels.h"
 
 namespace life {
 
-__device__ __forceinline__ void e1d(float u, float e[3], float w[3], float d[3]) {
+// Two sites' FP32 arithmetic in one instruction: the packed FADD2 / FMUL2 /
+// FFMA2 of sm_100 (__fadd2_rn, __fmul2_rn, __ffma2_rn). Each lane is an IEEE
+// round-to-nearest FP32 operation, so each lane of a V2 computation gives,
+// bit for bit, the float computation written with the same expressions. The
+// collision below is written once as a template over float and V2.
+struct V2 {
+    float2 v;
+};
+__device__ __forceinline__ V2 v2(float a) { return V2{make_float2(a, a)}; }
+__device__ __forceinline__ V2 v2(float a, float b) { return V2{make_float2(a, b)}; }
+__device__ __forceinline__ V2 operator+(V2 a, V2 b) { return V2{__fadd2_rn(a.v, b.v)}; }
+__device__ __forceinline__ V2 operator-(V2 a) { return V2{make_float2(-a.v.x, -a.v.y)}; }
+__device__ __forceinline__ V2 operator-(V2 a, V2 b) { return a + (-b); }  // a - b == a + (-b) in IEEE
+__device__ __forceinline__ V2 operator*(V2 a, V2 b) { return V2{__fmul2_rn(a.v, b.v)}; }
+__device__ __forceinline__ V2 operator+(float a, V2 b) { return v2(a) + b; }
+__device__ __forceinline__ V2 operator+(V2 a, float b) { return a + v2(b); }
+__device__ __forceinline__ V2 operator-(float a, V2 b) { return v2(a) - b; }
+__device__ __forceinline__ V2 operator-(V2 a, float b) { return a - v2(b); }
+__device__ __forceinline__ V2 operator*(float a, V2 b) { return v2(a) * b; }
+__device__ __forceinline__ V2 operator*(V2 a, float b) { return a * v2(b); }
+__device__ __forceinline__ V2 fmaf(V2 a, V2 b, V2 c) { return V2{__ffma2_rn(a.v, b.v, c.v)}; }
+__device__ __forceinline__ V2 fmaf(float a, V2 b, V2 c) { return fmaf(v2(a), b, c); }
+__device__ __forceinline__ V2 fmaf(V2 a, float b, V2 c) { return fmaf(a, v2(b), c); }
+__device__ __forceinline__ V2 fmaf(V2 a, V2 b, float c) { return fmaf(a, b, v2(c)); }
+__device__ __forceinline__ V2 fmaf(float a, float b, V2 c) { return fmaf(v2(a), v2(b), c); }
+__device__ __forceinline__ V2 fmaf(float a, V2 b, float c) { return fmaf(v2(a), b, v2(c)); }
+__device__ __forceinline__ V2 fmaf(V2 a, float b, float c) { return fmaf(a, v2(b), v2(c)); }
+using ::fmaf;
+template <class T> __device__ __forceinline__ T zero_of();
+template <> __device__ __forceinline__ float zero_of<float>() { return 0.0f; }
+template <> __device__ __forceinline__ V2 zero_of<V2>() { return v2(0.0f); }
+
+template <class T>
+__device__ __forceinline__ void e1d(T u, T e[3], float w[3], T d[3]) {
     // index 0: c = 0, 1: c = +1, 2: c = -1
-    const float u2 = u * u;
+    const T u2 = u * u;
     w[0] = 2.0f / 3.0f;
     w[1] = w[2] = 1.0f / 6.0f;
     d[0] = -u2;
@@ -48,33 +84,35 @@ __device__ __forceinline__ int ax(int c) { return c == 0 ? 0 : (c > 0 ? 1 : 2); 
 
 // c_v . (a, b) for the D2Q9 velocity v (components 0 or +-1, known at
 // compile time after unrolling): only the additions and signs it needs.
-__device__ __forceinline__ float cdot(int v, float a, float b) {
+template <class T>
+__device__ __forceinline__ T cdot(int v, T a, T b) {
     const int cx = cx_of(v), cy = cy_of(v);
-    const float xa = cx == 0 ? 0.0f : (cx > 0 ? a : -a);
+    const T xa = cx == 0 ? zero_of<T>() : (cx > 0 ? a : -a);
     if (cy == 0) return xa;
-    const float yb = cy > 0 ? b : -b;
+    const T yb = cy > 0 ? b : -b;
     return cx == 0 ? yb : xa + yb;
 }
 
 // FORCED = false: the force of this step is zero everywhere (no gravity, no
 // Womersley term), so every forcing term is an exact zero and is not formed.
-template <bool CM, bool FORCED>
-__device__ __forceinline__ void collide_dev32(const float g[9], float dr, float rho, float mx, float my, float ux,
-                                              float uy, float Gx, float Gy, float omega, float gs[9]) {
+// T = float: one site; T = V2: two sites, lane by lane the same operations.
+template <bool CM, bool FORCED, class T>
+__device__ __forceinline__ void collide_dev32(const T g[9], T dr, T rho, T mx, T my, T ux, T uy, float Gx, float Gy,
+                                              float omega, T gs[9]) {
     if (!CM) {
-        const float usq15 = 1.5f * fmaf(ux, ux, uy * uy);
-        const float uF = FORCED ? fmaf(ux, Gx, uy * Gy) : 0.0f;
+        const T usq15 = 1.5f * fmaf(ux, ux, uy * uy);
+        const T uF = FORCED ? fmaf(ux, Gx, uy * Gy) : zero_of<T>();
         const float fo = fmaf(-0.5f, omega, 1.0f);
 #pragma unroll
         for (int v = 0; v < 9; v++) {
             const float w = wgt_f(v);
-            const float cu = cdot(v, ux, uy);
-            const float inner = fmaf(4.5f * cu, cu, fmaf(3.0f, cu, -usq15));
-            const float geq = w * fmaf(rho, inner, dr);
-            const float a = fmaf(omega, geq - g[v], g[v]);
+            const T cu = cdot(v, ux, uy);
+            const T inner = fmaf(4.5f * cu, cu, fmaf(3.0f, cu, -usq15));
+            const T geq = w * fmaf(rho, inner, dr);
+            const T a = fmaf(omega, geq - g[v], g[v]);
             if (FORCED) {
                 const float cF = cdot(v, Gx, Gy);
-                const float Fv = (3.0f * w) * fmaf(3.0f * cu, cF, cF - uF);
+                const T Fv = (3.0f * w) * fmaf(3.0f * cu, cF, cF - uF);
                 gs[v] = fmaf(fo, Fv, a);
             } else {
                 gs[v] = a;
@@ -82,20 +120,21 @@ __device__ __forceinline__ void collide_dev32(const float g[9], float dr, float 
         }
     } else {
         // raw second moments of the deviations
-        const float dxxyy = (g[1] + g[2]) - (g[3] + g[4]);
-        const float gxy = (g[5] + g[6]) - (g[7] + g[8]);
+        const T dxxyy = (g[1] + g[2]) - (g[3] + g[4]);
+        const T gxy = (g[5] + g[6]) - (g[7] + g[8]);
         const float om1 = 1.0f - omega;
-        const float k4 = om1 * fmaf(ux * ux - uy * uy, rho, fmaf(2.0f * uy, my, fmaf(-2.0f * ux, mx, dxxyy)));
-        const float k5 = om1 * fmaf(ux * uy, rho, fmaf(-ux, my, fmaf(-uy, mx, gxy)));
+        const T k4 = om1 * fmaf(ux * ux - uy * uy, rho, fmaf(2.0f * uy, my, fmaf(-2.0f * ux, mx, dxxyy)));
+        const T k5 = om1 * fmaf(ux * uy, rho, fmaf(-ux, my, fmaf(-uy, mx, gxy)));
         // force moments (exact zeros, and unused, when not FORCED)
         const float k1 = FORCED ? 0.5f * Gx : 0.0f, k2 = FORCED ? 0.5f * Gy : 0.0f;
         const float k7 = FORCED ? Gx * (1.0f / 6.0f) : 0.0f, k6 = FORCED ? Gy * (1.0f / 6.0f) : 0.0f;
-        float ex[3], wx[3], dx[3], ey[3], wy[3], dy[3];
+        T ex[3], dx[3], ey[3], dy[3];
+        float wx[3], wy[3];
         e1d(ux, ex, wx, dx);
         e1d(uy, ey, wy, dy);
-        const float X2 = ux * ux, Y2 = uy * uy, XY = ux * uy;
+        const T X2 = ux * ux, Y2 = uy * uy, XY = ux * uy;
         // T_v1..T_v7 (force/stress columns of the inverse transform)
-        float T1[9], T2[9], T4[9], T5[9], T6[9], T7[9];
+        T T1[9], T2[9], T4[9], T5[9], T6[9], T7[9];
         T1[0] = 2.0f * ux * (Y2 - 1.0f);          T2[0] = 2.0f * uy * (X2 - 1.0f);
         T4[0] = -0.5f * (X2 - Y2);                T5[0] = 4.0f * XY;
         T6[0] = 2.0f * uy;                        T7[0] = 2.0f * ux;
@@ -126,9 +165,9 @@ __device__ __forceinline__ void collide_dev32(const float g[9], float dr, float 
 #pragma unroll
         for (int v = 0; v < 9; v++) {
             const int a = ax(cx_of(v)), b = ax(cy_of(v));
-            const float E = ex[a] * ey[b];
-            const float D = fmaf(dx[a], dy[b], fmaf(wx[a], dy[b], dx[a] * wy[b]));
-            float acc = fmaf(dr, E, D);
+            const T E = ex[a] * ey[b];
+            const T D = fmaf(dx[a], dy[b], fmaf(wx[a], dy[b], dx[a] * wy[b]));
+            T acc = fmaf(dr, E, D);
             if (FORCED) {
                 acc = fmaf(T1[v], k1, acc);
                 acc = fmaf(T2[v], k2, acc);
@@ -301,7 +340,177 @@ __global__ void __launch_bounds__(256, 6) k_step_lowp(const typename S::T* __res
     interior_site_lowp<CM, S>(A, B, L, t, i, j);
 }
 
+// ---- two x-adjacent sites per thread --------------------------------------
+//
+// A thread takes the sites (s, s+1), s even, and moves each population plane
+// as one aligned word per pair: the stored pair at (s, s+1) of the source row
+// (two halves or two floats). Populations streaming along x need the pair
+// shifted by one site: (s-1, s) for c_x = +1 and (s+1, s+2) for c_x = -1; a
+// warp covers 64 consecutive sites of one row, so each lane takes the missing
+// half of its pair from its neighbour lane's word (a shuffle), and lanes 0 and
+// 31 load the one word beyond the warp. The collision runs on both sites at
+// once in packed FP32 (V2), lane by lane the operations of the one-site path,
+// so the results are those of interior_site_lowp bit for bit. Pairs that touch
+// a boundary column, a periodic wrap or the convective outlet's columns take
+// the one-site path.
+template <class S>
+struct PairWord;
+template <>
+struct PairWord<StoreF16> {
+    using W = unsigned;  // (site s, site s+1) as two halves
+    __device__ static __forceinline__ W load(const __half* P, size_t idx) {
+        return __ldg(reinterpret_cast<const unsigned*>(P) + (idx >> 1));
+    }
+    // (prev.hi, cur.lo): the pair one site to the left
+    __device__ static __forceinline__ W left(W cur, int lane, const __half* P, size_t idx, bool has_left) {
+        W prev = __shfl_up_sync(0xffffffffu, cur, 1);
+        if (lane == 0) prev = has_left ? load(P, idx - 2) : 0u;
+        return __byte_perm(prev, cur, 0x5432);
+    }
+    // (cur.hi, next.lo): the pair one site to the right
+    __device__ static __forceinline__ W right(W cur, int lane, const __half* P, size_t idx, bool has_right) {
+        W next = __shfl_down_sync(0xffffffffu, cur, 1);
+        if (lane == 31) next = has_right ? load(P, idx + 2) : 0u;
+        return __byte_perm(cur, next, 0x5432);
+    }
+    __device__ static __forceinline__ V2 dev(W w, int v) {
+        __half2 h;
+        memcpy(&h, &w, sizeof h);
+        return V2{__half22float2(h)} * h16_scale(v);
+    }
+    __device__ static __forceinline__ void put(__half* P, size_t idx, V2 g, int v) {
+        const V2 o = g * h16_inv(v);
+        reinterpret_cast<__half2*>(P)[idx >> 1] = __float22half2_rn(o.v);
+    }
+};
+template <>
+struct PairWord<StoreF32> {
+    using W = float2;  // (site s, site s+1)
+    __device__ static __forceinline__ W load(const float* P, size_t idx) {
+        return __ldg(reinterpret_cast<const float2*>(P) + (idx >> 1));
+    }
+    __device__ static __forceinline__ W left(W cur, int lane, const float* P, size_t idx, bool has_left) {
+        float py = __shfl_up_sync(0xffffffffu, cur.y, 1);
+        if (lane == 0) py = has_left ? P[idx - 1] : 0.0f;
+        return make_float2(py, cur.x);
+    }
+    __device__ static __forceinline__ W right(W cur, int lane, const float* P, size_t idx, bool has_right) {
+        float nx = __shfl_down_sync(0xffffffffu, cur.x, 1);
+        if (lane == 31) nx = has_right ? P[idx + 2] : 0.0f;
+        return make_float2(cur.y, nx);
+    }
+    __device__ static __forceinline__ V2 dev(W w, int) { return V2{w}; }
+    __device__ static __forceinline__ void put(float* P, size_t idx, V2 g, int) {
+        reinterpret_cast<float2*>(P)[idx >> 1] = g.v;
+    }
+};
+
+// Sites (s, s+1) of an interior row 1 <= j <= Ny-2; every lane of the warp
+// calls it (the shuffles), lanes past the row end do nothing.
+template <bool CM, bool FORCED, class S>
+__device__ __forceinline__ void interior_pair_lowp(const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
+                                                   const LatDev& L, int t, int s, int j) {
+    using P = PairWord<S>;
+    const int lane = threadIdx.x & 31;
+    // the loads of lanes past the row stay inside the row's pitch
+    const int sc = s < L.pitch - 2 ? s : L.pitch - 2;
+    const bool has_left = sc >= 2, has_right = sc + 2 <= L.pitch - 2;
+    typename P::W w[9];
+#pragma unroll
+    for (int v = 0; v < 9; v++) {
+        const size_t idx = (size_t)v * L.S + (size_t)(j - cy_of(v)) * L.pitch + sc;
+        const typename P::W cur = P::load(A, idx);
+        if (cx_of(v) == 0) w[v] = cur;
+        else if (cx_of(v) > 0) w[v] = P::left(cur, lane, A, idx, has_left);
+        else w[v] = P::right(cur, lane, A, idx, has_right);
+    }
+    const bool pair_ok = s >= 2 && s + 1 <= L.Nx - 2 && !(L.convective && s + 1 >= L.Nx - 3);
+    if (!pair_ok) {
+        if (s < L.Nx) interior_site_lowp_f<CM, FORCED, S>(A, B, L, t, s, j);
+        if (s + 1 < L.Nx) interior_site_lowp_f<CM, FORCED, S>(A, B, L, t, s + 1, j);
+        return;
+    }
+    V2 g[9];
+#pragma unroll
+    for (int v = 0; v < 9; v++) g[v] = P::dev(w[v], v);
+    float Fxd = 0.0f, Fyd = 0.0f, Gxd = 0.0f, Gyd = 0.0f;
+    if (FORCED) {
+        force_xy_at_f(L, t, Fxd, Fyd);
+        force_xy_at_f(L, t + 1, Gxd, Gyd);
+    }
+    const V2 dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
+    const V2 rho = 1.0f + dr;
+    const V2 mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
+    const V2 my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
+    const V2 inv = v2(__frcp_rn(rho.v.x), __frcp_rn(rho.v.y));
+    const V2 ux = (FORCED ? fmaf(0.5f, Fxd, mx) : mx) * inv, uy = (FORCED ? fmaf(0.5f, Fyd, my) : my) * inv;
+    V2 gs[9];
+    collide_dev32<CM, FORCED>(g, dr, rho, mx, my, ux, uy, Gxd, Gyd, L.omega_f, gs);
+    const size_t base = (size_t)j * L.pitch + s;
+#pragma unroll
+    for (int v = 0; v < 9; v++) P::put(B, (size_t)v * L.S + base, gs[v], v);
+}
+
+// k_step_lowp with two sites per thread (512 sites per block).
+template <bool CM, class S>
+__global__ void __launch_bounds__(256, 4) k_step_lowp2(const typename S::T* __restrict__ A,
+                                                       typename S::T* __restrict__ B, LatDev L, int t, int pb,
+                                                       int bx, unsigned bx_m) {
+    t = step_t(L, t);
+    if ((int)blockIdx.x < pb) {
+        perimeter_site_call<CM, S>(A, B, L, t, blockIdx.x * blockDim.x + threadIdx.x);
+        return;
+    }
+    const unsigned b = blockIdx.x - pb;
+    const int j = bx_m ? (int)__umulhi(b, bx_m) : (int)(b / (unsigned)bx);
+    const int s = 2 * ((int)(b - (unsigned)j * (unsigned)bx) * (int)blockDim.x + (int)threadIdx.x);
+    if (j == 0 || j == L.Ny - 1) {  // the whole block: boundary rows or periodic wraps
+        if (s < L.Nx) interior_site_lowp<CM, S>(A, B, L, t, s, j);
+        if (s + 1 < L.Nx) interior_site_lowp<CM, S>(A, B, L, t, s + 1, j);
+        return;
+    }
+    if (lattice_forced(L)) interior_pair_lowp<CM, true, S>(A, B, L, t, s, j);
+    else interior_pair_lowp<CM, false, S>(A, B, L, t, s, j);
+}
+
+// Which step kernel a reduced-precision form uses: 1 = k_step_lowp (one site
+// per thread), 2 = k_step_lowp2 (two). LIFE_STEP_SITES=1|2 overrides.
+static int step_sites(int prec) {
+    static int forced = -1;
+    if (forced < 0) {
+        const char* e = getenv("LIFE_STEP_SITES");
+        forced = (e && (e[0] == '1' || e[0] == '2')) ? e[0] - '0' : 0;
+    }
+    if (forced) return forced;
+    return prec == LIFE_PREC_F16 ? 2 : 2;
+}
+
+static unsigned div_magic(int bx, long long bmax) {
+    // m = floor(2^32 / bx) + 1 gives floor(b / bx) = umulhi(b, m) exactly
+    // when b (m bx - 2^32) < 2^32 for the largest b; else 0 (divide)
+    const unsigned long long m = (1ull << 32) / (unsigned long long)bx + 1ull;
+    return (m < (1ull << 32) && (unsigned long long)bmax * (m * (unsigned long long)bx - (1ull << 32)) < (1ull << 32))
+               ? (unsigned)m : 0u;
+}
+
 cudaError_t launch_step_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
+    if (step_sites(L.prec) == 2) {
+        const int n = 2 * L.Nx + 2 * (L.Ny - 2);
+        const int pb = (n + 255) / 256, bx = (L.Nx + 511) / 512;
+        const unsigned grid = (unsigned)(pb + bx * L.Ny);
+        const unsigned bx_m = div_magic(bx, (long long)bx * L.Ny);
+        if (L.prec == LIFE_PREC_F32) {
+            if (L.cm) k_step_lowp2<true, StoreF32><<<grid, 256, 0, s>>>((const float*)A, (float*)B, L, t, pb, bx, bx_m);
+            else k_step_lowp2<false, StoreF32><<<grid, 256, 0, s>>>((const float*)A, (float*)B, L, t, pb, bx, bx_m);
+        } else {
+            if (L.cm)
+                k_step_lowp2<true, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t, pb, bx, bx_m);
+            else
+                k_step_lowp2<false, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t, pb, bx, bx_m);
+        }
+        return cudaGetLastError();
+    }
+
     const int n = 2 * L.Nx + 2 * (L.Ny - 2);
     const int pb = (n + 255) / 256, bx = (L.Nx + 255) / 256;
     const unsigned grid = (unsigned)(pb + bx * L.Ny);

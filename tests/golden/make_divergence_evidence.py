@@ -21,7 +21,13 @@ reference finished, the last step whose tip line it wrote, and the last line
 it printed (``Subiteration scheme hit 20 iterations...exiting`` when the
 coupling diverged, src/Objects.cpp:58-59).
 
-    python tests/golden/make_divergence_evidence.py [--threads N]
+    python tests/golden/make_divergence_evidence.py --sweep [--canopy K ...]
+        [--ensemble-thin-1e-3 K ...] [--threads N]
+
+``--canopy K`` runs request K of the seeded serving stream at its full length
+and ``--ensemble-thin-1e-3 K`` case K of the ensemble drawn with the
+configured stiffness range (1e-3..1e-1), both with info and tips every 50
+steps.
 """
 from __future__ import annotations
 
@@ -73,34 +79,73 @@ def run(name: str, p, b, work: str, threads: int) -> dict:
     res = subprocess.run([exe], cwd=rdir, env=env, capture_output=True, text=True)
     tips = open(os.path.join(rdir, "Results", "TipPositions.out")).read().strip().splitlines()
     lines = [ln for ln in res.stdout.strip().splitlines() if ln.strip()]
+    tips = tips if tips else ["", "0"]
     return {"completed": res.returncode == 0, "exit_status": res.returncode,
             "last_tip_step": int(tips[-1].split("\t")[0]) if len(tips) > 1 else 0,
             "last_tip_line": tips[-1], "last_output_line": lines[-1] if lines else "",
             "E": b[0].E, "rho": b[0].rho, "height": b[0].height}
 
 
+def canopy_request(k: int, seed: int = 7, steps=None, **kw):
+    """Request k of the seeded serving stream (life_gb300.ensemble.canopy_case)."""
+    import numpy as np
+    from life_gb300.ensemble import canopy_case
+    rng = np.random.Generator(np.random.PCG64(seed))
+    for _ in range(k + 1):
+        p, b, n = canopy_case(rng, precision=0, **kw)
+    n = steps or n
+    return p.replace(nSteps=n, tinfo=50, tVTK=n, tRestart=0), b
+
+
+def ensemble_case(k: int, **kw):
+    """Case k of the seeded ensemble (life_gb300.ensemble.ensemble_cases)."""
+    from life_gb300.ensemble import ensemble_cases
+    p, b = ensemble_cases(n=k + 1, precision=0, **kw)[k]
+    return p.replace(nSteps=STEPS, tinfo=50, tVTK=STEPS, tRestart=0), b
+
+
 def main(argv) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--threads", type=int, default=os.cpu_count() or 1)
+    ap.add_argument("--sweep", action="store_true", help="the single-filament stiffness sweep")
+    ap.add_argument("--canopy", type=int, nargs="*", default=[], help="serving-stream requests to run in full")
+    ap.add_argument("--ensemble-thin-1e-3", type=int, nargs="*", default=[],
+                    help="ensemble cases drawn with stiffness 1e-3..1e-1 (thickness 0.1, mass ratio 10)")
     a = ap.parse_args(argv[1:])
     if not os.path.isdir(os.path.join(REF, "src")):
         print(f"reference tree not found at {REF}", file=sys.stderr)
         return 2
-    work = tempfile.mkdtemp(prefix="life_evidence_")
+    path = os.path.join(HERE, "divergence_reference.json")
     out = {"steps": STEPS, "lattice": [512, 256], "filament_length": 40, "elements": 40, "inlet": 0.04,
            "tau": 0.548, "lapack": "openblas", "runs": {}}
-    try:
+    if os.path.exists(path):
+        with open(path) as fh:
+            out = json.load(fh)
+    jobs = []
+    if a.sweep:
         for sec, (h, mr) in SECTIONS.items():
             for s in STIFFNESS:
-                name = f"{sec}_stiffness{s:g}"
                 p, b = case(s, h, mr)
-                r = run(name, p, b, work, a.threads)
-                r.update(stiffness=s, section=sec, mass_ratio=mr)
-                out["runs"][name] = r
-                print(name, "completed" if r["completed"] else f"failed after step {r['last_tip_step']}",
-                      "|", r["last_output_line"], flush=True)
-                with open(os.path.join(HERE, "divergence_reference.json"), "w") as fh:
-                    json.dump(out, fh, indent=1, sort_keys=True)
+                jobs.append((f"{sec}_stiffness{s:g}", p, b, dict(stiffness=s, section=sec, mass_ratio=mr)))
+    for k in a.canopy:
+        p, b = canopy_request(k)
+        jobs.append((f"canopy_request{k}", p, b, dict(request=k, steps=p.nSteps, lattice=[p.Nx, p.Ny],
+                                                     stalks=len(b))))
+    for k in a.ensemble_thin_1e_3:
+        p, b = ensemble_case(k, stiffness=(1e-3, 1e-1))
+        jobs.append((f"ensemble_stiffness1e-3_case{k}", p, b,
+                     dict(case=k, lattice=[p.Nx, p.Ny], filaments=len(b),
+                          min_stiffness_E=min(x.E for x in b))))
+    work = tempfile.mkdtemp(prefix="life_evidence_")
+    try:
+        for name, p, b, meta in jobs:
+            r = run(name, p, b, work, a.threads)
+            r.update(meta)
+            out["runs"][name] = r
+            print(name, "completed" if r["completed"] else f"failed after step {r['last_tip_step']}",
+                  "|", r["last_output_line"], flush=True)
+            with open(path, "w") as fh:
+                json.dump(out, fh, indent=1, sort_keys=True)
     finally:
         shutil.rmtree(work, ignore_errors=True)
     return 0

@@ -1,0 +1,57 @@
+"""The one-launch step kernels of the reduced-precision forms (lattices of
+2^22 sites or more) against each other and against the separate perimeter +
+interior kernels of the host-driven loop: k_step_lowp2 (two x-adjacent sites
+per thread, packed FP32 arithmetic, shuffled pair loads), k_step_lowp (one
+site per thread) and LIFE_CASE_HOSTLOOP=1 must give the same bits after N
+steps, for BGK and central moments, with and without a step force, with a
+convective outlet, periodic x walls and an odd width (a lone last site)."""
+import os
+import subprocess
+import sys
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+CODE = r"""
+import hashlib, sys
+sys.path.insert(0, '.')
+from life_gb300.case import CaseParams, CONVECTIVE, FLUID, VELOCITY, WALL
+from life_gb300.lib import Case
+kind, prec = sys.argv[1], int(sys.argv[2])
+omega = 1.0 / 0.56
+nu = (1.0 / omega - 0.5) / 3.0
+if kind == 'cavity':
+    p = CaseParams(Nx=2049, Ny=2048, height_p=2047.0, rho_p=1.0, nu_p=nu, omega=omega, wall_left=WALL,
+                   wall_right=WALL, wall_bottom=WALL, wall_top=VELOCITY, uxInlet_p=0.1, precision=prec)
+elif kind == 'channel_cm_forced':
+    p = CaseParams(Nx=2050, Ny=2048, height_p=2047.0, rho_p=1.0, nu_p=nu, omega=omega, wall_left=VELOCITY,
+                   wall_right=CONVECTIVE, wall_bottom=WALL, wall_top=WALL, uxInlet_p=0.05, gravityY=-1e-6,
+                   central_moments=True, inlet_ramp=10.0, precision=prec)
+else:
+    p = CaseParams(Nx=2048, Ny=2051, height_p=2050.0, rho_p=1.0, nu_p=nu, omega=omega, wall_left=FLUID,
+                   wall_right=FLUID, wall_bottom=WALL, wall_top=WALL, gravityX=2e-6, precision=prec)
+with Case(p) as c:
+    c.step(30)
+    fl = c.fields(("rho", "u"))
+print("DIGEST", hashlib.sha256(fl["rho"].tobytes() + fl["u"].tobytes()).hexdigest())
+"""
+
+
+def digest(kind, prec, env):
+    res = subprocess.run([sys.executable, "-c", CODE, kind, str(prec)], cwd=ROOT, capture_output=True, text=True,
+                         env=dict(os.environ, **env))
+    assert res.returncode == 0, res.stderr[-2000:]
+    return [ln for ln in res.stdout.splitlines() if ln.startswith("DIGEST")][-1]
+
+
+@pytest.mark.parametrize("kind", ["cavity", "channel_cm_forced", "periodic_x_forced"])
+@pytest.mark.parametrize("prec", [1, 2])
+def test_step_kernels_bit_identical(kind, prec):
+    from life_gb300.build import build
+    build()
+    two = digest(kind, prec, {"LIFE_STEP_SITES": "2"})
+    one = digest(kind, prec, {"LIFE_STEP_SITES": "1"})
+    host = digest(kind, prec, {"LIFE_CASE_HOSTLOOP": "1"})
+    assert two == one == host
