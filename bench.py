@@ -291,6 +291,11 @@ def run_workload(args, world, rank):
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
+    if args.workload == "spread":
+        out = {"workload": "spread_scaling", **spread_leg(steps=args.steps, warmup=args.warmup)}
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        return 0
     if args.workload == "accuracy":
         out = {"workload": "accuracy", **accuracy_leg(args.steps, max(args.steps // 25, 50))}
         if rank == 0:
@@ -314,6 +319,36 @@ def run_workload(args, world, rank):
     if rank == 0:
         print(json.dumps(out), flush=True)
     return 0
+
+
+def spread_leg(counts=(0, 16, 32, 64, 128), steps: int = 200, warmup: int = 5) -> dict:
+    """IBM cost against marker count: a row of N rigid stalks (30 lattice
+    units, 31 markers each, the Honami example's stalks) clamped on the
+    bottom wall of a 3106 x 91 boundary-layer channel (the Honami example's
+    lattice), central moments, FP64. ms per step for each N; the IBM cost is
+    the difference to the same lattice without bodies."""
+    from life_gb300.case import BOUNDARY_LAYER, CONVECTIVE, FREESLIP, VELOCITY, WALL, CaseParams, Filament
+    from life_gb300.lib import Case
+    tau = 0.55
+    out = {"lattice": [3106, 91], "steps": steps, "points": []}
+    base = None
+    for n in counts:
+        p = CaseParams(Nx=3106, Ny=91, height_p=90.0, rho_p=1.0, nu_p=(tau - 0.5) / 3.0, omega=1.0 / tau,
+                       wall_left=VELOCITY, wall_right=CONVECTIVE, wall_bottom=WALL, wall_top=FREESLIP,
+                       profile=BOUNDARY_LAYER, uxInlet_p=0.04, inlet_ramp=50.0, central_moments=True, ref_L=30.0)
+        gap = 2900.0 / max(n, 1)
+        b = ([Filament(x=100.0, y=0.0, length=30.0, height=1.0, angle_deg=90.0, flexible=False, n_elements=None,
+                       clamped=True, rho=1.0, E=1.0, ID=0, number=n, dx=gap)] if n else [])
+        with Case(p, b) as c:
+            c.step(warmup)
+            tt, _, launches = c.bench_steps(steps)
+            markers = c.info().n_markers
+        ms = tt / steps
+        if n == 0:
+            base = ms
+        out["points"].append({"stalks": n, "markers": markers, "ms_per_step": round(ms, 4),
+                              "ibm_ms_per_step": round(ms - base, 4) if base is not None else None})
+    return out
 
 
 def _upward_crossings(t, y):
@@ -857,7 +892,7 @@ def main():
     ap.add_argument("--tile", default="", help="ensemble: fixed tile WxH instead of the autotuner")
     ap.add_argument("--batch-only", action="store_true", help="ensemble: skip the sequential per-case runs")
     ap.add_argument("--step-scale", type=float, default=0.25, help="serve: fraction of each request's steps")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "cylinder", "filament", "ensemble", "serve", "accuracy"],
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "cylinder", "filament", "ensemble", "serve", "accuracy", "spread"],
                     help="cavity: the headline line; cylinder/filament: timing of one IBM case; "
                          "ensemble: the 64-case batch against sequential per-case runs; "
                          "serve: the Poisson request stream; accuracy: FP32 vs FP64 cylinder "

@@ -400,7 +400,21 @@ int life_measure_fp64_rate(double* gflops);
 
 /* Parses geometry.config text with the reference's rules (leading '#' lines
  * skipped, whitespace tokens; src/Objects.cpp:338-458). Writes at most cap
- * descriptors, returns the number found in *n. */
+ * descriptors, returns the number found in *n.
+ * Besides CIRCLE and FILAMENT it reads one keyword of its own, added the way
+ * the reference's README (README.md:36-40) describes, for canopies of stalks
+ * of random length and stiffness:
+ *   CANOPY NUMBER STARTID STARTX STARTY SPACING_X SPACING_Y LENGTH_MIN
+ *          LENGTH_MAX HEIGHT ANGLE N_ELEMENTS|CONFORMING CLAMPED|SUPPORTED
+ *          DENSITY_PER_LENGTH YOUNG_MIN YOUNG_MAX SEED
+ * expands into NUMBER flexible FILAMENT descriptors (one body each, IDs from
+ * STARTID, stalk k at START + k*SPACING): length L = LENGTH_MIN +
+ * (LENGTH_MAX - LENGTH_MIN)*r, density DENSITY_PER_LENGTH*L, Young's modulus
+ * (YOUNG_MIN*(YOUNG_MAX/YOUNG_MIN)^r')*(L*L*L), where r, r' are the stalk's
+ * two draws of SplitMix64 seeded with SEED ((z >> 11) * 2^-53 per draw).
+ * With a mass ratio m and a bending stiffness S = EI/(rho U^2 L^3) at fluid
+ * density rho, inlet U, I = Dx H^3/12: DENSITY_PER_LENGTH = m rho / H and
+ * Young's modulus = 12 S rho U^2 L^3 / (Dx H^3). */
 int life_parse_geometry(const char* text, LifeBodyDesc* out, int32_t cap, int32_t* n);
 
 #ifdef __cplusplus

@@ -18,6 +18,7 @@ a reference case directory can be run unchanged.
 from __future__ import annotations
 
 import dataclasses
+import math
 import os
 import struct
 import subprocess
@@ -212,7 +213,83 @@ class Filament:
                 f"{'CLAMPED' if self.clamped else 'SUPPORTED'} {r(float(self.rho))} {r(float(self.E))}")
 
 
-Body = Union[Circle, Filament]
+def _splitmix64_draws(seed: int):
+    """SplitMix64 (Steele, Lea and Flood 2014), each output mapped to [0, 1)
+    with 53 bits: the draws of the CANOPY keyword."""
+    mask = (1 << 64) - 1
+    state = seed & mask
+    while True:
+        state = (state + 0x9E3779B97F4A7C15) & mask
+        z = state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & mask
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & mask
+        z ^= z >> 31
+        yield (z >> 11) * 2.0 ** -53
+
+
+@dataclass
+class Canopy:
+    """``CANOPY NUMBER STARTID STARTX STARTY SPACING_X SPACING_Y LENGTH_MIN
+    LENGTH_MAX HEIGHT ANGLE N_ELEMENTS|CONFORMING CLAMPED|SUPPORTED
+    DENSITY_PER_LENGTH YOUNG_MIN YOUNG_MAX SEED``: a geometry.config keyword of
+    this library (added as the reference's README, ``README.md:36-40``,
+    describes) for a row of flexible stalks of random length and stiffness.
+    Stalk k stands at (x + k dx, y + k dy); its length is
+    ``length_min + (length_max - length_min) r``, its density
+    ``density_per_length * L`` and its Young's modulus
+    ``(young_min * (young_max / young_min) ** r') * (L * L * L)``, with r, r' the
+    stalk's two draws of SplitMix64 seeded with ``seed``. ``expand`` gives the
+    FILAMENT bodies the library's parser (life_parse_geometry) builds."""
+
+    x: float
+    y: float
+    length_min: float
+    length_max: float
+    height: float
+    density_per_length: float
+    young_min: float
+    young_max: float
+    seed: int
+    angle_deg: float = 90.0
+    n_elements: Optional[int] = None
+    clamped: bool = True
+    ID: int = 0
+    number: int = 1
+    dx: float = 0.0
+    dy: float = 0.0
+
+    def config_line(self) -> str:
+        r = repr
+        nel = "CONFORMING" if self.n_elements is None else str(int(self.n_elements))
+        return (f"CANOPY {self.number} {self.ID} {r(float(self.x))} {r(float(self.y))} {r(float(self.dx))} "
+                f"{r(float(self.dy))} {r(float(self.length_min))} {r(float(self.length_max))} "
+                f"{r(float(self.height))} {r(float(self.angle_deg))} {nel} "
+                f"{'CLAMPED' if self.clamped else 'SUPPORTED'} {r(float(self.density_per_length))} "
+                f"{r(float(self.young_min))} {r(float(self.young_max))} {int(self.seed)}")
+
+    def expand(self) -> List["Filament"]:
+        draws = _splitmix64_draws(int(self.seed))
+        out = []
+        for k in range(int(self.number)):
+            rl, ry = next(draws), next(draws)
+            L = self.length_min + (self.length_max - self.length_min) * rl
+            E = (self.young_min * math.pow(self.young_max / self.young_min, ry)) * (L * L * L)
+            out.append(Filament(x=self.x + k * self.dx, y=self.y + k * self.dy, length=L, height=self.height,
+                                angle_deg=self.angle_deg, flexible=True, n_elements=self.n_elements,
+                                clamped=self.clamped, rho=self.density_per_length * L, E=E, ID=self.ID + k))
+        return out
+
+
+Body = Union[Circle, Filament, Canopy]
+
+
+def expand_bodies(bodies: Sequence) -> List[Body]:
+    """The body lines as the C-ABI takes them: CANOPY lines expanded into their
+    FILAMENT stalks (as life_parse_geometry does), other lines unchanged."""
+    out: List[Body] = []
+    for b in bodies:
+        out += b.expand() if isinstance(b, Canopy) else [b]
+    return out
 
 
 def geometry_config_text(bodies: Sequence[Body]) -> str:
@@ -255,6 +332,16 @@ def parse_geometry_config(text: str) -> List[Body]:
                                 clamped=(bc == "CLAMPED"), rho=rho, E=E, ID=ID, number=n,
                                 dx=dx, dy=dy))
             p += 15
+        elif kw == "CANOPY":
+            n, ID = int(toks[p + 1]), int(toks[p + 2])
+            x, y, dx, dy, lmin, lmax, H, ang = map(float, toks[p + 3:p + 11])
+            nel, bc = toks[p + 11], toks[p + 12]
+            dpl, ymin, ymax = map(float, toks[p + 13:p + 16])
+            out.append(Canopy(x=x, y=y, length_min=lmin, length_max=lmax, height=H, density_per_length=dpl,
+                              young_min=ymin, young_max=ymax, seed=int(toks[p + 16]), angle_deg=ang,
+                              n_elements=None if nel == "CONFORMING" else int(float(nel)),
+                              clamped=(bc == "CLAMPED"), ID=ID, number=n, dx=dx, dy=dy))
+            p += 17
         else:
             # The reference silently ignores an unknown keyword's line; we do not
             # guess a token count for it.

@@ -73,6 +73,8 @@ __global__ void k_ibm_clear(IbmScratch W, LatDev L) {
         W.force_ibm[s] = 0.0;
         W.force_ibm[L.S + s] = 0.0;
     }
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < W.nbodies; b += gridDim.x * blockDim.x)
+        W.body_box[b] = make_int4(0x7fffffff, -0x7fffffff, 0x7fffffff, -0x7fffffff);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *W.nsites = 0;
         *W.ntiles = 0;
@@ -86,6 +88,14 @@ __global__ void k_ibm_mark(MarkerDev M, IbmScratch W) {
     for (int s = 0; s < ns; s++) {
         const int tile = (M.sj[k * 9 + s] / TILE) * W.ntx + (M.si[k * 9 + s] / TILE);
         if (atomicCAS(&W.tile_flag[tile], 0u, 1u) == 0u) W.tiles[atomicAdd(W.ntiles, 1)] = tile;
+    }
+    if (ns > 0) {
+        const int4 bb = M.bbox[k];
+        int4* box = W.body_box + W.box_of[k];
+        atomicMin(&box->x, bb.x);
+        atomicMax(&box->y, bb.y);
+        atomicMin(&box->z, bb.z);
+        atomicMax(&box->w, bb.w);
     }
 }
 
@@ -112,10 +122,16 @@ __global__ void __launch_bounds__(256) k_ibm_spread(const typename S::T* __restr
         const int i = ti0 + (tid % TILE), j = tj0 + (tid / TILE);
         double ax = 0.0, ay = 0.0;
         bool touched = false;
-        for (int c0 = 0; c0 < M.n; c0 += 256) {
+        // bodies in body order, markers of a body in marker order: the
+        // contributions to a site are summed in global marker order
+        for (int bi = 0; bi < W.nbodies; bi++) {
+          const int4 box = W.body_box[bi];
+          if (box.x > ti0 + TILE - 1 || box.y < ti0 || box.z > tj0 + TILE - 1 || box.w < tj0) continue;
+          const int kend = W.body_start[bi + 1];
+          for (int c0 = W.body_start[bi]; c0 < kend; c0 += 256) {
             const int k = c0 + tid;
             bool hit = false;
-            if (k < M.n) {
+            if (k < kend) {
                 const int4 bb = M.bbox[k];
                 hit = bb.x <= ti0 + TILE - 1 && bb.y >= ti0 && bb.z <= tj0 + TILE - 1 && bb.w >= tj0;
             }
@@ -157,6 +173,7 @@ __global__ void __launch_bounds__(256) k_ibm_spread(const typename S::T* __restr
                     }
             }
             __syncthreads();
+          }
         }
         if (tid == 0) {
             W.tile_flag[tile] = 0u;
@@ -243,7 +260,13 @@ cudaError_t launch_ibm_spread(const void* A, void* B, const LatDev& L, int t, co
     k_ibm_clear<<<8, 256, 0, s>>>(W, L);
     if (M.n > 0) {
         k_ibm_mark<<<(M.n + 127) / 128, 128, 0, s>>>(M, W);
-        int grid = W.max_tiles < 4 * 152 ? W.max_tiles : 4 * 152;
+        // four CTAs per SM of this device, at most one per tile
+        static int sms[64] = {0};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev >= 0 && dev < 64 && sms[dev] == 0) cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+        const int nsm = (dev >= 0 && dev < 64 && sms[dev] > 0) ? sms[dev] : 1;
+        int grid = W.max_tiles < 4 * nsm ? W.max_tiles : 4 * nsm;
         if (grid < 1) grid = 1;
         TypedPtr<void> Ap{A}, Bp{B};
         IBM_DISPATCH(k_ibm_spread, grid, 256, Ap, Bp, L, t, M, W);

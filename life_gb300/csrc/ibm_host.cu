@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "fem_kernels.h"
@@ -89,6 +90,32 @@ int upload_markers(LifeCase* c) {
     CK(cudaMemsetAsync(W.nsites_prev, 0, sizeof(int), c->stream));
     CK(cudaMemsetAsync(W.tile_flag, 0, sizeof(unsigned) * W.max_tiles, c->stream));
     CK(cudaMemsetAsync(W.ntiles, 0, sizeof(int), c->stream));
+    // bodies as contiguous marker ranges (markers are stored body by body);
+    // one range over all markers if that ever does not hold
+    std::vector<int> start(1, 0);
+    bool contiguous = true;
+    for (int k = 1; k < n; k++) {
+        const int b0 = c->obj.m[k - 1].body, b1 = c->obj.m[k].body;
+        if (b1 != b0) {
+            if (b1 < b0) contiguous = false;
+            start.push_back(k);
+        }
+    }
+    start.push_back(n);
+    if (!contiguous || n == 0) start = {0, n};
+    W.nbodies = (int)start.size() - 1;
+    std::vector<int> box_of((size_t)std::max(n, 1), 0);
+    for (int r = 0; r < W.nbodies; r++)
+        for (int k = start[r]; k < start[r + 1]; k++) box_of[k] = r;
+    int *d_start = nullptr, *d_box_of = nullptr;
+    if ((rc = alloc_t(c, &d_start, start.size())) || (rc = alloc_t(c, &d_box_of, box_of.size())) ||
+        (rc = alloc_t(c, &W.body_box, (size_t)W.nbodies)))
+        return rc;
+    W.body_start = d_start;
+    W.box_of = d_box_of;
+    CK(cudaMemcpyAsync(d_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(d_box_of, box_of.data(), sizeof(int) * box_of.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     if ((rc = alloc_t(c, &c->d_fsi, 1)) || (rc = alloc_t(c, &c->d_status, 4))) return rc;
     FsiScalars f{};
     f.relax = c->p.relaxMax;
@@ -218,6 +245,17 @@ extern "C" int life_case_total_force(LifeCase* c, double* fx, double* fy) {
     return LIFE_OK;
 }
 
+// SplitMix64 (Steele, Lea and Flood 2014), mapped to [0, 1) with 53 bits:
+// the draws of the CANOPY keyword.
+static double canopy_draw(uint64_t& state) {
+    state += 0x9E3779B97F4A7C15ull;
+    uint64_t z = state;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * 0x1p-53;
+}
+
 extern "C" int life_parse_geometry(const char* text, LifeBodyDesc* out, int32_t cap, int32_t* n) {
     if (!text || !n) return set_error(LIFE_ERR_INVALID, "NULL argument");
     // Skip the leading comment lines (src/Objects.cpp:338-353).
@@ -273,6 +311,49 @@ extern "C" int life_parse_geometry(const char* text, LifeBodyDesc* out, int32_t 
                 d.rho = std::stod(tok[q + 13]);
                 d.E = std::stod(tok[q + 14]);
                 q += 15;
+            } else if (tok[q] == "CANOPY") {
+                // CANOPY NUMBER STARTID STARTX STARTY SPACING_X SPACING_Y
+                //        LENGTH_MIN LENGTH_MAX HEIGHT ANGLE N_ELEMENTS|CONFORMING
+                //        CLAMPED|SUPPORTED DENSITY_PER_LENGTH YOUNG_MIN YOUNG_MAX SEED
+                // NUMBER flexible stalks, stalk k at START + k SPACING with
+                // length L_k = LMIN + (LMAX - LMIN) r, density DPL L_k and
+                // Young's modulus Y_k L_k^3, Y_k = YMIN (YMAX / YMIN)^r'
+                // (log-uniform), r and r' the next two draws of SplitMix64
+                // seeded with SEED; each stalk becomes one FILAMENT body.
+                if (q + 17 > tok.size()) return set_error(LIFE_ERR_GEOMETRY, "truncated CANOPY line");
+                const int number = std::stoi(tok[q + 1]), id0 = std::stoi(tok[q + 2]);
+                const double sx = std::stod(tok[q + 3]), sy = std::stod(tok[q + 4]);
+                const double dx = std::stod(tok[q + 5]), dy = std::stod(tok[q + 6]);
+                const double lmin = std::stod(tok[q + 7]), lmax = std::stod(tok[q + 8]);
+                const double height = std::stod(tok[q + 9]), angle = std::stod(tok[q + 10]);
+                const int nel = tok[q + 11] == "CONFORMING" ? 0 : (int)std::stod(tok[q + 11]);
+                const int clamped = tok[q + 12] == "CLAMPED" ? 1 : 0;
+                const double dpl = std::stod(tok[q + 13]);
+                const double ymin = std::stod(tok[q + 14]), ymax = std::stod(tok[q + 15]);
+                uint64_t state = std::stoull(tok[q + 16]);
+                if (number < 0 || !(lmin > 0.0) || lmax < lmin || !(ymin > 0.0) || ymax < ymin)
+                    return set_error(LIFE_ERR_GEOMETRY, "bad CANOPY parameters");
+                q += 17;
+                for (int k = 0; k < number; k++) {
+                    LifeBodyDesc s{};
+                    s.kind = LIFE_BODY_FILAMENT;
+                    s.number = 1;
+                    s.id = id0 + k;
+                    s.x = sx + k * dx;
+                    s.y = sy + k * dy;
+                    const double rl = canopy_draw(state), ry = canopy_draw(state);
+                    s.length = lmin + (lmax - lmin) * rl;
+                    s.height = height;
+                    s.angle_deg = angle;
+                    s.flexible = 1;
+                    s.n_elements = nel;
+                    s.clamped = clamped;
+                    s.rho = dpl * s.length;
+                    s.E = (ymin * std::pow(ymax / ymin, ry)) * (s.length * s.length * s.length);
+                    if (out && count < cap) out[count] = s;
+                    count++;
+                }
+                continue;
             } else {
                 return set_error(LIFE_ERR_GEOMETRY, "unknown geometry keyword '" + tok[q] + "'");
             }

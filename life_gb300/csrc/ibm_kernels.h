@@ -33,6 +33,13 @@ struct IbmScratch {
     int* tiles;               // touched tiles
     int* ntiles;
     int ntx, nty, max_tiles;
+    // Bodies as contiguous marker ranges [body_start[b], body_start[b+1])
+    // and the bounding box of their support this step (imin, imax, jmin,
+    // jmax): a tile of the spread scans only the bodies whose box reaches it.
+    int nbodies;
+    const int* body_start;    // [nbodies + 1]
+    const int* box_of;        // [n] the range of each marker
+    int4* body_box;           // [nbodies]
 };
 
 // Population buffers are untyped; their element type follows L.prec.

@@ -361,16 +361,24 @@ struct PairWord<StoreF16> {
     __device__ static __forceinline__ W load(const __half* P, size_t idx) {
         return __ldg(reinterpret_cast<const unsigned*>(P) + (idx >> 1));
     }
+    // the word beyond the warp that lane 0 (the pair to the left) or lane 31
+    // (to the right) needs; issued with the other loads
+    __device__ static __forceinline__ W edge_left(const __half* P, size_t idx, bool take) {
+        return take ? load(P, idx - 2) : 0u;
+    }
+    __device__ static __forceinline__ W edge_right(const __half* P, size_t idx, bool take) {
+        return take ? load(P, idx + 2) : 0u;
+    }
     // (prev.hi, cur.lo): the pair one site to the left
-    __device__ static __forceinline__ W left(W cur, int lane, const __half* P, size_t idx, bool has_left) {
+    __device__ static __forceinline__ W left(W cur, W edge, int lane) {
         W prev = __shfl_up_sync(0xffffffffu, cur, 1);
-        if (lane == 0) prev = has_left ? load(P, idx - 2) : 0u;
+        if (lane == 0) prev = edge;
         return __byte_perm(prev, cur, 0x5432);
     }
     // (cur.hi, next.lo): the pair one site to the right
-    __device__ static __forceinline__ W right(W cur, int lane, const __half* P, size_t idx, bool has_right) {
+    __device__ static __forceinline__ W right(W cur, W edge, int lane) {
         W next = __shfl_down_sync(0xffffffffu, cur, 1);
-        if (lane == 31) next = has_right ? load(P, idx + 2) : 0u;
+        if (lane == 31) next = edge;
         return __byte_perm(cur, next, 0x5432);
     }
     __device__ static __forceinline__ V2 dev(W w, int v) {
@@ -389,14 +397,20 @@ struct PairWord<StoreF32> {
     __device__ static __forceinline__ W load(const float* P, size_t idx) {
         return __ldg(reinterpret_cast<const float2*>(P) + (idx >> 1));
     }
-    __device__ static __forceinline__ W left(W cur, int lane, const float* P, size_t idx, bool has_left) {
+    __device__ static __forceinline__ W edge_left(const float* P, size_t idx, bool take) {
+        return make_float2(take ? __ldg(P + idx - 1) : 0.0f, 0.0f);
+    }
+    __device__ static __forceinline__ W edge_right(const float* P, size_t idx, bool take) {
+        return make_float2(take ? __ldg(P + idx + 2) : 0.0f, 0.0f);
+    }
+    __device__ static __forceinline__ W left(W cur, W edge, int lane) {
         float py = __shfl_up_sync(0xffffffffu, cur.y, 1);
-        if (lane == 0) py = has_left ? P[idx - 1] : 0.0f;
+        if (lane == 0) py = edge.x;
         return make_float2(py, cur.x);
     }
-    __device__ static __forceinline__ W right(W cur, int lane, const float* P, size_t idx, bool has_right) {
+    __device__ static __forceinline__ W right(W cur, W edge, int lane) {
         float nx = __shfl_down_sync(0xffffffffu, cur.x, 1);
-        if (lane == 31) nx = has_right ? P[idx + 2] : 0.0f;
+        if (lane == 31) nx = edge.x;
         return make_float2(cur.y, nx);
     }
     __device__ static __forceinline__ V2 dev(W w, int) { return V2{w}; }
@@ -415,14 +429,20 @@ __device__ __forceinline__ void interior_pair_lowp(const typename S::T* __restri
     // the loads of lanes past the row stay inside the row's pitch
     const int sc = s < L.pitch - 2 ? s : L.pitch - 2;
     const bool has_left = sc >= 2, has_right = sc + 2 <= L.pitch - 2;
-    typename P::W w[9];
+    // every load first (the pairs and the words beyond the warp), then the
+    // shuffles that shift the x-streaming planes
+    typename P::W w[9], edge[9];
 #pragma unroll
     for (int v = 0; v < 9; v++) {
         const size_t idx = (size_t)v * L.S + (size_t)(j - cy_of(v)) * L.pitch + sc;
-        const typename P::W cur = P::load(A, idx);
-        if (cx_of(v) == 0) w[v] = cur;
-        else if (cx_of(v) > 0) w[v] = P::left(cur, lane, A, idx, has_left);
-        else w[v] = P::right(cur, lane, A, idx, has_right);
+        w[v] = P::load(A, idx);
+        if (cx_of(v) > 0) edge[v] = P::edge_left(A, idx, lane == 0 && has_left);
+        if (cx_of(v) < 0) edge[v] = P::edge_right(A, idx, lane == 31 && has_right);
+    }
+#pragma unroll
+    for (int v = 0; v < 9; v++) {
+        if (cx_of(v) > 0) w[v] = P::left(w[v], edge[v], lane);
+        if (cx_of(v) < 0) w[v] = P::right(w[v], edge[v], lane);
     }
     const bool pair_ok = s >= 2 && s + 1 <= L.Nx - 2 && !(L.convective && s + 1 >= L.Nx - 3);
     if (!pair_ok) {
@@ -453,7 +473,7 @@ __device__ __forceinline__ void interior_pair_lowp(const typename S::T* __restri
 
 // k_step_lowp with two sites per thread (512 sites per block).
 template <bool CM, class S>
-__global__ void __launch_bounds__(256, 4) k_step_lowp2(const typename S::T* __restrict__ A,
+__global__ void __launch_bounds__(256, CM ? 4 : 5) k_step_lowp2(const typename S::T* __restrict__ A,
                                                        typename S::T* __restrict__ B, LatDev L, int t, int pb,
                                                        int bx, unsigned bx_m) {
     t = step_t(L, t);
@@ -482,7 +502,7 @@ static int step_sites(int prec) {
         forced = (e && (e[0] == '1' || e[0] == '2')) ? e[0] - '0' : 0;
     }
     if (forced) return forced;
-    return prec == LIFE_PREC_F16 ? 2 : 2;
+    return prec == LIFE_PREC_F16 ? 1 : 1;
 }
 
 static unsigned div_magic(int bx, long long bmax) {

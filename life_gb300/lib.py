@@ -18,7 +18,7 @@ import numpy as np
 
 from .abi import (ERRORS, LifeBatchInfo, LifeCaseInfo, LifeRequestInfo, LifeServerConfig, LifeServerStats,
                   LifeStatus, body_structs, params_struct)
-from .case import CaseParams
+from .case import CaseParams, expand_bodies
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "liblife_gb300.so")
@@ -131,6 +131,7 @@ class Case:
         self.params = params
         self._owned = _handle is None
         if _handle is None:
+            bodies = expand_bodies(bodies)
             ps = params_struct(params)
             bs = body_structs(bodies)
             h = C.c_void_p()
@@ -337,7 +338,7 @@ class Batch:
 
     def __init__(self, cases: Sequence):
         L = lib()
-        self._cases = [(p, list(b)) for p, b in cases]
+        self._cases = [(p, expand_bodies(b)) for p, b in cases]
         n = len(self._cases)
         ps = (type(params_struct(self._cases[0][0])) * n)()
         for k, (p, _) in enumerate(self._cases):
@@ -443,6 +444,7 @@ class Server:
         self.close()
 
     def submit(self, params: CaseParams, bodies: Sequence, steps: int) -> int:
+        bodies = expand_bodies(bodies)
         ps = params_struct(params)
         bs = body_structs(bodies)
         rid = C.c_int64()

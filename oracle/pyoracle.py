@@ -15,7 +15,7 @@ from typing import Dict, Optional, Sequence
 import numpy as np
 
 from life_gb300.abi import body_structs, params_struct
-from life_gb300.case import CaseParams
+from life_gb300.case import CaseParams, expand_bodies
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liblife_oracle.so")
@@ -90,6 +90,7 @@ class Oracle:
     def __init__(self, params: CaseParams, bodies: Sequence = (), trig: str = "libm"):
         self._L = L = lib(trig)
         self.params = params
+        bodies = expand_bodies(bodies)
         ps = params_struct(params)
         bs = body_structs(bodies)
         h = C.c_void_p()
