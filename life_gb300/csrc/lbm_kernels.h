@@ -30,6 +30,8 @@ struct VtiScale {
 // state after step t (initial: the state before the first step).
 cudaError_t launch_export_vti(const void* P, const LatDev& L, int t, bool initial, const VtiScale& V, double* dens,
                               double* pres, double* vel, cudaStream_t s);
+// Bounded waits of the TMA-staged step kernel that gave up (0 normally).
+int tma_timeouts();
 cudaError_t launch_maxvel(const void* P, const LatDev& L, int t, unsigned long long* out, cudaStream_t s);
 
 // One case of a batched interior launch: its lattice view and buffers for the

@@ -25,12 +25,16 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
+
+#include <cudaTypedefs.h>
 
 #include "collide_cm.cuh"
 #include "lbm_device.cuh"
 #include "lbm_kernels.h"
+#include "tma.cuh"
 
 namespace life {
 
@@ -183,6 +187,10 @@ __device__ __forceinline__ void collide_dev32(const T g[9], T dr, T rho, T mx, T
     }
 }
 
+template <bool CM, bool FORCED, class S>
+__device__ __forceinline__ void finish_site_lowp(const float g[9], typename S::T* __restrict__ B, const LatDev& L,
+                                                 int t, int i, int j);
+
 // One interior site, reduced-precision storage. Sites on a boundary-condition
 // wall are left to the perimeter kernel.
 template <bool CM, bool FORCED, class S>
@@ -205,6 +213,15 @@ __device__ __forceinline__ void interior_site_lowp_f(const typename S::T* __rest
             g[v] = S::dev(A[(size_t)v * L.S + (size_t)sj * L.pitch + si], v);
         }
     }
+    finish_site_lowp<CM, FORCED, S>(g, B, L, t, i, j);
+}
+
+// The rest of an interior site once its nine pulled deviations g are in
+// registers: moments, outlet columns, collision, store.
+template <bool CM, bool FORCED, class S>
+__device__ __forceinline__ void finish_site_lowp(const float g[9], typename S::T* __restrict__ B, const LatDev& L,
+                                                 int t, int i, int j) {
+    const size_t base = (size_t)j * L.pitch + i;
     float Fxd = 0.0f, Fyd = 0.0f, Gxd = 0.0f, Gyd = 0.0f;
     if (FORCED) {
         force_xy_at_f(L, t, Fxd, Fyd);
@@ -493,16 +510,211 @@ __global__ void __launch_bounds__(256, CM ? 4 : 5) k_step_lowp2(const typename S
     else interior_pair_lowp<CM, false, S>(A, B, L, t, s, j);
 }
 
-// Which step kernel a reduced-precision form uses: 1 = k_step_lowp (one site
-// per thread), 2 = k_step_lowp2 (two). LIFE_STEP_SITES=1|2 overrides.
-static int step_sites(int prec) {
-    static int forced = -1;
-    if (forced < 0) {
-        const char* e = getenv("LIFE_STEP_SITES");
-        forced = (e && (e[0] == '1' || e[0] == '2')) ? e[0] - '0' : 0;
+// ---- TMA-staged tiles ---------------------------------------------------
+//
+// A persistent CTA walks the interior tiles (W x H sites of rows 1..Ny-2 and
+// columns 1..Nx-2). For each tile one thread issues nine bulk tensor copies
+// (one per population plane) of the tile plus a halo of one row above and
+// below and HALO sites left and right (HALO keeps the box start on a 16-byte
+// boundary), into one of two shared-memory stages, while the CTA computes the
+// tile of the other stage; the copies' completion is counted on the stage's
+// mbarrier. The sites then read their nine pulled populations from shared
+// memory and finish exactly as in the one-site path (finish_site_lowp), so
+// the results are the same bits. The first blocks of the grid take the
+// boundary-condition sites and the periodic edge sites, as in k_step_lowp.
+template <class S>
+struct TmaTile;
+template <>
+struct TmaTile<StoreF16> {
+    static constexpr int W = 128, H = 8, HALO = 8, ELEM = 2;
+    static constexpr CUtensorMapDataType DTYPE = CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+};
+template <>
+struct TmaTile<StoreF32> {
+    static constexpr int W = 128, H = 4, HALO = 4, ELEM = 4;
+    static constexpr CUtensorMapDataType DTYPE = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+};
+template <class S>
+struct TmaShape {
+    static constexpr int Wb = TmaTile<S>::W + 2 * TmaTile<S>::HALO, Hb = TmaTile<S>::H + 2;
+    static constexpr int BOX = Wb * Hb * TmaTile<S>::ELEM;  // bytes of one plane's box
+    static constexpr int PLANE = (BOX + 127) / 128 * 128;   // 128-byte aligned plane slots
+    static constexpr int STAGE = 9 * PLANE;
+    // two stages, two mbarriers and a flag, and slack to align the stages to
+    // 128 bytes (the bulk tensor copies' shared-memory alignment)
+    static constexpr int SMEM = 2 * STAGE + 128 + 128;
+};
+
+// Waits that gave up (never expected; the host turns a non-zero count into
+// LIFE_ERR_TIMEOUT).
+__device__ int g_tma_timeouts;
+
+__device__ __forceinline__ bool perimeter_ij(const LatDev& L, int q, int& i, int& j) {
+    const int Nx = L.Nx, Ny = L.Ny;
+    if (q < Nx) { i = q; j = 0; }
+    else if (q < 2 * Nx) { i = q - Nx; j = Ny - 1; }
+    else if (q < 2 * Nx + (Ny - 2)) { i = 0; j = q - 2 * Nx + 1; }
+    else if (q < 2 * Nx + 2 * (Ny - 2)) { i = Nx - 1; j = q - 2 * Nx - (Ny - 2) + 1; }
+    else return false;
+    return true;
+}
+
+template <bool CM, bool FORCED, class S>
+__device__ __forceinline__ void tma_tile_sites(const unsigned char* stage, typename S::T* __restrict__ B,
+                                               const LatDev& L, int t, int i0, int j0) {
+    using TT = TmaTile<S>;
+    using SH = TmaShape<S>;
+    const int ii = (int)threadIdx.x % TT::W;
+    const int i = i0 + ii;
+    if (i < 1 || i > L.Nx - 2) return;
+    for (int jj = (int)threadIdx.x / TT::W; jj < TT::H; jj += (int)blockDim.x / TT::W) {
+        const int j = j0 + jj;
+        if (j > L.Ny - 2) break;
+        float g[9];
+#pragma unroll
+        for (int v = 0; v < 9; v++) {
+            const typename S::T* plane = reinterpret_cast<const typename S::T*>(stage + v * SH::PLANE);
+            g[v] = S::dev(plane[(jj + 1 - cy_of(v)) * SH::Wb + (ii + TT::HALO - cx_of(v))], v);
+        }
+        finish_site_lowp<CM, FORCED, S>(g, B, L, t, i, j);
     }
-    if (forced) return forced;
-    return prec == LIFE_PREC_F16 ? 1 : 1;
+}
+
+template <bool CM, class S>
+__global__ void __launch_bounds__(256) k_step_tma(const __grid_constant__ CUtensorMap tm,
+                                                  const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
+                                                  LatDev L, int t, int pb, int tiles_x, int ntiles) {
+    using TT = TmaTile<S>;
+    using SH = TmaShape<S>;
+    t = step_t(L, t);
+    if ((int)blockIdx.x < pb) {
+        // boundary-condition sites; an edge site of a periodic wall is an
+        // interior site with wrapped neighbours (each call skips the other kind)
+        const int q = blockIdx.x * blockDim.x + threadIdx.x;
+        perimeter_site_call<CM, S>(A, B, L, t, q);
+        int i, j;
+        if (perimeter_ij(L, q, i, j)) interior_site_lowp<CM, S>(A, B, L, t, i, j);
+        return;
+    }
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
+                                                           ~static_cast<uintptr_t>(127));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * SH::STAGE);
+    int& s_ok = *reinterpret_cast<int*>(smem + 2 * SH::STAGE + 16);
+    const int cta = (int)blockIdx.x - pb, ncta = (int)gridDim.x - pb;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    auto issue = [&](int tile, int st) {
+        const int i0 = (tile % tiles_x) * TT::W, j0 = 1 + (tile / tiles_x) * TT::H;
+        mbar_arrive_expect_tx(&bar[st], 9u * SH::BOX);
+#pragma unroll 1
+        for (int v = 0; v < 9; v++)
+            tma_load_3d(smem + st * SH::STAGE + v * SH::PLANE, &tm, i0 - TT::HALO, j0 - 1, v, &bar[st]);
+    };
+    if (threadIdx.x == 0 && cta < ntiles) issue(cta, 0);
+    const bool forced = lattice_forced(L);
+    int k = 0;
+    for (int tile = cta; tile < ntiles; tile += ncta, k++) {
+        const int st = k & 1;
+        const bool next = tile + ncta < ntiles;
+        if (threadIdx.x == 0) {
+            if (next) {
+                fence_proxy_async_smem();
+                issue(tile + ncta, st ^ 1);
+            }
+            s_ok = mbar_wait_bounded(&bar[st], (unsigned)(k >> 1) & 1u, 1u << 22) ? 1 : 0;
+            if (!s_ok) {
+                // give the copy in flight into the other stage time to land
+                // before the CTA (and its shared memory) goes away
+                if (next) mbar_wait_bounded(&bar[st ^ 1], (unsigned)((k + 1) >> 1) & 1u, 1u << 22);
+                atomicAdd(&g_tma_timeouts, 1);
+            }
+        }
+        __syncthreads();
+        if (!s_ok) return;
+        const int i0 = (tile % tiles_x) * TT::W, j0 = 1 + (tile / tiles_x) * TT::H;
+        if (forced) tma_tile_sites<CM, true, S>(smem + st * SH::STAGE, B, L, t, i0, j0);
+        else tma_tile_sites<CM, false, S>(smem + st * SH::STAGE, B, L, t, i0, j0);
+        __syncthreads();
+    }
+}
+
+// The tensor map of one population buffer: dims (pitch, Ny, 9 planes), box
+// (Wb, Hb, 1), no swizzle, zero fill outside the buffer.
+template <class S>
+static cudaError_t plane_tensor_map(CUtensorMap* tm, const void* base, const LatDev& L) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    using TT = TmaTile<S>;
+    using SH = TmaShape<S>;
+    const cuuint64_t dims[3] = {(cuuint64_t)L.pitch, (cuuint64_t)L.Ny, 9};
+    const cuuint64_t strides[2] = {(cuuint64_t)L.pitch * TT::ELEM, (cuuint64_t)L.S * TT::ELEM};
+    const cuuint32_t box[3] = {(cuuint32_t)SH::Wb, (cuuint32_t)SH::Hb, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = encode(tm, TT::DTYPE, 3, const_cast<void*>(base), dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+template <bool CM, class S>
+static cudaError_t launch_step_tma_t(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
+    using TT = TmaTile<S>;
+    using SH = TmaShape<S>;
+    static int per_sm[64] = {0}, sms[64] = {0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!per_sm[dev]) {
+        e = cudaFuncSetAttribute(k_step_tma<CM, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, SH::SMEM);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[dev], k_step_tma<CM, S>, 256, SH::SMEM);
+        if (e != cudaSuccess) return e;
+        if (per_sm[dev] < 1) per_sm[dev] = 1;
+    }
+    CUtensorMap tm;
+    if ((e = plane_tensor_map<S>(&tm, A, L)) != cudaSuccess) return e;
+    const int n = 2 * L.Nx + 2 * (L.Ny - 2);
+    const int pb = (n + 255) / 256;
+    const int tiles_x = (L.Nx - 1 + TT::W - 1) / TT::W, tiles_y = (L.Ny - 2 + TT::H - 1) / TT::H;
+    const int ntiles = tiles_x * tiles_y;
+    const int persistent = std::min(ntiles, sms[dev] * per_sm[dev]);
+    k_step_tma<CM, S><<<pb + std::max(persistent, 1), 256, SH::SMEM, s>>>(
+        tm, (const typename S::T*)A, (typename S::T*)B, L, t, pb, tiles_x, ntiles);
+    return cudaGetLastError();
+}
+
+int tma_timeouts() {
+    int h = 0;
+    if (cudaMemcpyFromSymbol(&h, g_tma_timeouts, sizeof h) != cudaSuccess) return -1;
+    return h;
+}
+
+// Which step kernel a reduced-precision case uses, LIFE_STEP_KERNEL:
+// "site" (k_step_lowp, one site per thread), "pair" (k_step_lowp2) or "tma"
+// (k_step_tma, TMA-staged tiles; the default).
+enum { STEP_SITE = 1, STEP_PAIR = 2, STEP_TMA = 3 };
+static int step_kernel(int) {
+    static int choice = 0;
+    if (!choice) {
+        const char* e = getenv("LIFE_STEP_KERNEL");
+        choice = STEP_TMA;
+        if (e && !strcmp(e, "site")) choice = STEP_SITE;
+        else if (e && !strcmp(e, "pair")) choice = STEP_PAIR;
+    }
+    return choice;
 }
 
 static unsigned div_magic(int bx, long long bmax) {
@@ -514,7 +726,13 @@ static unsigned div_magic(int bx, long long bmax) {
 }
 
 cudaError_t launch_step_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
-    if (step_sites(L.prec) == 2) {
+    const int kind = step_kernel(L.prec);
+    if (kind == STEP_TMA) {
+        if (L.prec == LIFE_PREC_F32)
+            return L.cm ? launch_step_tma_t<true, StoreF32>(A, B, L, t, s) : launch_step_tma_t<false, StoreF32>(A, B, L, t, s);
+        return L.cm ? launch_step_tma_t<true, StoreF16>(A, B, L, t, s) : launch_step_tma_t<false, StoreF16>(A, B, L, t, s);
+    }
+    if (kind == STEP_PAIR) {
         const int n = 2 * L.Nx + 2 * (L.Ny - 2);
         const int pb = (n + 255) / 256, bx = (L.Nx + 511) / 512;
         const unsigned grid = (unsigned)(pb + bx * L.Ny);

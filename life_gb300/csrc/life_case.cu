@@ -407,6 +407,12 @@ extern "C" int life_case_destroy(LifeCase* c) {
 }
 
 static int check_device_status(LifeCase* c) {
+    if (c->p.precision != LIFE_PREC_F64 && tma_timeouts() > 0 && c->status_code == 0) {
+        c->status_code = LIFE_ERR_TIMEOUT;
+        c->status_t = c->t;
+        c->status_msg = "a shared-memory tile copy of the step kernel did not complete";
+        return LIFE_OK;
+    }
     if (!c->d_status) return LIFE_OK;
     int h[4];
     CK(cudaMemcpyAsync(h, c->d_status, sizeof(h), cudaMemcpyDeviceToHost, c->stream));

@@ -1,10 +1,10 @@
 """The one-launch step kernels of the reduced-precision forms (lattices of
 2^22 sites or more) against each other and against the separate perimeter +
-interior kernels of the host-driven loop: k_step_lowp2 (two x-adjacent sites
-per thread, packed FP32 arithmetic, shuffled pair loads), k_step_lowp (one
-site per thread) and LIFE_CASE_HOSTLOOP=1 must give the same bits after N
-steps, for BGK and central moments, with and without a step force, with a
-convective outlet, periodic x walls and an odd width (a lone last site)."""
+interior kernels of the host-driven loop: k_step_tma (TMA-staged tiles, the
+default), k_step_lowp (one site per thread, LIFE_STEP_KERNEL=site) and
+LIFE_CASE_HOSTLOOP=1 must give the same bits after N steps, for BGK and
+central moments, with and without a step force, with a convective outlet,
+periodic x walls and an odd width."""
 import os
 import subprocess
 import sys
@@ -51,7 +51,8 @@ def digest(kind, prec, env):
 def test_step_kernels_bit_identical(kind, prec):
     from life_gb300.build import build
     build()
-    two = digest(kind, prec, {"LIFE_STEP_SITES": "2"})
-    one = digest(kind, prec, {"LIFE_STEP_SITES": "1"})
+    tma = digest(kind, prec, {})
+    one = digest(kind, prec, {"LIFE_STEP_KERNEL": "site"})
     host = digest(kind, prec, {"LIFE_CASE_HOSTLOOP": "1"})
-    assert two == one == host
+    assert one == host, "one-site step kernel vs host-driven kernels"
+    assert tma == one, "TMA-staged step kernel vs one-site step kernel"
