@@ -38,37 +38,8 @@
 
 namespace life {
 
-// Two sites' FP32 arithmetic in one instruction: the packed FADD2 / FMUL2 /
-// FFMA2 of sm_100 (__fadd2_rn, __fmul2_rn, __ffma2_rn). Each lane is an IEEE
-// round-to-nearest FP32 operation, so each lane of a V2 computation gives,
-// bit for bit, the float computation written with the same expressions. The
-// collision below is written once as a template over float and V2.
-struct V2 {
-    float2 v;
-};
-__device__ __forceinline__ V2 v2(float a) { return V2{make_float2(a, a)}; }
-__device__ __forceinline__ V2 v2(float a, float b) { return V2{make_float2(a, b)}; }
-__device__ __forceinline__ V2 operator+(V2 a, V2 b) { return V2{__fadd2_rn(a.v, b.v)}; }
-__device__ __forceinline__ V2 operator-(V2 a) { return V2{make_float2(-a.v.x, -a.v.y)}; }
-__device__ __forceinline__ V2 operator-(V2 a, V2 b) { return a + (-b); }  // a - b == a + (-b) in IEEE
-__device__ __forceinline__ V2 operator*(V2 a, V2 b) { return V2{__fmul2_rn(a.v, b.v)}; }
-__device__ __forceinline__ V2 operator+(float a, V2 b) { return v2(a) + b; }
-__device__ __forceinline__ V2 operator+(V2 a, float b) { return a + v2(b); }
-__device__ __forceinline__ V2 operator-(float a, V2 b) { return v2(a) - b; }
-__device__ __forceinline__ V2 operator-(V2 a, float b) { return a - v2(b); }
-__device__ __forceinline__ V2 operator*(float a, V2 b) { return v2(a) * b; }
-__device__ __forceinline__ V2 operator*(V2 a, float b) { return a * v2(b); }
-__device__ __forceinline__ V2 fmaf(V2 a, V2 b, V2 c) { return V2{__ffma2_rn(a.v, b.v, c.v)}; }
-__device__ __forceinline__ V2 fmaf(float a, V2 b, V2 c) { return fmaf(v2(a), b, c); }
-__device__ __forceinline__ V2 fmaf(V2 a, float b, V2 c) { return fmaf(a, v2(b), c); }
-__device__ __forceinline__ V2 fmaf(V2 a, V2 b, float c) { return fmaf(a, b, v2(c)); }
-__device__ __forceinline__ V2 fmaf(float a, float b, V2 c) { return fmaf(v2(a), v2(b), c); }
-__device__ __forceinline__ V2 fmaf(float a, V2 b, float c) { return fmaf(v2(a), b, v2(c)); }
-__device__ __forceinline__ V2 fmaf(V2 a, float b, float c) { return fmaf(a, v2(b), v2(c)); }
-using ::fmaf;
 template <class T> __device__ __forceinline__ T zero_of();
 template <> __device__ __forceinline__ float zero_of<float>() { return 0.0f; }
-template <> __device__ __forceinline__ V2 zero_of<V2>() { return v2(0.0f); }
 
 template <class T>
 __device__ __forceinline__ void e1d(T u, T e[3], float w[3], T d[3]) {
@@ -99,7 +70,6 @@ __device__ __forceinline__ T cdot(int v, T a, T b) {
 
 // FORCED = false: the force of this step is zero everywhere (no gravity, no
 // Womersley term), so every forcing term is an exact zero and is not formed.
-// T = float: one site; T = V2: two sites, lane by lane the same operations.
 template <bool CM, bool FORCED, class T>
 __device__ __forceinline__ void collide_dev32(const T g[9], T dr, T rho, T mx, T my, T ux, T uy, float Gx, float Gy,
                                               float omega, T gs[9]) {
@@ -357,159 +327,6 @@ __global__ void __launch_bounds__(256, 6) k_step_lowp(const typename S::T* __res
     interior_site_lowp<CM, S>(A, B, L, t, i, j);
 }
 
-// ---- two x-adjacent sites per thread --------------------------------------
-//
-// A thread takes the sites (s, s+1), s even, and moves each population plane
-// as one aligned word per pair: the stored pair at (s, s+1) of the source row
-// (two halves or two floats). Populations streaming along x need the pair
-// shifted by one site: (s-1, s) for c_x = +1 and (s+1, s+2) for c_x = -1; a
-// warp covers 64 consecutive sites of one row, so each lane takes the missing
-// half of its pair from its neighbour lane's word (a shuffle), and lanes 0 and
-// 31 load the one word beyond the warp. The collision runs on both sites at
-// once in packed FP32 (V2), lane by lane the operations of the one-site path,
-// so the results are those of interior_site_lowp bit for bit. Pairs that touch
-// a boundary column, a periodic wrap or the convective outlet's columns take
-// the one-site path.
-template <class S>
-struct PairWord;
-template <>
-struct PairWord<StoreF16> {
-    using W = unsigned;  // (site s, site s+1) as two halves
-    __device__ static __forceinline__ W load(const __half* P, size_t idx) {
-        return __ldg(reinterpret_cast<const unsigned*>(P) + (idx >> 1));
-    }
-    // the word beyond the warp that lane 0 (the pair to the left) or lane 31
-    // (to the right) needs; issued with the other loads
-    __device__ static __forceinline__ W edge_left(const __half* P, size_t idx, bool take) {
-        return take ? load(P, idx - 2) : 0u;
-    }
-    __device__ static __forceinline__ W edge_right(const __half* P, size_t idx, bool take) {
-        return take ? load(P, idx + 2) : 0u;
-    }
-    // (prev.hi, cur.lo): the pair one site to the left
-    __device__ static __forceinline__ W left(W cur, W edge, int lane) {
-        W prev = __shfl_up_sync(0xffffffffu, cur, 1);
-        if (lane == 0) prev = edge;
-        return __byte_perm(prev, cur, 0x5432);
-    }
-    // (cur.hi, next.lo): the pair one site to the right
-    __device__ static __forceinline__ W right(W cur, W edge, int lane) {
-        W next = __shfl_down_sync(0xffffffffu, cur, 1);
-        if (lane == 31) next = edge;
-        return __byte_perm(cur, next, 0x5432);
-    }
-    __device__ static __forceinline__ V2 dev(W w, int v) {
-        __half2 h;
-        memcpy(&h, &w, sizeof h);
-        return V2{__half22float2(h)} * h16_scale(v);
-    }
-    __device__ static __forceinline__ void put(__half* P, size_t idx, V2 g, int v) {
-        const V2 o = g * h16_inv(v);
-        reinterpret_cast<__half2*>(P)[idx >> 1] = __float22half2_rn(o.v);
-    }
-};
-template <>
-struct PairWord<StoreF32> {
-    using W = float2;  // (site s, site s+1)
-    __device__ static __forceinline__ W load(const float* P, size_t idx) {
-        return __ldg(reinterpret_cast<const float2*>(P) + (idx >> 1));
-    }
-    __device__ static __forceinline__ W edge_left(const float* P, size_t idx, bool take) {
-        return make_float2(take ? __ldg(P + idx - 1) : 0.0f, 0.0f);
-    }
-    __device__ static __forceinline__ W edge_right(const float* P, size_t idx, bool take) {
-        return make_float2(take ? __ldg(P + idx + 2) : 0.0f, 0.0f);
-    }
-    __device__ static __forceinline__ W left(W cur, W edge, int lane) {
-        float py = __shfl_up_sync(0xffffffffu, cur.y, 1);
-        if (lane == 0) py = edge.x;
-        return make_float2(py, cur.x);
-    }
-    __device__ static __forceinline__ W right(W cur, W edge, int lane) {
-        float nx = __shfl_down_sync(0xffffffffu, cur.x, 1);
-        if (lane == 31) nx = edge.x;
-        return make_float2(cur.y, nx);
-    }
-    __device__ static __forceinline__ V2 dev(W w, int) { return V2{w}; }
-    __device__ static __forceinline__ void put(float* P, size_t idx, V2 g, int) {
-        reinterpret_cast<float2*>(P)[idx >> 1] = g.v;
-    }
-};
-
-// Sites (s, s+1) of an interior row 1 <= j <= Ny-2; every lane of the warp
-// calls it (the shuffles), lanes past the row end do nothing.
-template <bool CM, bool FORCED, class S>
-__device__ __forceinline__ void interior_pair_lowp(const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
-                                                   const LatDev& L, int t, int s, int j) {
-    using P = PairWord<S>;
-    const int lane = threadIdx.x & 31;
-    // the loads of lanes past the row stay inside the row's pitch
-    const int sc = s < L.pitch - 2 ? s : L.pitch - 2;
-    const bool has_left = sc >= 2, has_right = sc + 2 <= L.pitch - 2;
-    // every load first (the pairs and the words beyond the warp), then the
-    // shuffles that shift the x-streaming planes
-    typename P::W w[9], edge[9];
-#pragma unroll
-    for (int v = 0; v < 9; v++) {
-        const size_t idx = (size_t)v * L.S + (size_t)(j - cy_of(v)) * L.pitch + sc;
-        w[v] = P::load(A, idx);
-        if (cx_of(v) > 0) edge[v] = P::edge_left(A, idx, lane == 0 && has_left);
-        if (cx_of(v) < 0) edge[v] = P::edge_right(A, idx, lane == 31 && has_right);
-    }
-#pragma unroll
-    for (int v = 0; v < 9; v++) {
-        if (cx_of(v) > 0) w[v] = P::left(w[v], edge[v], lane);
-        if (cx_of(v) < 0) w[v] = P::right(w[v], edge[v], lane);
-    }
-    const bool pair_ok = s >= 2 && s + 1 <= L.Nx - 2 && !(L.convective && s + 1 >= L.Nx - 3);
-    if (!pair_ok) {
-        if (s < L.Nx) interior_site_lowp_f<CM, FORCED, S>(A, B, L, t, s, j);
-        if (s + 1 < L.Nx) interior_site_lowp_f<CM, FORCED, S>(A, B, L, t, s + 1, j);
-        return;
-    }
-    V2 g[9];
-#pragma unroll
-    for (int v = 0; v < 9; v++) g[v] = P::dev(w[v], v);
-    float Fxd = 0.0f, Fyd = 0.0f, Gxd = 0.0f, Gyd = 0.0f;
-    if (FORCED) {
-        force_xy_at_f(L, t, Fxd, Fyd);
-        force_xy_at_f(L, t + 1, Gxd, Gyd);
-    }
-    const V2 dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
-    const V2 rho = 1.0f + dr;
-    const V2 mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
-    const V2 my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
-    const V2 inv = v2(__frcp_rn(rho.v.x), __frcp_rn(rho.v.y));
-    const V2 ux = (FORCED ? fmaf(0.5f, Fxd, mx) : mx) * inv, uy = (FORCED ? fmaf(0.5f, Fyd, my) : my) * inv;
-    V2 gs[9];
-    collide_dev32<CM, FORCED>(g, dr, rho, mx, my, ux, uy, Gxd, Gyd, L.omega_f, gs);
-    const size_t base = (size_t)j * L.pitch + s;
-#pragma unroll
-    for (int v = 0; v < 9; v++) P::put(B, (size_t)v * L.S + base, gs[v], v);
-}
-
-// k_step_lowp with two sites per thread (512 sites per block).
-template <bool CM, class S>
-__global__ void __launch_bounds__(256, CM ? 4 : 5) k_step_lowp2(const typename S::T* __restrict__ A,
-                                                       typename S::T* __restrict__ B, LatDev L, int t, int pb,
-                                                       int bx, unsigned bx_m) {
-    t = step_t(L, t);
-    if ((int)blockIdx.x < pb) {
-        perimeter_site_call<CM, S>(A, B, L, t, blockIdx.x * blockDim.x + threadIdx.x);
-        return;
-    }
-    const unsigned b = blockIdx.x - pb;
-    const int j = bx_m ? (int)__umulhi(b, bx_m) : (int)(b / (unsigned)bx);
-    const int s = 2 * ((int)(b - (unsigned)j * (unsigned)bx) * (int)blockDim.x + (int)threadIdx.x);
-    if (j == 0 || j == L.Ny - 1) {  // the whole block: boundary rows or periodic wraps
-        if (s < L.Nx) interior_site_lowp<CM, S>(A, B, L, t, s, j);
-        if (s + 1 < L.Nx) interior_site_lowp<CM, S>(A, B, L, t, s + 1, j);
-        return;
-    }
-    if (lattice_forced(L)) interior_pair_lowp<CM, true, S>(A, B, L, t, s, j);
-    else interior_pair_lowp<CM, false, S>(A, B, L, t, s, j);
-}
-
 // ---- TMA-staged tiles ---------------------------------------------------
 //
 // A persistent CTA walks the interior tiles (W x H sites of rows 1..Ny-2 and
@@ -702,27 +519,23 @@ int tma_timeouts() {
     return h;
 }
 
-// Which step kernel a reduced-precision case uses, LIFE_STEP_KERNEL:
-// "site" (k_step_lowp, one site per thread), "pair" (k_step_lowp2) or "tma"
-// (k_step_tma, TMA-staged tiles; the default).
-enum { STEP_SITE = 1, STEP_PAIR = 2, STEP_TMA = 3 };
-static int step_kernel(int) {
-    static int choice = 0;
-    if (!choice) {
+// Which step kernel a reduced-precision case uses: the TMA-staged tiles for
+// FP16 storage (whose one-site kernel is bound by instruction issue and load
+// latency, not by HBM), the one-site kernel for FP32 storage (within 10 % of
+// the HBM roofline already; the staged tiles' halo rows cost it more than the
+// staging saves). LIFE_STEP_KERNEL=site|tma overrides, for measurements and
+// for the tests that compare the two bit for bit.
+enum { STEP_SITE = 1, STEP_TMA = 3 };
+static int step_kernel(int prec) {
+    static int forced = -1;
+    if (forced < 0) {
         const char* e = getenv("LIFE_STEP_KERNEL");
-        choice = STEP_TMA;
-        if (e && !strcmp(e, "site")) choice = STEP_SITE;
-        else if (e && !strcmp(e, "pair")) choice = STEP_PAIR;
+        forced = 0;
+        if (e && !strcmp(e, "site")) forced = STEP_SITE;
+        else if (e && !strcmp(e, "tma")) forced = STEP_TMA;
     }
-    return choice;
-}
-
-static unsigned div_magic(int bx, long long bmax) {
-    // m = floor(2^32 / bx) + 1 gives floor(b / bx) = umulhi(b, m) exactly
-    // when b (m bx - 2^32) < 2^32 for the largest b; else 0 (divide)
-    const unsigned long long m = (1ull << 32) / (unsigned long long)bx + 1ull;
-    return (m < (1ull << 32) && (unsigned long long)bmax * (m * (unsigned long long)bx - (1ull << 32)) < (1ull << 32))
-               ? (unsigned)m : 0u;
+    if (forced) return forced;
+    return prec == LIFE_PREC_F16 ? STEP_TMA : STEP_SITE;
 }
 
 cudaError_t launch_step_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
@@ -731,22 +544,6 @@ cudaError_t launch_step_lowp(const void* A, void* B, const LatDev& L, int t, cud
         if (L.prec == LIFE_PREC_F32)
             return L.cm ? launch_step_tma_t<true, StoreF32>(A, B, L, t, s) : launch_step_tma_t<false, StoreF32>(A, B, L, t, s);
         return L.cm ? launch_step_tma_t<true, StoreF16>(A, B, L, t, s) : launch_step_tma_t<false, StoreF16>(A, B, L, t, s);
-    }
-    if (kind == STEP_PAIR) {
-        const int n = 2 * L.Nx + 2 * (L.Ny - 2);
-        const int pb = (n + 255) / 256, bx = (L.Nx + 511) / 512;
-        const unsigned grid = (unsigned)(pb + bx * L.Ny);
-        const unsigned bx_m = div_magic(bx, (long long)bx * L.Ny);
-        if (L.prec == LIFE_PREC_F32) {
-            if (L.cm) k_step_lowp2<true, StoreF32><<<grid, 256, 0, s>>>((const float*)A, (float*)B, L, t, pb, bx, bx_m);
-            else k_step_lowp2<false, StoreF32><<<grid, 256, 0, s>>>((const float*)A, (float*)B, L, t, pb, bx, bx_m);
-        } else {
-            if (L.cm)
-                k_step_lowp2<true, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t, pb, bx, bx_m);
-            else
-                k_step_lowp2<false, StoreF16><<<grid, 256, 0, s>>>((const __half*)A, (__half*)B, L, t, pb, bx, bx_m);
-        }
-        return cudaGetLastError();
     }
 
     const int n = 2 * L.Nx + 2 * (L.Ny - 2);

@@ -1,7 +1,8 @@
 """The one-launch step kernels of the reduced-precision forms (lattices of
 2^22 sites or more) against each other and against the separate perimeter +
 interior kernels of the host-driven loop: k_step_tma (TMA-staged tiles, the
-default), k_step_lowp (one site per thread, LIFE_STEP_KERNEL=site) and
+FP16 form's default, LIFE_STEP_KERNEL=tma), k_step_lowp (one site per thread,
+the FP32 form's default, LIFE_STEP_KERNEL=site) and
 LIFE_CASE_HOSTLOOP=1 must give the same bits after N steps, for BGK and
 central moments, with and without a step force, with a convective outlet,
 periodic x walls and an odd width."""
@@ -51,7 +52,7 @@ def digest(kind, prec, env):
 def test_step_kernels_bit_identical(kind, prec):
     from life_gb300.build import build
     build()
-    tma = digest(kind, prec, {})
+    tma = digest(kind, prec, {"LIFE_STEP_KERNEL": "tma"})
     one = digest(kind, prec, {"LIFE_STEP_KERNEL": "site"})
     host = digest(kind, prec, {"LIFE_CASE_HOSTLOOP": "1"})
     assert one == host, "one-site step kernel vs host-driven kernels"
