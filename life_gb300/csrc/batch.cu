@@ -155,7 +155,8 @@ static int upload_case_table(LifeBatch* b) {
 static bool fused_step(const LifeBatch* b) {
     if (b->cases.size() != 1 || b->prec == LIFE_PREC_F64) return false;
     const LifeCase* c = b->cases[0];
-    return (long long)c->Nx * c->Ny >= (1LL << 22);
+    // (a per-site force is taken only by the separate interior kernel)
+    return !c->site_force && (long long)c->Nx * c->Ny >= (1LL << 22);
 }
 
 static cudaError_t launch_batch_interior(LifeBatch* b, int phase, cudaStream_t s) {

@@ -205,15 +205,16 @@ __global__ void __launch_bounds__(256) k_ibm_spread(const typename S::T* __restr
             W.sites[atomicAdd(W.nsites, 1)] = s;
             double f[9], rho, ux, uy, Fx, Fy;
             site_state<CM, S>(A, L, t, i, j, f, rho, ux, uy);
-            force_xy_at(L, t, Fx, Fy);
+            force_xy_of(L, t, i, j, Fx, Fy);
             macroscopic_ibm(f, Fx, Fy, ax, ay, rho, ux, uy);
+            store_history(L, site_type(L, i, j), i, j, rho, ux, uy);
             if (L.convective && i >= L.Nx - 3) {
                 const int c = i - (L.Nx - 3);
                 L.outlet_u[((size_t)c * L.Ny + j) * 2 + 0] = ux;
                 L.outlet_u[((size_t)c * L.Ny + j) * 2 + 1] = uy;
             }
             double Gx, Gy, fs[9];
-            force_xy_at(L, t + 1, Gx, Gy);
+            force_xy_next(L, t + 1, rho, Gx, Gy);
             collide<CM>(f, rho, ux, uy, Gx + ax, Gy + ay, L.omega, L.cs, fs);
 #pragma unroll
             for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = S::save(fs[v], v);

@@ -277,6 +277,15 @@ __device__ __forceinline__ void force_xy_at_f(const LatDev& L, int t, float& Fx,
     }
 }
 
+// force_xy of step t in float at a site whose density after step t-1 was
+// rho_n (per-site force; reduced-precision kernels, constants rounded on the
+// host).
+__device__ __forceinline__ void force_xy_site_f(const LatDev& L, int t, float rho_n, float& Fx, float& Fy) {
+    const StepScalars& s = L.steps[t % L.steps_cap];
+    Fx = fmaf(rho_n * L.Drho_f, L.gx_f, s.ax_f) * L.fscdm_f;
+    Fy = fmaf(rho_n * L.Drho_f, L.gy_f, s.ay_f) * L.fscdm_f;
+}
+
 // Whether this case has a step force at all (a value every thread of a
 // launch shares): a Womersley pressure gradient or a gravity that is not
 // +-0, tested on the bits (no FP64 comparison).
@@ -301,13 +310,45 @@ __device__ __forceinline__ void force_xy_at(const LatDev& L, int t, double& Fx, 
     }
 }
 
+// force_xy of step t at a site whose density after step t-1 was rho_n, with
+// gravity beside the Womersley term (GridClass::lbmKernel,
+// src/Grid.cpp:59-60, in its operation order).
+__device__ __forceinline__ void force_xy_site(const LatDev& L, int t, double rho_n, double& Fx, double& Fy) {
+    const StepScalars& s = L.steps[t % L.steps_cap];
+    Fx = (rho_n * L.Drho * L.gx + s.ax) * L.fsc / L.Dm;
+    Fy = (rho_n * L.Drho * L.gy + s.ay) * L.fsc / L.Dm;
+}
+
+// force_xy of step t at site (i, j): the step's value, or with a per-site
+// force the value formed from the site's density after step t-1.
+__device__ __forceinline__ void force_xy_of(const LatDev& L, int t, int i, int j, double& Fx, double& Fy) {
+    if (L.site_force) force_xy_site(L, t, L.rho_prev[(size_t)j * L.pitch + i], Fx, Fy);
+    else force_xy_at(L, t, Fx, Fy);
+}
+
+// force_xy of step t+1 at a site whose density after step t is rho (the
+// force the collision of the next step uses).
+__device__ __forceinline__ void force_xy_next(const LatDev& L, int t_next, double rho, double& Fx, double& Fy) {
+    if (L.site_force) force_xy_site(L, t_next, rho, Fx, Fy);
+    else force_xy_at(L, t_next, Fx, Fy);
+}
+
+// Slot of a pressure-boundary corner site in LatDev::corner_prev/next, or -1.
+// A corner is a site with a normal in both directions (site_normal).
+__device__ __forceinline__ int pressure_corner(int type, int nx, int ny, int i, int j) {
+    if (type != LIFE_PRESSURE || nx == 0 || ny == 0) return -1;
+    return (i == 0 ? 0 : 1) + (j == 0 ? 0 : 2);
+}
+
 // Post-macroscopic moments of a fluid site of step t (read by boundary sites:
-// Utils::extrapolate / zeroGradient, inc/Utils.h:137-217).
+// Utils::extrapolate / zeroGradient, inc/Utils.h:137-217), with the site's
+// own force_xy.
 template <class S>
-__device__ __forceinline__ void fluid_moments(const typename S::T* __restrict__ P, const LatDev& L, int i, int j,
-                                              double Fx, double Fy, double& rho, double& ux, double& uy) {
+__device__ __forceinline__ void fluid_moments(const typename S::T* __restrict__ P, const LatDev& L, int t, int i,
+                                              int j, double Fx, double Fy, double& rho, double& ux, double& uy) {
     double f[9];
     gather<S>(P, L, i, j, f);
+    if (L.site_force) force_xy_site(L, t, L.rho_prev[(size_t)j * L.pitch + i], Fx, Fy);
     macroscopic(f, Fx, Fy, rho, ux, uy);
 }
 
@@ -372,7 +413,7 @@ __device__ __forceinline__ void site_state(const typename S::T* __restrict__ P, 
                                            double f[9], double& rho, double& ux, double& uy) {
     gather<S>(P, L, i, j, f);
     double Fx, Fy;
-    force_xy_at(L, t, Fx, Fy);
+    force_xy_of(L, t, i, j, Fx, Fy);
     const int type = site_type(L, i, j);
     if (type != LIFE_FLUID) {
         if (type == LIFE_CONVECTIVE) {
@@ -394,8 +435,8 @@ __device__ __forceinline__ void site_state(const typename S::T* __restrict__ P, 
             } else if (type == LIFE_FREESLIP || type == LIFE_PRESSURE) {
                 // zeroGradient order 2 along the normal on the new velocity field
                 double q1, a1x, a1y, q2, a2x, a2y;
-                fluid_moments<S>(P, L, i + nx, j + ny, Fx, Fy, q1, a1x, a1y);
-                fluid_moments<S>(P, L, i + 2 * nx, j + 2 * ny, Fx, Fy, q2, a2x, a2y);
+                fluid_moments<S>(P, L, t, i + nx, j + ny, Fx, Fy, q1, a1x, a1y);
+                fluid_moments<S>(P, L, t, i + 2 * nx, j + 2 * ny, Fx, Fy, q2, a2x, a2y);
                 if (type == LIFE_FREESLIP) un[nd] = 0.0;
                 else rn = L.rho_in[j];
                 const int d = 1 - nd;
@@ -403,11 +444,15 @@ __device__ __forceinline__ void site_state(const typename S::T* __restrict__ P, 
                 un[d] = (4.0 / 3.0) * a1 - (1.0 / 3.0) * a2;
                 r1 = q1;
                 r2 = q2;
+                // a pressure corner sets only the tangential velocity; the
+                // normal one is the site's velocity after the previous step
+                const int k = pressure_corner(type, nx, ny, i, j);
+                if (k >= 0) un[nd] = L.corner_prev[k * 2 + nd];
             }
             if (corner && (type == LIFE_VELOCITY || type == LIFE_WALL)) {
                 double a, b;
-                fluid_moments<S>(P, L, i + nx, j + ny, Fx, Fy, r1, a, b);
-                fluid_moments<S>(P, L, i + 2 * nx, j + 2 * ny, Fx, Fy, r2, a, b);
+                fluid_moments<S>(P, L, t, i + nx, j + ny, Fx, Fy, r1, a, b);
+                fluid_moments<S>(P, L, t, i + 2 * nx, j + 2 * ny, Fx, Fy, r2, a, b);
             }
             regularised<CM>(f, type, nx, ny, nd, rn, un, L.cs, r1, r2);
         }
@@ -444,13 +489,29 @@ __device__ __forceinline__ void store_collided(typename S::T* __restrict__ B, co
                                                int j, const double f[9], double rho, double ux, double uy, double Ix,
                                                double Iy) {
     double Fx, Fy, fs[9];
-    force_xy_at(L, t_next, Fx, Fy);
+    force_xy_next(L, t_next, rho, Fx, Fy);
     collide<CM>(f, rho, ux, uy, Fx + Ix, Fy + Iy, L.omega, L.cs, fs);
     const size_t s = (size_t)j * L.pitch + i;
 #pragma unroll
     for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = S::save(fs[v], v);
 }
 
+
+// What the next step reads of this step's result at a boundary site: the
+// density (per-site force) and, at a pressure corner, the velocity.
+__device__ __forceinline__ void store_history(const LatDev& L, int type, int i, int j, double rho, double ux,
+                                              double uy) {
+    if (L.site_force) L.rho_next[(size_t)j * L.pitch + i] = rho;
+    if (type == LIFE_PRESSURE) {
+        int nx, ny, nd;
+        site_normal(L, i, j, nx, ny, nd);
+        const int k = pressure_corner(type, nx, ny, i, j);
+        if (k >= 0) {
+            L.corner_next[k * 2 + 0] = ux;
+            L.corner_next[k * 2 + 1] = uy;
+        }
+    }
+}
 
 // Boundary-condition site q of the perimeter, enumerated bottom row, top row,
 // left column, right column: its step-t state by site_state() (regularised /
@@ -466,10 +527,12 @@ __device__ __forceinline__ void perimeter_site(const typename S::T* __restrict__
     else if (q < 2 * Nx + (Ny - 2)) { i = 0; j = q - 2 * Nx + 1; }
     else if (q < 2 * Nx + 2 * (Ny - 2)) { i = Nx - 1; j = q - 2 * Nx - (Ny - 2) + 1; }
     else return;
-    if (site_type(L, i, j) == LIFE_FLUID) return;
+    const int type = site_type(L, i, j);
+    if (type == LIFE_FLUID) return;
     double f[9], rho, ux, uy;
     site_state<CM, S>(A, L, t, i, j, f, rho, ux, uy);
     outlet_outputs(L, i, j, f, ux, uy);
+    store_history(L, type, i, j, rho, ux, uy);
     store_collided<CM, S>(B, L, t + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
 }
 

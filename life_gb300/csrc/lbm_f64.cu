@@ -44,7 +44,7 @@ __global__ void k_init(typename S::T* __restrict__ B, LatDev L, int t0) {
         double f[9], fs[9], Fx, Fy;
 #pragma unroll
         for (int v = 0; v < 9; v++) f[v] = equilibrium<CM>(v, rho, ux, uy);
-        force_xy_at(L, t0 + 1, Fx, Fy);
+        force_xy_next(L, t0 + 1, rho, Fx, Fy);
         collide<CM>(f, rho, ux, uy, Fx + 0.0, Fy + 0.0, L.omega, L.cs, fs);
 #pragma unroll
         for (int v = 0; v < 9; v++) {
@@ -57,8 +57,10 @@ __global__ void k_init(typename S::T* __restrict__ B, LatDev L, int t0) {
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= L.Nx) return;
-    const int w = site_type(L, i, j) == LIFE_WALL ? 1 : 0;
+    const int type = site_type(L, i, j);
+    const int w = type == LIFE_WALL ? 1 : 0;
     outlet_outputs(L, i, j, s_f[w], s_u[w][0], s_u[w][1]);
+    store_history(L, type, i, j, 1.0, s_u[w][0], s_u[w][1]);
     const size_t s = (size_t)j * L.pitch + i;
 #pragma unroll
     for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = s_out[w][v];
@@ -67,8 +69,10 @@ __global__ void k_init(typename S::T* __restrict__ B, LatDev L, int t0) {
 // One time step, interior sites, FP64: S_t from P_t (A), then P_{t+1} into B.
 // Sites on a boundary-condition wall are left to k_perimeter; IBM support
 // sites are collided again by the IBM fix-up kernel once the spread force is
-// known. Same arithmetic as site_state() for a fluid site.
-template <bool CM>
+// known. Same arithmetic as site_state() for a fluid site. SITE: the case
+// has a per-site force (WOMERSLEY with gravity), a separate instantiation so
+// the other cases' kernels do not carry its registers.
+template <bool CM, bool SITE>
 __device__ __forceinline__ void interior_site_f64(const double* __restrict__ A, double* __restrict__ B,
                                                   const LatDev& L, int t, int i, int j) {
     if (site_type(L, i, j) != LIFE_FLUID) return;
@@ -81,11 +85,26 @@ __device__ __forceinline__ void interior_site_f64(const double* __restrict__ A, 
 #pragma unroll
         for (int v = 0; v < 9; v++) f[v] = A[(size_t)v * L.S + base - cx_of(v) - (long long)cy_of(v) * L.pitch];
     }
-    if (lattice_forced_d(L)) {
+    if (SITE) {
+        const size_t s = (size_t)j * L.pitch + i;
+        force_xy_site(L, t, L.rho_prev[s], Fx, Fy);
+        macroscopic(f, Fx, Fy, rho, ux, uy);
+        outlet_outputs(L, i, j, f, ux, uy);
+        L.rho_next[s] = rho;
+        double Gx, Gy, fs[9];
+        force_xy_site(L, t + 1, rho, Gx, Gy);
+        collide<CM>(f, rho, ux, uy, Gx + 0.0, Gy + 0.0, L.omega, L.cs, fs);
+#pragma unroll
+        for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = fs[v];
+    } else if (lattice_forced_d(L)) {
         force_xy_at(L, t, Fx, Fy);
         macroscopic(f, Fx, Fy, rho, ux, uy);
         outlet_outputs(L, i, j, f, ux, uy);
-        store_collided<CM, StoreF64>(B, L, t + 1, i, j, f, rho, ux, uy, 0.0, 0.0);
+        double Gx, Gy, fs[9];
+        force_xy_at(L, t + 1, Gx, Gy);
+        collide<CM>(f, rho, ux, uy, Gx + 0.0, Gy + 0.0, L.omega, L.cs, fs);
+#pragma unroll
+        for (int v = 0; v < 9; v++) B[(size_t)v * L.S + (size_t)j * L.pitch + i] = fs[v];
     } else {
         // zero force at every step: the velocity without the force half-term
         // (the same value) and no forcing terms in the collision
@@ -99,12 +118,12 @@ __device__ __forceinline__ void interior_site_f64(const double* __restrict__ A, 
     }
 }
 
-template <bool CM>
+template <bool CM, bool SITE>
 __global__ void __launch_bounds__(128) k_interior_f64(const double* __restrict__ A, double* __restrict__ B, LatDev L,
                                                       int t) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     if (i >= L.Nx) return;
-    interior_site_f64<CM>(A, B, L, step_t(L, t), i, j);
+    interior_site_f64<CM, SITE>(A, B, L, step_t(L, t), i, j);
 }
 
 // All cases of a batch in one persistent launch (see k_interior_batch_lowp).
@@ -123,8 +142,13 @@ __global__ void __launch_bounds__(256) k_interior_batch_f64(const BatchLatCase* 
         double* B = (double*)C.B[phase];
         const int j1 = (ty + 1) * tile_h < L.Ny ? (ty + 1) * tile_h : L.Ny;
         for (int j = ty * tile_h; j < j1; j++) {
-            if (L.cm) interior_site_f64<true>(A, B, L, t, i, j);
-            else interior_site_f64<false>(A, B, L, t, i, j);
+            if (L.site_force) {
+                if (L.cm) interior_site_f64<true, true>(A, B, L, t, i, j);
+                else interior_site_f64<false, true>(A, B, L, t, i, j);
+            } else {
+                if (L.cm) interior_site_f64<true, false>(A, B, L, t, i, j);
+                else interior_site_f64<false, false>(A, B, L, t, i, j);
+            }
         }
     }
 }
@@ -181,6 +205,7 @@ __global__ void k_state(typename S::T* __restrict__ B, LatDev L, int t, const do
     for (int v = 0; v < 9; v++) f[v] = f_in[id * 9 + v];
     const double rho = rho_in[id], ux = u_in[id * 2], uy = u_in[id * 2 + 1];
     outlet_outputs(L, i, j, f, ux, uy);
+    store_history(L, site_type(L, i, j), i, j, rho, ux, uy);
     store_collided<CM, S>(B, L, t + 1, i, j, f, rho, ux, uy, fibm_in[id * 2], fibm_in[id * 2 + 1]);
 }
 
@@ -203,7 +228,7 @@ __global__ void k_export(const typename S::T* __restrict__ P, LatDev L, int t, d
         Iy = L.force_ibm[L.S + s];
         if (Ix != 0.0 || Iy != 0.0) {
             double Fx, Fy;
-            force_xy_at(L, t, Fx, Fy);
+            force_xy_of(L, t, i, j, Fx, Fy);
             macroscopic_ibm(f, Fx, Fy, Ix, Iy, rho, ux, uy);
         }
     }
@@ -240,7 +265,7 @@ __global__ void k_export_vti(const typename S::T* __restrict__ P, LatDev L, int 
             const double Ix = L.force_ibm[s], Iy = L.force_ibm[L.S + s];
             if (Ix != 0.0 || Iy != 0.0) {
                 double Fx, Fy;
-                force_xy_at(L, t, Fx, Fy);
+                force_xy_of(L, t, i, j, Fx, Fy);
                 macroscopic_ibm(f, Fx, Fy, Ix, Iy, rho, ux, uy);
             }
         }
@@ -289,7 +314,7 @@ __global__ void k_maxvel(const typename S::T* __restrict__ P, LatDev L, int t, u
             double Ix = L.force_ibm[s], Iy = L.force_ibm[L.S + s];
             if (Ix != 0.0 || Iy != 0.0) {
                 double Fx, Fy;
-                force_xy_at(L, t, Fx, Fy);
+                force_xy_of(L, t, i, j, Fx, Fy);
                 macroscopic_ibm(f, Fx, Fy, Ix, Iy, rho, ux, uy);
             }
         }
@@ -332,8 +357,13 @@ cudaError_t launch_init(void* B, const LatDev& L, int t0, cudaStream_t s) {
 }
 
 cudaError_t launch_interior_f64(const double* A, double* B, const LatDev& L, int t, cudaStream_t s) {
-    if (L.cm) k_interior_f64<true><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
-    else k_interior_f64<false><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
+    if (L.site_force) {
+        if (L.cm) k_interior_f64<true, true><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
+        else k_interior_f64<false, true><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
+    } else {
+        if (L.cm) k_interior_f64<true, false><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
+        else k_interior_f64<false, false><<<grid_of(L), 128, 0, s>>>(A, B, L, t);
+    }
     return cudaGetLastError();
 }
 

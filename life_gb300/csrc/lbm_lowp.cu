@@ -157,13 +157,13 @@ __device__ __forceinline__ void collide_dev32(const T g[9], T dr, T rho, T mx, T
     }
 }
 
-template <bool CM, bool FORCED, class S>
+template <bool CM, bool FORCED, class S, bool SITE = false>
 __device__ __forceinline__ void finish_site_lowp(const float g[9], typename S::T* __restrict__ B, const LatDev& L,
                                                  int t, int i, int j);
 
 // One interior site, reduced-precision storage. Sites on a boundary-condition
 // wall are left to the perimeter kernel.
-template <bool CM, bool FORCED, class S>
+template <bool CM, bool FORCED, class S, bool SITE = false>
 __device__ __forceinline__ void interior_site_lowp_f(const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
                                                      const LatDev& L, int t, int i, int j) {
     if (site_type(L, i, j) != LIFE_FLUID) return;
@@ -183,22 +183,32 @@ __device__ __forceinline__ void interior_site_lowp_f(const typename S::T* __rest
             g[v] = S::dev(A[(size_t)v * L.S + (size_t)sj * L.pitch + si], v);
         }
     }
-    finish_site_lowp<CM, FORCED, S>(g, B, L, t, i, j);
+    finish_site_lowp<CM, FORCED, S, SITE>(g, B, L, t, i, j);
 }
 
 // The rest of an interior site once its nine pulled deviations g are in
-// registers: moments, outlet columns, collision, store.
-template <bool CM, bool FORCED, class S>
+// registers: moments, outlet columns, collision, store. SITE: the case has a
+// per-site force (WOMERSLEY with gravity; a separate instantiation, used only
+// by the kernels that take such cases).
+template <bool CM, bool FORCED, class S, bool SITE>
 __device__ __forceinline__ void finish_site_lowp(const float g[9], typename S::T* __restrict__ B, const LatDev& L,
                                                  int t, int i, int j) {
     const size_t base = (size_t)j * L.pitch + i;
     float Fxd = 0.0f, Fyd = 0.0f, Gxd = 0.0f, Gyd = 0.0f;
     if (FORCED) {
-        force_xy_at_f(L, t, Fxd, Fyd);
-        force_xy_at_f(L, t + 1, Gxd, Gyd);
+        if (SITE) {
+            force_xy_site_f(L, t, (float)L.rho_prev[base], Fxd, Fyd);
+        } else {
+            force_xy_at_f(L, t, Fxd, Fyd);
+            force_xy_at_f(L, t + 1, Gxd, Gyd);
+        }
     }
     const float dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
     const float rho = 1.0f + dr;
+    if (FORCED && SITE) {
+        force_xy_site_f(L, t + 1, rho, Gxd, Gyd);
+        L.rho_next[base] = (double)rho;
+    }
     const float mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
     const float my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
     const float inv = __frcp_rn(rho);  // = 1.0f / rho, correctly rounded
@@ -220,10 +230,13 @@ __device__ __forceinline__ bool lattice_forced(const LatDev& L) {
     return L.womersley || L.Fx0_f != 0.0f || L.Fy0_f != 0.0f;
 }
 
-template <bool CM, class S>
+// SITE_OK: the kernel also takes cases with a per-site force (the one-step
+// kernels k_step_lowp / k_step_tma do not; such cases use k_interior_lowp).
+template <bool CM, class S, bool SITE_OK = true>
 __device__ __forceinline__ void interior_site_lowp(const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
                                                    const LatDev& L, int t, int i, int j) {
-    if (lattice_forced(L)) interior_site_lowp_f<CM, true, S>(A, B, L, t, i, j);
+    if (SITE_OK && L.site_force) interior_site_lowp_f<CM, true, S, true>(A, B, L, t, i, j);
+    else if (lattice_forced(L)) interior_site_lowp_f<CM, true, S>(A, B, L, t, i, j);
     else interior_site_lowp_f<CM, false, S>(A, B, L, t, i, j);
 }
 
@@ -324,7 +337,7 @@ __global__ void __launch_bounds__(256, 6) k_step_lowp(const typename S::T* __res
     const int j = bx_m ? (int)__umulhi(b, bx_m) : (int)(b / (unsigned)bx);
     const int i = (int)(b - (unsigned)j * (unsigned)bx) * blockDim.x + threadIdx.x;
     if (i >= L.Nx) return;
-    interior_site_lowp<CM, S>(A, B, L, t, i, j);
+    interior_site_lowp<CM, S, false>(A, B, L, t, i, j);
 }
 
 // ---- TMA-staged tiles ---------------------------------------------------
@@ -398,7 +411,7 @@ __device__ __forceinline__ void tma_tile_sites(const unsigned char* stage, typen
 }
 
 template <bool CM, class S>
-__global__ void __launch_bounds__(256) k_step_tma(const __grid_constant__ CUtensorMap tm,
+__global__ void __launch_bounds__(256, 3) k_step_tma(const __grid_constant__ CUtensorMap tm,
                                                   const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
                                                   LatDev L, int t, int pb, int tiles_x, int ntiles) {
     using TT = TmaTile<S>;
@@ -410,7 +423,7 @@ __global__ void __launch_bounds__(256) k_step_tma(const __grid_constant__ CUtens
         const int q = blockIdx.x * blockDim.x + threadIdx.x;
         perimeter_site_call<CM, S>(A, B, L, t, q);
         int i, j;
-        if (perimeter_ij(L, q, i, j)) interior_site_lowp<CM, S>(A, B, L, t, i, j);
+        if (perimeter_ij(L, q, i, j)) interior_site_lowp<CM, S, false>(A, B, L, t, i, j);
         return;
     }
     extern __shared__ __align__(128) unsigned char smem_raw[];

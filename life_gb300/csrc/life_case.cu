@@ -160,6 +160,10 @@ int life::ensure_steps(LifeCase* c, int t0, int n) {
             s.fy = (0.0 + p.dpdy * ph) * sc / c->Dm;
             s.fx_f = (float)s.fx;
             s.fy_f = (float)s.fy;
+            s.ax = p.dpdx * ph;
+            s.ay = p.dpdy * ph;
+            s.ax_f = (float)s.ax;
+            s.ay_f = (float)s.ay;
         }
         h[k] = s;
     }
@@ -211,6 +215,20 @@ LatDev life::lattice_view(const LifeCase* c, int t) {
     L.force_ibm = c->W.force_ibm;
     L.t_dev = c->t_dev;
     L.t_off = c->t_off;
+    L.site_force = c->site_force;
+    L.Drho = c->Drho;
+    L.gx = c->p.gravityX;
+    L.gy = c->p.gravityY;
+    L.fsc = (c->Dx * c->Dt) * (c->Dx * c->Dt);
+    L.Dm = c->Dm;
+    L.Drho_f = (float)c->Drho;
+    L.gx_f = (float)c->p.gravityX;
+    L.gy_f = (float)c->p.gravityY;
+    L.fscdm_f = (float)(L.fsc / c->Dm);
+    L.rho_prev = c->d_rho_hist[(t - 1) & 1];
+    L.rho_next = c->d_rho_hist[t & 1];
+    L.corner_prev = c->d_corner_u[(t - 1) & 1];
+    L.corner_next = c->d_corner_u[t & 1];
     return L;
 }
 
@@ -224,16 +242,6 @@ static int validate(const LifeCaseParams* p) {
         return set_error(LIFE_ERR_INVALID, "Currently convective BC only supported for right boundary...exiting");
     if (p->wall_right == LIFE_CONVECTIVE && p->Nx < 4)
         return set_error(LIFE_ERR_INVALID, "convective outlet needs at least 4 columns");
-    // Pressure walls at y corners keep the previous step's normal velocity in
-    // the reference (u_n[eY] is never reset there); the device state does not
-    // carry that history.
-    for (int yw : {p->wall_bottom, p->wall_top})
-        if (yw == LIFE_PRESSURE && (p->wall_left != LIFE_FLUID || p->wall_right != LIFE_FLUID))
-            return set_error(LIFE_ERR_INVALID,
-                             "pressure boundary on a y wall with non-periodic x walls (corner velocity history) is not "
-                             "supported");
-    if (p->has_womersley && (p->gravityX != 0.0 || p->gravityY != 0.0))
-        return set_error(LIFE_ERR_INVALID, "WOMERSLEY with nonzero gravity is not supported on the GPU path");
     if (p->precision != LIFE_PREC_F64 && p->precision != LIFE_PREC_F32 && p->precision != LIFE_PREC_F16)
         return set_error(LIFE_ERR_INVALID, "unknown precision");
     if (p->omega <= 0.0) return set_error(LIFE_ERR_INVALID, "omega must be positive");
@@ -302,6 +310,7 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
     const double sc = (c->Dx * c->Dt) * (c->Dx * c->Dt);
     c->Fx0 = (rho0 * c->Drho * p.gravityX + p.dpdx) * sc / c->Dm;
     c->Fy0 = (rho0 * c->Drho * p.gravityY + p.dpdy) * sc / c->Dm;
+    c->site_force = p.has_womersley && (p.gravityX != 0.0 || p.gravityY != 0.0);
     c->u0x = p.ux0_p * c->Dt / c->Dx;
     c->u0y = p.uy0_p * c->Dt / c->Dx;
     c->init_mode = p.has_inlet_ramp ? 0 : (p.profile >= 0 ? 1 : 2);
@@ -366,7 +375,10 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
         (rc = dev_alloc_t(c, &c->d_outlet_u, (size_t)3 * p.Ny * 2)) ||
         (rc = dev_alloc_t(c, &c->d_outlet_f[0], (size_t)p.Ny * 3)) ||
         (rc = dev_alloc_t(c, &c->d_outlet_f[1], (size_t)p.Ny * 3)) ||
-        (rc = dev_alloc_t(c, &c->d_delU, (size_t)p.Ny * 2)) || (rc = dev_alloc_t(c, &c->d_red, 4))) {
+        (rc = dev_alloc_t(c, &c->d_delU, (size_t)p.Ny * 2)) || (rc = dev_alloc_t(c, &c->d_red, 4)) ||
+        (rc = dev_alloc_t(c, &c->d_corner_u[0], 8)) || (rc = dev_alloc_t(c, &c->d_corner_u[1], 8)) ||
+        (c->site_force && ((rc = dev_alloc_t(c, &c->d_rho_hist[0], plane)) ||
+                           (rc = dev_alloc_t(c, &c->d_rho_hist[1], plane))))) {
         free_case(c);
         return rc;
     }

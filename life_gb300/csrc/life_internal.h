@@ -73,6 +73,11 @@ struct LifeCase {
     double* d_outlet_u = nullptr;
     double* d_outlet_f[2] = {nullptr, nullptr};
     double* d_delU = nullptr;
+    // densities after alternate steps (WOMERSLEY with gravity only) and the
+    // corner velocities after alternate steps (see LatDev)
+    bool site_force = false;
+    double* d_rho_hist[2] = {nullptr, nullptr};
+    double* d_corner_u[2] = {nullptr, nullptr};
     unsigned long long* d_red = nullptr;
     cudaStream_t stream = nullptr;   // every kernel of the case is ordered on this stream
     cudaStream_t side = nullptr;     // perimeter kernel, forked from and joined to `stream`

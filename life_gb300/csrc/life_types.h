@@ -11,11 +11,15 @@ namespace life {
 // (so they equal the reference's values bit for bit): the inlet ramp
 // coefficient used by step t's boundary conditions (GridClass::getRampCoefficient,
 // reference src/Grid.cpp:548-556) and step t's uniform Womersley force
-// (src/Grid.cpp:52-62).
+// (src/Grid.cpp:52-62). With gravity beside the Womersley term the force
+// differs per site and the table holds its pressure-gradient terms
+// dpdx * cos(...) and dpdy * cos(...) instead.
 struct StepScalars {
     double ramp;
     double fx, fy;
     float fx_f, fy_f;  // (float)fx, (float)fy for the reduced-precision kernels
+    double ax, ay;     // dpdx * cos(...), dpdy * cos(...) of step t
+    float ax_f, ay_f;
 };
 
 // Everything a lattice kernel needs, passed by value.
@@ -51,6 +55,22 @@ struct LatDev {
     // t_dev is set, kernels use *t_dev + t_off instead of their t argument.
     const int* t_dev;
     int t_off;
+    // WOMERSLEY with gravity (src/Grid.cpp:52-62): force_xy of step t at a
+    // site is ((rho_n * Drho) * g + dpdx cos(...)) * (Dx Dt)^2 / Dm, with
+    // rho_n the site's density after step t-1. The step reads those densities
+    // from rho_prev and writes its own into rho_next (two buffers alternating
+    // by step parity, pitch layout).
+    int site_force;
+    double Drho, gx, gy, fsc, Dm;  // fsc = (Dx Dt)^2
+    float Drho_f, gx_f, gy_f, fscdm_f;
+    const double* rho_prev;
+    double* rho_next;
+    // Pressure corners keep the normal velocity of the previous step
+    // (applyBCs sets only the tangential one there, src/Grid.cpp:354-369):
+    // u after step t-1 (corner_prev) and after step t (corner_next) of the
+    // four corners, slot (i == Nx-1) + 2 (j == Ny-1), two components each.
+    const double* corner_prev;
+    double* corner_next;
 };
 
 }  // namespace life

@@ -61,6 +61,20 @@ def golden_cases() -> Dict[str, Tuple[CaseParams, List]]:
     C["freeslip_pressure_gravity_cm"] = (lattice_case(
         40, 28, 1.0 / 0.6, 300, wall_left=PRESSURE, wall_right=PRESSURE, wall_bottom=FREESLIP,
         wall_top=WALL, gravityX=2e-5, ux0_p=0.01, central_moments=True, ref_U=0.01), [])
+    # WOMERSLEY with gravity: the force of every site depends on its density
+    # after the previous step (src/Grid.cpp:52-62)
+    C["womersley_gravity_cm"] = (lattice_case(26, 31, 1.0 / 0.68, 300, wall_left=FLUID,
+                                              wall_right=FLUID, wall_bottom=WALL, wall_top=WALL,
+                                              womersley=2.5, dpdx=2e-5, dpdy=-1e-6, gravityX=8e-6,
+                                              gravityY=-3e-6, central_moments=True, ref_U=0.01), [])
+    # pressure walls on y with non-periodic x walls: the corners keep the
+    # previous step's normal velocity (src/Grid.cpp:354-369)
+    C["pressure_top_corners"] = (lattice_case(40, 30, 1.0 / 0.6, 300, wall_left=VELOCITY,
+                                              wall_right=WALL, wall_bottom=WALL, wall_top=PRESSURE,
+                                              uxInlet_p=0.03, inlet_ramp=50.0), [])
+    C["pressure_ywalls_convective_cm"] = (lattice_case(
+        48, 28, 1.0 / 0.62, 300, wall_left=VELOCITY, wall_right=CONVECTIVE, wall_bottom=PRESSURE,
+        wall_top=PRESSURE, uxInlet_p=0.04, ux0_p=0.04, uy0_p=0.002, central_moments=True), [])
     C["periodic_y_uniform_init"] = (lattice_case(
         30, 26, 1.0 / 0.75, 250, wall_left=VELOCITY, wall_right=PRESSURE, wall_bottom=FLUID,
         wall_top=FLUID, uxInlet_p=0.03, ux0_p=0.03, uy0_p=0.001), [])

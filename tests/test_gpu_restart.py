@@ -17,7 +17,8 @@ from cases import golden_cases
 
 pytestmark = pytest.mark.gpu
 NAMES = ["cavity_cm", "channel_convective_freeslip_cm", "cylinder_rigid_cm", "cylinders_uni_bgk",
-         "filament_flex_deflect", "turek_like_uni", "honami_like_cm", "filament_supported_and_rigid"]
+         "filament_flex_deflect", "turek_like_uni", "honami_like_cm", "filament_supported_and_rigid",
+         "womersley_gravity_cm", "pressure_ywalls_convective_cm"]
 N1, N2 = 40, 33
 
 
