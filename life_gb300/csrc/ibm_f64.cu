@@ -223,6 +223,39 @@ __global__ void __launch_bounds__(256) k_ibm_spread(const typename S::T* __restr
     }
 }
 
+// ObjectsClass::removeOverlapMarkers (src/Objects.cpp:873-884): every marker
+// pair n1 < n2 whose distance is below half a lattice spacing, with the
+// reference's arithmetic (sum of squares from +0, square root, division).
+// Block n1 (grid-stride) tests n2 > n1 on its threads; hits are appended in
+// any order (the host sorts them) while the count stays within cap, and the
+// count is returned in full so the host can retry with a larger list.
+__global__ void k_overlap_pairs(const double* __restrict__ pos, int nm, double Dx, int* __restrict__ count,
+                                int2* __restrict__ out, int cap) {
+    for (int n1 = blockIdx.x; n1 < nm; n1 += gridDim.x) {
+        const double x1 = pos[2 * n1], y1 = pos[2 * n1 + 1];
+        for (int n2 = n1 + 1 + (int)threadIdx.x; n2 < nm; n2 += blockDim.x) {
+            const double d0 = x1 - pos[2 * n2], d1 = y1 - pos[2 * n2 + 1];
+            double dd = 0.0;
+            dd += d0 * d0;
+            dd += d1 * d1;
+            if (sqrt(dd) / Dx < 0.5) {
+                const int k = atomicAdd(count, 1);
+                if (k < cap) out[k] = make_int2(n1, n2);
+            }
+        }
+    }
+}
+
+cudaError_t launch_overlap_pairs(const double* pos, int nm, double Dx, int* count, int2* out, int cap,
+                                 cudaStream_t s) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = nm < 8 * sms ? (nm > 0 ? nm : 1) : 8 * sms;
+    k_overlap_pairs<<<grid, 256, 0, s>>>(pos, nm, Dx, count, out, cap);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ launchers
 #define IBM_DISPATCH(KERNEL, GRID, BLOCK, ...)                                                             \
     do {                                                                                                   \

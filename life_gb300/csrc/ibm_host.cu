@@ -27,6 +27,46 @@ static int alloc_t(LifeCase* c, T** p, size_t n) {
     return alloc_track(c, (void**)p, sizeof(T) * n);
 }
 
+// removeOverlapMarkers' pair test on the device (objects.h OverlapScan): the
+// close pairs, sorted into the reference's (n1, n2) loop order.
+int life::device_overlap_scan(const double* pos, int nm, double Dx, std::vector<std::pair<int, int>>* pairs,
+                              std::string* err) {
+    (void)err;
+    pairs->clear();
+    if (nm < 2) return LIFE_OK;
+    double* d_pos = nullptr;
+    int* d_count = nullptr;
+    int2* d_out = nullptr;
+    int cap = 1 << 16, count = 0;
+    cudaError_t e = cudaMalloc(&d_pos, sizeof(double) * 2 * (size_t)nm);
+    if (e == cudaSuccess) e = cudaMalloc(&d_count, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(d_pos, pos, sizeof(double) * 2 * (size_t)nm, cudaMemcpyHostToDevice);
+    for (int pass = 0; e == cudaSuccess && pass < 2; pass++) {
+        if (d_out) cudaFree(d_out);
+        d_out = nullptr;
+        e = cudaMalloc(&d_out, sizeof(int2) * (size_t)cap);
+        if (e == cudaSuccess) e = cudaMemset(d_count, 0, sizeof(int));
+        if (e == cudaSuccess) e = launch_overlap_pairs(d_pos, nm, Dx, d_count, d_out, cap, 0);
+        if (e == cudaSuccess) e = cudaMemcpy(&count, d_count, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess || count <= cap) break;
+        cap = count;  // the first list was too short: run again with room for all
+    }
+    std::vector<int2> h;
+    if (e == cudaSuccess && count > cap) e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) {
+        h.resize(count);
+        if (count) e = cudaMemcpy(h.data(), d_out, sizeof(int2) * (size_t)count, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(d_out);
+    cudaFree(d_count);
+    cudaFree(d_pos);
+    if (e != cudaSuccess) return cuda_fail(e, "marker overlap scan");
+    pairs->reserve(count);
+    for (const int2& q : h) pairs->emplace_back(q.x, q.y);
+    std::sort(pairs->begin(), pairs->end());
+    return LIFE_OK;
+}
+
 // Copies the host marker table to the device arrays.
 int push_markers(LifeCase* c) {
     const auto& m = c->obj.m;

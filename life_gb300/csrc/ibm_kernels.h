@@ -42,6 +42,10 @@ struct IbmScratch {
     int4* body_box;           // [nbodies]
 };
 
+// Close marker pairs of removeOverlapMarkers (appended unordered, see
+// k_overlap_pairs).
+cudaError_t launch_overlap_pairs(const double* pos, int nm, double Dx, int* count, int2* out, int cap,
+                                 cudaStream_t s);
 // Population buffers are untyped; their element type follows L.prec.
 // With t_dev, the step is read from device memory when the kernel runs.
 cudaError_t launch_ibm_interp(const void* P, const LatDev& L, int t, const MarkerDev& M, double velScale,

@@ -339,7 +339,15 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
     Grid0 g{p.Nx, p.Ny, c->Dx, c->Dt, c->Dm, p.gravityX, p.gravityY, p.ref_L, p.alpha, p.delta};
     c->g0 = g;
     std::string err;
-    int rc = build_objects(g, p, bodies, n_bodies, c->obj, &err);
+    // Large marker sets test their pairs for overlap on the device;
+    // LIFE_OVERLAP_SCAN=device / host forces one side for every set.
+    int scan_min = kOverlapScanMin;
+    OverlapScan scan = device_overlap_scan;
+    if (const char* v = std::getenv("LIFE_OVERLAP_SCAN")) {
+        if (std::strcmp(v, "device") == 0) scan_min = 0;
+        else if (std::strcmp(v, "host") == 0) scan = nullptr;
+    }
+    int rc = build_objects(g, p, bodies, n_bodies, c->obj, &err, scan, scan_min);
     if (rc) {
         free_case(c);
         return set_error(rc, err);

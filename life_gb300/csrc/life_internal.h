@@ -129,4 +129,7 @@ void free_fem(LifeCase* c);
 cudaError_t launch_record(const LifeCase* c, int t, cudaStream_t s);
 void free_recorder(LifeCase* c);
 int ensure_steps(LifeCase* c, int t0, int n);
+// removeOverlapMarkers' pair test on the device (an OverlapScan, objects.h).
+int device_overlap_scan(const double* pos, int nm, double Dx, std::vector<std::pair<int, int>>* pairs,
+                        std::string* err);
 }  // namespace life

@@ -3,9 +3,12 @@
 // without FMA contraction so start-up values equal the reference's.
 #include "objects.h"
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <thread>
 
 #include "band_lu.h"
 
@@ -251,13 +254,85 @@ static void fem_update_values(HFem& f) {
     }
 }
 
-// forceVector + massMatrix + stiffMatrix of all elements
+// Products with an element rotation T (fem_element_transform): T is block
+// diagonal, [[c, s], [-s, c]] on DOFs 0-1 and 3-4 and 1 on DOFs 2 and 5, so
+// row or column q of T is non-zero only at the DOFs of q's block (t_blk).
+// These forms skip the structurally zero terms of mat6_mul / mat6_vec and add
+// the others in the same order. A skipped term is an exact zero, and adding a
+// zero leaves a sum that started at +0 unchanged (such a sum is never -0), so
+// every result equals the dense product's bit for bit.
+static inline int t_blk(int q, int k[2]) {
+    if (q == 2 || q == 5) {
+        k[0] = q;
+        return 1;
+    }
+    k[0] = q < 3 ? 0 : 3;
+    k[1] = k[0] + 1;
+    return 2;
+}
+// R = T^T A
+static void mat6_tt_mul(double R[6][6], const double T[6][6], const double A[6][6]) {
+    for (int i = 0; i < 6; i++) {
+        int k[2];
+        const int nk = t_blk(i, k);
+        for (int j = 0; j < 6; j++) {
+            double s = 0.0;
+            for (int q = 0; q < nk; q++) s += T[k[q]][i] * A[k[q]][j];
+            R[i][j] = s;
+        }
+    }
+}
+// R = A T
+static void mat6_mul_t(double R[6][6], const double A[6][6], const double T[6][6]) {
+    for (int j = 0; j < 6; j++) {
+        int k[2];
+        const int nk = t_blk(j, k);
+        for (int i = 0; i < 6; i++) {
+            double s = 0.0;
+            for (int q = 0; q < nk; q++) s += A[i][k[q]] * T[k[q]][j];
+            R[i][j] = s;
+        }
+    }
+}
+// r = T^T v
+static void mat6_tt_vec(double r[6], const double T[6][6], const double v[6]) {
+    for (int i = 0; i < 6; i++) {
+        int k[2];
+        const int nk = t_blk(i, k);
+        double s = 0.0;
+        for (int q = 0; q < nk; q++) s += T[k[q]][i] * v[k[q]];
+        r[i] = s;
+    }
+}
+
+// Largest |dof_i - dof_j| within one element: assembly writes K only there.
+static int fem_half_band(const HFem& f) {
+    int hw = 0;
+    for (const auto& e : f.el) {
+        int lo = e.dof[0], hi = e.dof[0];
+        for (int k = 1; k < 6; k++) {
+            lo = e.dof[k] < lo ? e.dof[k] : lo;
+            hi = e.dof[k] > hi ? e.dof[k] : hi;
+        }
+        hw = hi - lo > hw ? hi - lo : hw;
+    }
+    return hw;
+}
+
+// forceVector + stiffMatrix of all elements for the static solve
 // (FEMBodyClass::buildGlobalMatrices, src/FEMBody.cpp:90-109;
-// src/FEMElement.cpp:72-138)
-static void fem_build_global(HFem& f) {
-    const int n = f.dofs;
-    std::fill(f.M.begin(), f.M.end(), 0.0);
-    std::fill(f.K.begin(), f.K.end(), 0.0);
+// src/FEMElement.cpp:72-138; the mass matrix is not used by
+// newtonRaphsonStatic and is not formed). Every entry of K is the same sum in
+// the same element order as the dense assembly. K is stored densely, but only
+// entries with |row - col| <= 2 hw can be non-zero: assembly writes |.| <= hw
+// and the band LU's fill-in reaches kl + ku <= 2 hw. Only those are cleared,
+// the rest stay zero from the allocation.
+static void fem_build_static(HFem& f, int hw) {
+    const int n = f.dofs, w = 2 * hw;
+    for (int r = 0; r < n; r++) {
+        const int c0 = r - w > 0 ? r - w : 0, c1 = r + w < n - 1 ? r + w : n - 1;
+        std::fill(f.K.begin() + (size_t)r * n + c0, f.K.begin() + (size_t)r * n + c1 + 1, 0.0);
+    }
     std::fill(f.F.begin(), f.F.end(), 0.0);
     for (auto& e : f.el) {
         double u = (HSQ(e.L) - HSQ(e.L0)) / (e.L + e.L0);
@@ -272,16 +347,11 @@ static void fem_build_global(HFem& f) {
         e.F[3] = F0;
         e.F[4] = -(1.0 / e.L0) * (M1 + M2);
         e.F[5] = M2;
-        double Tt[6][6], tmp[6][6], G[6][6], G2[6][6], FG[6];
-        mat6_T(Tt, e.T);
-        mat6_vec(FG, Tt, e.F);
+        double tmp[6][6], G[6][6], G2[6][6], FG[6];
+        mat6_tt_vec(FG, e.T, e.F);
         for (int i = 0; i < 6; i++) f.F[e.dof[i]] += FG[i];
-        mat6_mul(tmp, Tt, e.M);
-        mat6_mul(G, tmp, e.T);
-        for (int i = 0; i < 6; i++)
-            for (int j = 0; j < 6; j++) f.M[(size_t)e.dof[i] * n + e.dof[j]] += G[i][j];
-        mat6_mul(tmp, Tt, e.KL);
-        mat6_mul(G, tmp, e.T);
+        mat6_tt_mul(tmp, e.T, e.KL);
+        mat6_mul_t(G, tmp, e.T);
         const double Fa = -e.F[0], V0 = e.F[4], L0 = e.L0;
         e.KNL[0][1] = -V0 / L0;
         e.KNL[0][4] = V0 / L0;
@@ -295,8 +365,8 @@ static void fem_build_global(HFem& f) {
         e.KNL[4][1] = -Fa / L0;
         e.KNL[4][3] = -V0 / L0;
         e.KNL[4][4] = Fa / L0;
-        mat6_mul(tmp, Tt, e.KNL);
-        mat6_mul(G2, tmp, e.T);
+        mat6_tt_mul(tmp, e.T, e.KNL);
+        mat6_mul_t(G2, tmp, e.T);
         for (int i = 0; i < 6; i++)
             for (int j = 0; j < 6; j++) f.K[(size_t)e.dof[i] * n + e.dof[j]] += G[i][j] + G2[i][j];
     }
@@ -354,6 +424,23 @@ static void fem_update_ibm(HObjects& o, HBody& b) {
     }
 }
 
+// lu_bandwidth of a matrix whose entries with |row - col| > w are zero,
+// scanning only the others (the same kl, ku).
+static void band_extent(const double* A, int dim, int bc, int w, int* kl, int* ku) {
+    int lo = 0, hi = 0;
+    const int n = dim - bc;
+    for (int j = 0; j < n; j++) {
+        const int i0 = j - w > 0 ? j - w : 0, i1 = j + w < n - 1 ? j + w : n - 1;
+        for (int i = i0; i <= i1; i++)
+            if (A[(long long)(bc + j) * dim + (bc + i)] != 0.0) {
+                if (i - j > lo) lo = i - j;
+                if (j - i > hi) hi = j - i;
+            }
+    }
+    *kl = lo;
+    *ku = hi;
+}
+
 // FEMBodyClass::setInitialDeflection + staticFEM + newtonRaphsonStatic
 // (src/FEMBody.cpp:352-484)
 static int fem_initial_deflection(const Grid0& g, const LifeCaseParams& p, HObjects& o, HBody& b, std::string* err) {
@@ -368,17 +455,18 @@ static int fem_initial_deflection(const Grid0& g, const LifeCaseParams& p, HObje
     for (int i = 0; i < 2; i++) gf[i] = 0.0 + T[i][0] * lf[0] + T[i][1] * lf[1];
     f.R[n - 3] = gf[0];
     f.R[n - 2] = gf[1];
-    std::vector<double> rhs(n), Kc(f.K.size());
+    std::vector<double> rhs(n);
     std::vector<int> piv(n);
+    const int hw = fem_half_band(f);
     double errv;
     int it = 0;
     do {
         f.itNR = 0;
         do {
-            fem_build_global(f);
+            fem_build_static(f, hw);
             for (int i = 0; i < n; i++) rhs[i] = f.R[i] - f.F[i];
             int kl, ku;
-            lu_bandwidth(f.K.data(), n, f.bc, &kl, &ku);
+            band_extent(f.K.data(), n, f.bc, 2 * hw, &kl, &ku);
             lu_band_factor(f.K.data(), n, f.bc, kl, ku, piv.data());
             lu_band_solve(f.K.data(), n, f.bc, kl, ku, piv.data(), rhs.data(), f.delU.data());
             for (int i = 0; i < n; i++) f.U[i] = f.U[i] + f.delU[i];
@@ -487,26 +575,41 @@ static HFem* build_fem(const Grid0& g, const double pos[2], const LifeBodyDesc& 
 }
 
 // ObjectsClass::removeOverlapMarkers (src/Objects.cpp:867-938)
-static int remove_overlap(const Grid0& g, HObjects& o, std::string* err) {
+static int remove_overlap(const Grid0& g, HObjects& o, std::string* err, OverlapScan scan, int scan_min) {
     std::vector<int> erase;
     const int nm = (int)o.m.size();
-    for (int n1 = 0; n1 < nm; n1++)
-        for (int n2 = n1 + 1; n2 < nm; n2++) {
-            double d0 = o.m[n1].pos[0] - o.m[n2].pos[0], d1 = o.m[n1].pos[1] - o.m[n2].pos[1];
-            double dd = 0.0;
-            dd += d0 * d0;
-            dd += d1 * d1;
-            if (std::sqrt(dd) / g.Dx < 0.5) {
-                int f1 = o.b[o.m[n1].body].flex, f2 = o.b[o.m[n2].body].flex;
-                if (f1 && f2) {
-                    if (err) *err = "Cannot place two flexible bodies so close to each other...exiting";
-                    return LIFE_ERR_GEOMETRY;
-                }
-                if (f1 && !f2) erase.push_back(o.m[n2].ID);
-                if (!f1 && f2) erase.push_back(o.m[n1].ID);
-                if (!f1 && !f2) erase.push_back(o.m[n1].ID);
-            }
+    auto close_pair = [&](int n1, int n2) -> int {
+        int f1 = o.b[o.m[n1].body].flex, f2 = o.b[o.m[n2].body].flex;
+        if (f1 && f2) {
+            if (err) *err = "Cannot place two flexible bodies so close to each other...exiting";
+            return LIFE_ERR_GEOMETRY;
         }
+        if (f1 && !f2) erase.push_back(o.m[n2].ID);
+        if (!f1 && f2) erase.push_back(o.m[n1].ID);
+        if (!f1 && !f2) erase.push_back(o.m[n1].ID);
+        return LIFE_OK;
+    };
+    if (scan && nm >= scan_min) {
+        std::vector<double> pos((size_t)nm * 2);
+        for (int n = 0; n < nm; n++) {
+            pos[2 * n] = o.m[n].pos[0];
+            pos[2 * n + 1] = o.m[n].pos[1];
+        }
+        std::vector<std::pair<int, int>> pairs;
+        if (int rc = scan(pos.data(), nm, g.Dx, &pairs, err)) return rc;
+        for (const auto& pr : pairs)
+            if (int rc = close_pair(pr.first, pr.second)) return rc;
+    } else {
+        for (int n1 = 0; n1 < nm; n1++)
+            for (int n2 = n1 + 1; n2 < nm; n2++) {
+                double d0 = o.m[n1].pos[0] - o.m[n2].pos[0], d1 = o.m[n1].pos[1] - o.m[n2].pos[1];
+                double dd = 0.0;
+                dd += d0 * d0;
+                dd += d1 * d1;
+                if (std::sqrt(dd) / g.Dx < 0.5)
+                    if (int rc = close_pair(n1, n2)) return rc;
+            }
+    }
     for (int id : erase) {
         int k = -1;
         for (int n = 0; n < (int)o.m.size(); n++)
@@ -525,7 +628,7 @@ static int remove_overlap(const Grid0& g, HObjects& o, std::string* err) {
 }
 
 int build_objects(const Grid0& g, const LifeCaseParams& p, const LifeBodyDesc* d, int nd, HObjects& o,
-                  std::string* err) {
+                  std::string* err, OverlapScan scan, int scan_min) {
     for (int k = 0; k < nd; k++) {
         const LifeBodyDesc& bd = d[k];
         if (bd.kind != LIFE_BODY_CIRCLE && bd.kind != LIFE_BODY_FILAMENT) {
@@ -579,19 +682,42 @@ int build_objects(const Grid0& g, const LifeCaseParams& p, const LifeBodyDesc* d
                 if (err) *err = "Duplicate body IDs in geometry.config...exiting";
                 return LIFE_ERR_GEOMETRY;
             }
-    int rc = remove_overlap(g, o, err);
+    int rc = remove_overlap(g, o, err, scan, scan_min);
     if (rc) return rc;
     o.hasIBM = !o.b.empty();
     for (auto& b : o.b)
         if (b.flex) o.hasFlex = true;
     if (o.hasIBM) {
         // ObjectsClass::initialiseObjects (src/Objects.cpp:941-961)
-        if (p.has_initial_deflect && o.hasFlex)
-            for (auto& b : o.b)
-                if (b.flex) {
-                    rc = fem_initial_deflection(g, p, o, b, err);
-                    if (rc) return rc;
+        if (p.has_initial_deflect && o.hasFlex) {
+            // Bodies are independent (each writes its own FEM state and its own
+            // markers), so host threads take whole bodies; the first failing
+            // body in body order reports its error, as the sequential loop would.
+            std::vector<int> flex;
+            for (size_t k = 0; k < o.b.size(); k++)
+                if (o.b[k].flex) flex.push_back((int)k);
+            std::vector<int> rcs(flex.size(), LIFE_OK);
+            std::vector<std::string> errs(flex.size());
+            std::atomic<int> next{0};
+            auto work = [&]() {
+                for (int q; (q = next++) < (int)flex.size();)
+                    rcs[q] = fem_initial_deflection(g, p, o, o.b[flex[q]], &errs[q]);
+            };
+            const unsigned ncpu = std::thread::hardware_concurrency();
+            const int nt = (int)std::min<size_t>(flex.size(), ncpu ? ncpu : 1);
+            if (nt <= 1) {
+                work();
+            } else {
+                std::vector<std::thread> pool;
+                for (int k = 0; k < nt; k++) pool.emplace_back(work);
+                for (auto& th : pool) th.join();
+            }
+            for (size_t q = 0; q < flex.size(); q++)
+                if (rcs[q]) {
+                    if (err) *err = errs[q];
+                    return rcs[q];
                 }
+        }
         for (size_t k = 0; k < o.m.size(); k++) {
             rc = host_find_support(g, o.m[k], err);
             if (rc) return rc;

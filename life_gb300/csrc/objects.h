@@ -4,6 +4,7 @@
 // reference's operation order; the per-step work runs on the device.
 #pragma once
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/life_gb300.h"
@@ -66,11 +67,22 @@ struct HObjects {
     ~HObjects();
 };
 
+// The marker pairs (n1 < n2) closer than half a lattice spacing, in
+// (n1, n2) order: the test of ObjectsClass::removeOverlapMarkers
+// (src/Objects.cpp:873-884) over all pairs. pos is [nm][2]. Returns LIFE_OK
+// or an error code with *err set.
+typedef int (*OverlapScan)(const double* pos, int nm, double Dx, std::vector<std::pair<int, int>>* pairs,
+                           std::string* err);
+
 // Builds bodies (ObjectsClass::geometryReadIn + IBMBodyClass ctors), removes
 // overlapping markers and runs initialiseObjects. Returns LIFE_OK or an
-// error code with *err set.
+// error code with *err set. With `scan`, marker sets of at least `scan_min`
+// markers find their close pairs through it (the device kernel); smaller
+// sets, or no scan, test the pairs on the host. Both apply the same test to
+// the same values.
+constexpr int kOverlapScanMin = 2048;
 int build_objects(const Grid0& g, const LifeCaseParams& p, const LifeBodyDesc* d, int nd, HObjects& out,
-                  std::string* err);
+                  std::string* err, OverlapScan scan = nullptr, int scan_min = kOverlapScanMin);
 
 // IBM start-up helpers (also used after restarts).
 int host_find_support(const Grid0& g, HMarker& m, std::string* err);
