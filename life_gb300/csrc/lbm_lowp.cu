@@ -33,13 +33,79 @@
 
 #include "collide_cm.cuh"
 #include "lbm_device.cuh"
+#include <type_traits>
+
 #include "lbm_kernels.h"
 #include "tma.cuh"
 
 namespace life {
 
+// Two sites' FP32 arithmetic in one instruction: the packed f32x2 add / mul /
+// fma of sm_100+, written as inline PTX with the explicit .rn rounding mode.
+// Each lane is an IEEE round-to-nearest FP32 operation, so each lane of a V2
+// computation gives, bit for bit, the float computation written with the
+// same expressions (a - b is a + (-b) in IEEE arithmetic, signed zeros
+// included; negation flips the sign bits), provided no product is fused
+// into a following addition: in this kernel the compiler did fuse one
+// lane's multiply and add into an fma (with the __fmul2_rn / __fadd2_rn
+// intrinsics and with this inline PTX alike; measured as one unit in the
+// last place on ~1 site in 10^6 per step), which the one-site path, compiled
+// without contraction, does not do. The BGK collision below is therefore
+// written so that no product feeds an addition, and the packed form is used
+// for BGK only.
+struct V2 {
+    unsigned long long b;  // lane x in the low 32 bits, lane y in the high 32 bits
+    __device__ __forceinline__ float x() const {
+        float lo, hi;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(b));
+        return lo;
+    }
+    __device__ __forceinline__ float y() const {
+        float lo, hi;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(b));
+        return hi;
+    }
+};
+__device__ __forceinline__ V2 v2(float a, float b) {
+    V2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.b) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ V2 v2(float a) { return v2(a, a); }
+__device__ __forceinline__ V2 operator+(V2 a, V2 b) {
+    V2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.b) : "l"(a.b), "l"(b.b));
+    return r;
+}
+__device__ __forceinline__ V2 operator-(V2 a) { return V2{a.b ^ 0x8000000080000000ull}; }
+__device__ __forceinline__ V2 operator-(V2 a, V2 b) { return a + (-b); }
+__device__ __forceinline__ V2 operator*(V2 a, V2 b) {
+    V2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.b) : "l"(a.b), "l"(b.b));
+    return r;
+}
+__device__ __forceinline__ V2 operator+(float a, V2 b) { return v2(a) + b; }
+__device__ __forceinline__ V2 operator+(V2 a, float b) { return a + v2(b); }
+__device__ __forceinline__ V2 operator-(float a, V2 b) { return v2(a) - b; }
+__device__ __forceinline__ V2 operator-(V2 a, float b) { return a - v2(b); }
+__device__ __forceinline__ V2 operator*(float a, V2 b) { return v2(a) * b; }
+__device__ __forceinline__ V2 operator*(V2 a, float b) { return a * v2(b); }
+__device__ __forceinline__ V2 fmaf(V2 a, V2 b, V2 c) {
+    V2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.b) : "l"(a.b), "l"(b.b), "l"(c.b));
+    return r;
+}
+__device__ __forceinline__ V2 fmaf(float a, V2 b, V2 c) { return fmaf(v2(a), b, c); }
+__device__ __forceinline__ V2 fmaf(V2 a, float b, V2 c) { return fmaf(a, v2(b), c); }
+__device__ __forceinline__ V2 fmaf(V2 a, V2 b, float c) { return fmaf(a, b, v2(c)); }
+__device__ __forceinline__ V2 fmaf(float a, float b, V2 c) { return fmaf(v2(a), v2(b), c); }
+__device__ __forceinline__ V2 fmaf(float a, V2 b, float c) { return fmaf(v2(a), b, v2(c)); }
+__device__ __forceinline__ V2 fmaf(V2 a, float b, float c) { return fmaf(a, v2(b), v2(c)); }
+using ::fmaf;
+
 template <class T> __device__ __forceinline__ T zero_of();
 template <> __device__ __forceinline__ float zero_of<float>() { return 0.0f; }
+template <> __device__ __forceinline__ V2 zero_of<V2>() { return v2(0.0f); }
 
 template <class T>
 __device__ __forceinline__ void e1d(T u, T e[3], float w[3], T d[3]) {
@@ -70,20 +136,29 @@ __device__ __forceinline__ T cdot(int v, T a, T b) {
 
 // FORCED = false: the force of this step is zero everywhere (no gravity, no
 // Womersley term), so every forcing term is an exact zero and is not formed.
+// px, py: the momentum with the half force term, inv = 1/rho (ux = px inv,
+// uy = py inv). In BGK no product feeds an addition: c.u of a diagonal
+// direction is (px +- py) inv, and w (rho inner + dr) - g is one fused
+// multiply-add. A compiler that fuses a product into a following addition
+// (as one did for the packed two-site form) then has nothing to fuse, so the
+// one-site and two-site forms round identically.
 template <bool CM, bool FORCED, class T>
-__device__ __forceinline__ void collide_dev32(const T g[9], T dr, T rho, T mx, T my, T ux, T uy, float Gx, float Gy,
-                                              float omega, T gs[9]) {
+__device__ __forceinline__ void collide_dev32(const T g[9], T dr, T rho, T mx, T my, T ux, T uy, T px, T py, T inv,
+                                              float Gx, float Gy, float omega, T gs[9]) {
     if (!CM) {
         const T usq15 = 1.5f * fmaf(ux, ux, uy * uy);
         const T uF = FORCED ? fmaf(ux, Gx, uy * Gy) : zero_of<T>();
         const float fo = fmaf(-0.5f, omega, 1.0f);
+        const T cs = (px + py) * inv, cd = (px - py) * inv;  // c.u of (1,1) and (1,-1)
 #pragma unroll
         for (int v = 0; v < 9; v++) {
             const float w = wgt_f(v);
-            const T cu = cdot(v, ux, uy);
+            const int cx = cx_of(v), cy = cy_of(v);
+            const T cu = cy == 0 ? (cx == 0 ? zero_of<T>() : (cx > 0 ? ux : -ux))
+                       : cx == 0 ? (cy > 0 ? uy : -uy)
+                       : cx == cy ? (cx > 0 ? cs : -cs) : (cx > 0 ? cd : -cd);
             const T inner = fmaf(4.5f * cu, cu, fmaf(3.0f, cu, -usq15));
-            const T geq = w * fmaf(rho, inner, dr);
-            const T a = fmaf(omega, geq - g[v], g[v]);
+            const T a = fmaf(omega, fmaf(w, fmaf(rho, inner, dr), -g[v]), g[v]);
             if (FORCED) {
                 const float cF = cdot(v, Gx, Gy);
                 const T Fv = (3.0f * w) * fmaf(3.0f * cu, cF, cF - uF);
@@ -212,14 +287,15 @@ __device__ __forceinline__ void finish_site_lowp(const float g[9], typename S::T
     const float mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
     const float my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
     const float inv = __frcp_rn(rho);  // = 1.0f / rho, correctly rounded
-    const float ux = (FORCED ? fmaf(0.5f, Fxd, mx) : mx) * inv, uy = (FORCED ? fmaf(0.5f, Fyd, my) : my) * inv;
+    const float px = FORCED ? fmaf(0.5f, Fxd, mx) : mx, py = FORCED ? fmaf(0.5f, Fyd, my) : my;
+    const float ux = px * inv, uy = py * inv;
     if (L.convective && i >= L.Nx - 3) {
         const int c = i - (L.Nx - 3);
         L.outlet_u[((size_t)c * L.Ny + j) * 2 + 0] = ux;
         L.outlet_u[((size_t)c * L.Ny + j) * 2 + 1] = uy;
     }
     float gs[9];
-    collide_dev32<CM, FORCED>(g, dr, rho, mx, my, ux, uy, Gxd, Gyd, L.omega_f, gs);
+    collide_dev32<CM, FORCED>(g, dr, rho, mx, my, ux, uy, px, py, inv, Gxd, Gyd, L.omega_f, gs);
 #pragma unroll
     for (int v = 0; v < 9; v++) B[(size_t)v * L.S + base] = S::put(gs[v], v);
 }
@@ -410,6 +486,79 @@ __device__ __forceinline__ void tma_tile_sites(const unsigned char* stage, typen
     }
 }
 
+// FP16 BGK tiles with two x-adjacent sites per thread (an even column and the
+// next): half2 loads where the pulled pair is aligned (directions with no x
+// component), the collision in packed FP32x2 (V2), and one half2 store per
+// direction. Each lane computes exactly what finish_site_lowp computes for
+// its site (the same operations in the same order), so the results are the
+// same bits. Pairs with a site outside columns 1..Nx-2, or reaching the
+// convective outlet's last three columns (which also write side outputs),
+// take the one-site path.
+template <bool FORCED>
+__device__ __forceinline__ void tma_tile_pairs_f16(const unsigned char* stage, __half* __restrict__ B,
+                                                   const LatDev& L, int t, int i0, int j0) {
+    using S = StoreF16;
+    using TT = TmaTile<S>;
+    using SH = TmaShape<S>;
+    constexpr int PW = TT::W / 2;
+    const int ii = 2 * ((int)threadIdx.x % PW);
+    const int i = i0 + ii;
+    const bool full = i >= 1 && i + 1 <= L.Nx - 2 && !(L.convective && i + 1 >= L.Nx - 3);
+    for (int jj = (int)threadIdx.x / PW; jj < TT::H; jj += (int)blockDim.x / PW) {
+        const int j = j0 + jj;
+        if (j > L.Ny - 2) break;
+        if (!full) {
+            for (int q = 0; q < 2; q++) {
+                const int iq = i + q;
+                if (iq < 1 || iq > L.Nx - 2) continue;
+                float g[9];
+#pragma unroll
+                for (int v = 0; v < 9; v++) {
+                    const __half* plane = reinterpret_cast<const __half*>(stage + v * SH::PLANE);
+                    g[v] = S::dev(plane[(jj + 1 - cy_of(v)) * SH::Wb + (ii + q + TT::HALO - cx_of(v))], v);
+                }
+                finish_site_lowp<false, FORCED, S>(g, B, L, t, iq, j);
+            }
+            continue;
+        }
+        V2 g[9];
+#pragma unroll
+        for (int v = 0; v < 9; v++) {
+            const __half* plane = reinterpret_cast<const __half*>(stage + v * SH::PLANE);
+            const int at = (jj + 1 - cy_of(v)) * SH::Wb + (ii + TT::HALO - cx_of(v));
+            if (cx_of(v) == 0) {
+                // (ii + HALO) is even: an aligned pair, converted one half at
+                // a time as the one-site path does
+                const __half2 h = *reinterpret_cast<const __half2*>(plane + at);
+                g[v] = v2(__half2float(__low2half(h)), __half2float(__high2half(h))) * h16_scale(v);
+            } else {
+                g[v] = v2(__half2float(plane[at]), __half2float(plane[at + 1])) * h16_scale(v);
+            }
+        }
+        float Fxd = 0.0f, Fyd = 0.0f, Gxd = 0.0f, Gyd = 0.0f;
+        if (FORCED) {
+            force_xy_at_f(L, t, Fxd, Fyd);
+            force_xy_at_f(L, t + 1, Gxd, Gyd);
+        }
+        const V2 dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
+        const V2 rho = 1.0f + dr;
+        const V2 mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
+        const V2 my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
+        const V2 inv = v2(__frcp_rn(rho.x()), __frcp_rn(rho.y()));
+        const V2 px = FORCED ? fmaf(0.5f, Fxd, mx) : mx, py = FORCED ? fmaf(0.5f, Fyd, my) : my;
+        const V2 ux = px * inv, uy = py * inv;
+        V2 gs[9];
+        collide_dev32<false, FORCED>(g, dr, rho, mx, my, ux, uy, px, py, inv, Gxd, Gyd, L.omega_f, gs);
+        __half2* out = reinterpret_cast<__half2*>(B + (size_t)j * L.pitch + i);
+#pragma unroll
+        for (int v = 0; v < 9; v++) {
+            // one conversion per value, as the one-site path (S::put) rounds
+            const V2 o = gs[v] * h16_inv(v);
+            out[(size_t)v * (L.S >> 1)] = __halves2half2(__float2half_rn(o.x()), __float2half_rn(o.y()));
+        }
+    }
+}
+
 template <bool CM, class S>
 __global__ void __launch_bounds__(256, 3) k_step_tma(const __grid_constant__ CUtensorMap tm,
                                                   const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
@@ -467,8 +616,13 @@ __global__ void __launch_bounds__(256, 3) k_step_tma(const __grid_constant__ CUt
         __syncthreads();
         if (!s_ok) return;
         const int i0 = (tile % tiles_x) * TT::W, j0 = 1 + (tile / tiles_x) * TT::H;
-        if (forced) tma_tile_sites<CM, true, S>(smem + st * SH::STAGE, B, L, t, i0, j0);
-        else tma_tile_sites<CM, false, S>(smem + st * SH::STAGE, B, L, t, i0, j0);
+        if constexpr (std::is_same<S, StoreF16>::value && !CM) {
+            if (forced) tma_tile_pairs_f16<true>(smem + st * SH::STAGE, B, L, t, i0, j0);
+            else tma_tile_pairs_f16<false>(smem + st * SH::STAGE, B, L, t, i0, j0);
+        } else {
+            if (forced) tma_tile_sites<CM, true, S>(smem + st * SH::STAGE, B, L, t, i0, j0);
+            else tma_tile_sites<CM, false, S>(smem + st * SH::STAGE, B, L, t, i0, j0);
+        }
         __syncthreads();
     }
 }
