@@ -430,14 +430,24 @@ __global__ void __launch_bounds__(256, 6) k_step_lowp(const typename S::T* __res
 // boundary-condition sites and the periodic edge sites, as in k_step_lowp.
 template <class S>
 struct TmaTile;
+#ifndef LIFE_TMA_F16_H
+#define LIFE_TMA_F16_H 8
+#endif
+#ifndef LIFE_TMA_F16_STAGES
+#define LIFE_TMA_F16_STAGES 2
+#endif
+#ifndef LIFE_TMA_F16_CTAS
+#define LIFE_TMA_F16_CTAS 3
+#endif
 template <>
 struct TmaTile<StoreF16> {
-    static constexpr int W = 128, H = 8, HALO = 8, ELEM = 2;
+    static constexpr int W = 128, H = LIFE_TMA_F16_H, HALO = 8, ELEM = 2, STAGES = LIFE_TMA_F16_STAGES;
+    static constexpr int CTAS = LIFE_TMA_F16_CTAS;  // resident CTAs per SM the register budget is set for
     static constexpr CUtensorMapDataType DTYPE = CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
 };
 template <>
 struct TmaTile<StoreF32> {
-    static constexpr int W = 128, H = 4, HALO = 4, ELEM = 4;
+    static constexpr int W = 128, H = 4, HALO = 4, ELEM = 4, STAGES = 2, CTAS = 3;
     static constexpr CUtensorMapDataType DTYPE = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
 };
 template <class S>
@@ -446,9 +456,11 @@ struct TmaShape {
     static constexpr int BOX = Wb * Hb * TmaTile<S>::ELEM;  // bytes of one plane's box
     static constexpr int PLANE = (BOX + 127) / 128 * 128;   // 128-byte aligned plane slots
     static constexpr int STAGE = 9 * PLANE;
-    // two stages, two mbarriers and a flag, and slack to align the stages to
-    // 128 bytes (the bulk tensor copies' shared-memory alignment)
-    static constexpr int SMEM = 2 * STAGE + 128 + 128;
+    static constexpr int NST = TmaTile<S>::STAGES;
+    // the stages, one mbarrier per stage and a flag, and slack to align the
+    // stages to 128 bytes (the bulk tensor copies' shared-memory alignment)
+    static constexpr int SMEM = NST * STAGE + 128 + 128;
+    static_assert(8 * NST + 4 * (NST + 1) <= 128, "mbarriers and tile slots fit the 128-byte tail");
 };
 
 // Waits that gave up (never expected; the host turns a non-zero count into
@@ -560,11 +572,12 @@ __device__ __forceinline__ void tma_tile_pairs_f16(const unsigned char* stage, _
 }
 
 template <bool CM, class S>
-__global__ void __launch_bounds__(256, 3) k_step_tma(const __grid_constant__ CUtensorMap tm,
+__global__ void __launch_bounds__(256, TmaTile<S>::CTAS) k_step_tma(const __grid_constant__ CUtensorMap tm,
                                                   const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
                                                   LatDev L, int t, int pb, int tiles_x, int ntiles) {
     using TT = TmaTile<S>;
     using SH = TmaShape<S>;
+    constexpr int NST = SH::NST;
     t = step_t(L, t);
     if ((int)blockIdx.x < pb) {
         // boundary-condition sites; an edge site of a periodic wall is an
@@ -578,12 +591,13 @@ __global__ void __launch_bounds__(256, 3) k_step_tma(const __grid_constant__ CUt
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
                                                            ~static_cast<uintptr_t>(127));
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * SH::STAGE);
-    int& s_ok = *reinterpret_cast<int*>(smem + 2 * SH::STAGE + 16);
-    const int cta = (int)blockIdx.x - pb, ncta = (int)gridDim.x - pb;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NST * SH::STAGE);
+    int* s_tile = reinterpret_cast<int*>(smem + NST * SH::STAGE + 8 * NST);  // tile held by each stage, or -1
+    int& s_ok = s_tile[NST];
+    const int ncta = (int)gridDim.x - pb;
+    int* ctr = L.tile_ctr;  // [0]: tiles handed out, [1]: CTAs finished
     if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int q = 0; q < NST; q++) mbar_init(&bar[q], 1);
         mbar_fence_init();
     }
     __syncthreads();
@@ -594,27 +608,37 @@ __global__ void __launch_bounds__(256, 3) k_step_tma(const __grid_constant__ CUt
         for (int v = 0; v < 9; v++)
             tma_load_3d(smem + st * SH::STAGE + v * SH::PLANE, &tm, i0 - TT::HALO, j0 - 1, v, &bar[st]);
     };
-    if (threadIdx.x == 0 && cta < ntiles) issue(cta, 0);
+    // Tiles are handed out by a counter, so CTAs that start late (behind the
+    // boundary blocks) take fewer tiles and the step ends evenly. The stage of
+    // tile k+NST-1 is filled while tile k is computed; it is the stage tile
+    // k-1 used. The results do not depend on which CTA takes which tile.
+    auto grab = [&](int st) {
+        const int tile = atomicAdd(&ctr[0], 1);
+        s_tile[st] = tile < ntiles ? tile : -1;
+        if (tile < ntiles) issue(tile, st);
+    };
+    if (threadIdx.x == 0)
+        for (int q = 0; q < NST - 1; q++) grab(q);
     const bool forced = lattice_forced(L);
-    int k = 0;
-    for (int tile = cta; tile < ntiles; tile += ncta, k++) {
-        const int st = k & 1;
-        const bool next = tile + ncta < ntiles;
+    for (int k = 0;; k++) {
+        const int st = k % NST;
         if (threadIdx.x == 0) {
-            if (next) {
-                fence_proxy_async_smem();
-                issue(tile + ncta, st ^ 1);
-            }
-            s_ok = mbar_wait_bounded(&bar[st], (unsigned)(k >> 1) & 1u, 1u << 22) ? 1 : 0;
-            if (!s_ok) {
-                // give the copy in flight into the other stage time to land
+            fence_proxy_async_smem();
+            grab((k + NST - 1) % NST);
+            s_ok = 1;
+            if (s_tile[st] >= 0 && !mbar_wait_bounded(&bar[st], (unsigned)(k / NST) & 1u, 1u << 22)) {
+                // give the copies in flight into the other stages time to land
                 // before the CTA (and its shared memory) goes away
-                if (next) mbar_wait_bounded(&bar[st ^ 1], (unsigned)((k + 1) >> 1) & 1u, 1u << 22);
+                for (int q = 1; q < NST; q++)
+                    if (s_tile[(k + q) % NST] >= 0)
+                        mbar_wait_bounded(&bar[(k + q) % NST], (unsigned)((k + q) / NST) & 1u, 1u << 22);
                 atomicAdd(&g_tma_timeouts, 1);
+                s_ok = 0;
             }
         }
         __syncthreads();
-        if (!s_ok) return;
+        const int tile = s_tile[st];
+        if (tile < 0 || !s_ok) break;
         const int i0 = (tile % tiles_x) * TT::W, j0 = 1 + (tile / tiles_x) * TT::H;
         if constexpr (std::is_same<S, StoreF16>::value && !CM) {
             if (forced) tma_tile_pairs_f16<true>(smem + st * SH::STAGE, B, L, t, i0, j0);
@@ -624,6 +648,15 @@ __global__ void __launch_bounds__(256, 3) k_step_tma(const __grid_constant__ CUt
             else tma_tile_sites<CM, false, S>(smem + st * SH::STAGE, B, L, t, i0, j0);
         }
         __syncthreads();
+    }
+    // the last CTA to finish clears the counters for the next launch
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&ctr[1], 1) == ncta - 1) {
+            ctr[0] = 0;
+            ctr[1] = 0;
+            __threadfence();
+        }
     }
 }
 

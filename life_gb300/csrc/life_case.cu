@@ -229,6 +229,7 @@ LatDev life::lattice_view(const LifeCase* c, int t) {
     L.rho_next = c->d_rho_hist[t & 1];
     L.corner_prev = c->d_corner_u[(t - 1) & 1];
     L.corner_next = c->d_corner_u[t & 1];
+    L.tile_ctr = c->d_tile_ctr;
     return L;
 }
 
@@ -385,6 +386,7 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
         (rc = dev_alloc_t(c, &c->d_outlet_f[1], (size_t)p.Ny * 3)) ||
         (rc = dev_alloc_t(c, &c->d_delU, (size_t)p.Ny * 2)) || (rc = dev_alloc_t(c, &c->d_red, 4)) ||
         (rc = dev_alloc_t(c, &c->d_corner_u[0], 8)) || (rc = dev_alloc_t(c, &c->d_corner_u[1], 8)) ||
+        (rc = dev_alloc_t(c, &c->d_tile_ctr, 2)) ||
         (c->site_force && ((rc = dev_alloc_t(c, &c->d_rho_hist[0], plane)) ||
                            (rc = dev_alloc_t(c, &c->d_rho_hist[1], plane))))) {
         free_case(c);
@@ -393,6 +395,7 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
     cudaMemcpyAsync(c->d_u_in, u_in.data(), sizeof(double) * u_in.size(), cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(c->d_rho_in, rho_in.data(), sizeof(double) * rho_in.size(), cudaMemcpyHostToDevice, c->stream);
     cudaMemsetAsync(c->d_delU, 0, sizeof(double) * p.Ny * 2, c->stream);
+    cudaMemsetAsync(c->d_tile_ctr, 0, sizeof(int) * 2, c->stream);
     if (c->obj.hasIBM) {
         if ((rc = upload_markers(c))) {
             free_case(c);

@@ -78,6 +78,7 @@ struct LifeCase {
     bool site_force = false;
     double* d_rho_hist[2] = {nullptr, nullptr};
     double* d_corner_u[2] = {nullptr, nullptr};
+    int* d_tile_ctr = nullptr;  // LatDev::tile_ctr
     unsigned long long* d_red = nullptr;
     cudaStream_t stream = nullptr;   // every kernel of the case is ordered on this stream
     cudaStream_t side = nullptr;     // perimeter kernel, forked from and joined to `stream`

@@ -71,6 +71,10 @@ struct LatDev {
     // four corners, slot (i == Nx-1) + 2 (j == Ny-1), two components each.
     const double* corner_prev;
     double* corner_next;
+    // Two counters of the one-launch step kernel with staged tiles: step t
+    // hands out its tiles from tile_ctr[t & 1] and clears tile_ctr[(t+1) & 1]
+    // for the next step.
+    int* tile_ctr;
 };
 
 }  // namespace life
