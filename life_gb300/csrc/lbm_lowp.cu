@@ -437,7 +437,7 @@ struct TmaTile;
 #define LIFE_TMA_F16_STAGES 2
 #endif
 #ifndef LIFE_TMA_F16_CTAS
-#define LIFE_TMA_F16_CTAS 3
+#define LIFE_TMA_F16_CTAS 4
 #endif
 template <>
 struct TmaTile<StoreF16> {
