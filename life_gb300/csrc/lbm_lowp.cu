@@ -431,13 +431,13 @@ __global__ void __launch_bounds__(256, 6) k_step_lowp(const typename S::T* __res
 template <class S>
 struct TmaTile;
 #ifndef LIFE_TMA_F16_H
-#define LIFE_TMA_F16_H 8
+#define LIFE_TMA_F16_H 12
 #endif
 #ifndef LIFE_TMA_F16_STAGES
 #define LIFE_TMA_F16_STAGES 2
 #endif
 #ifndef LIFE_TMA_F16_CTAS
-#define LIFE_TMA_F16_CTAS 4
+#define LIFE_TMA_F16_CTAS 3
 #endif
 template <>
 struct TmaTile<StoreF16> {
@@ -454,13 +454,14 @@ template <class S>
 struct TmaShape {
     static constexpr int Wb = TmaTile<S>::W + 2 * TmaTile<S>::HALO, Hb = TmaTile<S>::H + 2;
     static constexpr int BOX = Wb * Hb * TmaTile<S>::ELEM;  // bytes of one plane's box
-    static constexpr int PLANE = (BOX + 127) / 128 * 128;   // 128-byte aligned plane slots
-    static constexpr int STAGE = 9 * PLANE;
+    // the nine planes of a tile arrive as one (Wb, Hb, 9) box, densely packed
+    static constexpr int PLANE = BOX;
+    static constexpr int STAGE = (9 * PLANE + 127) / 128 * 128;
     static constexpr int NST = TmaTile<S>::STAGES;
     // the stages, one mbarrier per stage and a flag, and slack to align the
     // stages to 128 bytes (the bulk tensor copies' shared-memory alignment)
     static constexpr int SMEM = NST * STAGE + 128 + 128;
-    static_assert(8 * NST + 4 * (NST + 1) <= 128, "mbarriers and tile slots fit the 128-byte tail");
+    static_assert(16 * NST + 4 * (NST + 1) <= 128, "mbarriers and tile slots fit the 128-byte tail");
 };
 
 // Waits that gave up (never expected; the host turns a non-zero count into
@@ -506,19 +507,18 @@ __device__ __forceinline__ void tma_tile_sites(const unsigned char* stage, typen
 // same bits. Pairs with a site outside columns 1..Nx-2, or reaching the
 // convective outlet's last three columns (which also write side outputs),
 // take the one-site path.
+// The pair of columns (ii, ii+1) of tile row jj.
 template <bool FORCED>
-__device__ __forceinline__ void tma_tile_pairs_f16(const unsigned char* stage, __half* __restrict__ B,
-                                                   const LatDev& L, int t, int i0, int j0) {
+__device__ __forceinline__ void tma_pair_f16(const unsigned char* stage, __half* __restrict__ B, const LatDev& L,
+                                             int t, int i0, int j0, int jj, int ii) {
     using S = StoreF16;
     using TT = TmaTile<S>;
     using SH = TmaShape<S>;
-    constexpr int PW = TT::W / 2;
-    const int ii = 2 * ((int)threadIdx.x % PW);
     const int i = i0 + ii;
     const bool full = i >= 1 && i + 1 <= L.Nx - 2 && !(L.convective && i + 1 >= L.Nx - 3);
-    for (int jj = (int)threadIdx.x / PW; jj < TT::H; jj += (int)blockDim.x / PW) {
+    {
         const int j = j0 + jj;
-        if (j > L.Ny - 2) break;
+        if (j > L.Ny - 2) return;
         if (!full) {
             for (int q = 0; q < 2; q++) {
                 const int iq = i + q;
@@ -531,7 +531,7 @@ __device__ __forceinline__ void tma_tile_pairs_f16(const unsigned char* stage, _
                 }
                 finish_site_lowp<false, FORCED, S>(g, B, L, t, iq, j);
             }
-            continue;
+            return;
         }
         V2 g[9];
 #pragma unroll
@@ -571,6 +571,115 @@ __device__ __forceinline__ void tma_tile_pairs_f16(const unsigned char* stage, _
     }
 }
 
+// A whole tile by the CTA (the pairs of 64 columns on rows threadIdx / 64).
+template <bool FORCED>
+__device__ __forceinline__ void tma_tile_pairs_f16(const unsigned char* stage, __half* __restrict__ B,
+                                                   const LatDev& L, int t, int i0, int j0) {
+    constexpr int PW = TmaTile<StoreF16>::W / 2;
+    const int ii = 2 * ((int)threadIdx.x % PW);
+    for (int jj = (int)threadIdx.x / PW; jj < TmaTile<StoreF16>::H; jj += (int)blockDim.x / PW)
+        tma_pair_f16<FORCED>(stage, B, L, t, i0, j0, jj, ii);
+}
+
+// The last CTA of a launch to finish clears the tile counters for the next
+// launch (called once by every persistent CTA, after its last tile).
+__device__ __forceinline__ void step_tma_done(int* ctr, int ncta) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&ctr[1], 1) == ncta - 1) {
+            ctr[0] = 0;
+            ctr[1] = 0;
+            __threadfence();
+        }
+    }
+}
+
+// FP16 BGK tiles with a pipeline per warp instead of CTA barriers: the warps
+// share each tile's site pairs (two sites per lane per pass). Stage s has a
+// "full" mbarrier (the producer's arrival with the copies' byte count, or a
+// plain arrival with tile -1 when the counter is exhausted) and an "empty"
+// mbarrier that every warp arrives on when it has read the stage. Thread 0 is
+// also the producer: before computing tile k it refills the stage of tile
+// k-1 with tile k+NST-1 once all warps have released it. A warp therefore
+// waits only for its own data and, through the producer, for the slowest
+// warp two tiles back, not for every warp at every tile.
+__device__ __forceinline__ void tma_tiles_by_warp(const CUtensorMap& tm, __half* __restrict__ B, const LatDev& L,
+                                                  int t, int tiles_x, int ntiles, unsigned char* smem) {
+    using S = StoreF16;
+    using TT = TmaTile<S>;
+    using SH = TmaShape<S>;
+    constexpr int NST = SH::NST, NW = 8;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + NST * SH::STAGE);
+    uint64_t* empty = full + NST;
+    int* s_tile = reinterpret_cast<int*>(empty + NST);  // tile held by each stage, or -1
+    int& s_err = s_tile[NST];
+    int* ctr = L.tile_ctr;
+    const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < NST; q++) {
+            mbar_init(&full[q], 1);
+            mbar_init(&empty[q], NW);
+        }
+        s_err = 0;
+        mbar_fence_init();
+    }
+    __syncthreads();
+    // producer state (thread 0): stage fills so far, whether tiles ran out
+    int fills[NST] = {0};
+    bool out = false;
+    auto fill = [&](int st) {
+        const int tile = atomicAdd(&ctr[0], 1);
+        s_tile[st] = tile < ntiles ? tile : -1;
+        fills[st]++;
+        if (tile < ntiles) {
+            const int i0 = (tile % tiles_x) * TT::W, j0 = 1 + (tile / tiles_x) * TT::H;
+            mbar_arrive_expect_tx(&full[st], 9u * SH::BOX);
+            tma_load_3d(smem + st * SH::STAGE, &tm, i0 - TT::HALO, j0 - 1, 0, &full[st]);
+        } else {
+            out = true;
+            mbar_arrive(&full[st]);
+        }
+    };
+    if (threadIdx.x == 0)
+        for (int q = 0; q < NST - 1 && !out; q++) fill(q);
+    const bool forced = lattice_forced(L);
+    for (int k = 0;; k++) {
+        const int st = k % NST;
+        if (threadIdx.x == 0 && !out) {
+            const int kp = k + NST - 1, sp = kp % NST;
+            // the stage's previous tile (kp - NST) must be released by all warps
+            if (kp < NST || mbar_wait_bounded(&empty[sp], (unsigned)(kp / NST - 1) & 1u, 1u << 22)) {
+                fence_proxy_async_smem();
+                fill(sp);
+            } else {
+                atomicAdd(&g_tma_timeouts, 1);
+                s_err = 1;
+                out = true;
+            }
+        }
+        if (!mbar_wait_bounded(&full[st], (unsigned)(k / NST) & 1u, 1u << 22)) {
+            if (lane == 0) atomicAdd(&g_tma_timeouts, 1);
+            break;
+        }
+        const int tile = s_tile[st];
+        if (tile < 0 || *(volatile int*)&s_err) break;
+        const int i0 = (tile % tiles_x) * TT::W, j0 = 1 + (tile / tiles_x) * TT::H;
+        // pair p of the tile: row p / 64, columns 2 (p % 64) and the next
+        for (int p = warp * 32 + lane; p < TT::H * (TT::W / 2); p += NW * 32) {
+            if (forced) tma_pair_f16<true>(smem + st * SH::STAGE, B, L, t, i0, j0, p / (TT::W / 2), 2 * (p % (TT::W / 2)));
+            else tma_pair_f16<false>(smem + st * SH::STAGE, B, L, t, i0, j0, p / (TT::W / 2), 2 * (p % (TT::W / 2)));
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);
+    }
+    __syncthreads();
+    // copies still in flight (after a timeout) land before the CTA leaves
+    if (threadIdx.x == 0)
+        for (int q = 0; q < NST; q++)
+            if (fills[q] > 0) mbar_wait_bounded(&full[q], (unsigned)(fills[q] - 1) & 1u, 1u << 22);
+}
+
 template <bool CM, class S>
 __global__ void __launch_bounds__(256, TmaTile<S>::CTAS) k_step_tma(const __grid_constant__ CUtensorMap tm,
                                                   const typename S::T* __restrict__ A, typename S::T* __restrict__ B,
@@ -591,11 +700,16 @@ __global__ void __launch_bounds__(256, TmaTile<S>::CTAS) k_step_tma(const __grid
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
                                                            ~static_cast<uintptr_t>(127));
+    const int ncta = (int)gridDim.x - pb;
+    int* ctr = L.tile_ctr;  // [0]: tiles handed out, [1]: CTAs finished
+    if constexpr (std::is_same<S, StoreF16>::value && !CM) {
+        tma_tiles_by_warp(tm, B, L, t, tiles_x, ntiles, smem);
+        step_tma_done(ctr, ncta);
+        return;
+    }
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + NST * SH::STAGE);
     int* s_tile = reinterpret_cast<int*>(smem + NST * SH::STAGE + 8 * NST);  // tile held by each stage, or -1
     int& s_ok = s_tile[NST];
-    const int ncta = (int)gridDim.x - pb;
-    int* ctr = L.tile_ctr;  // [0]: tiles handed out, [1]: CTAs finished
     if (threadIdx.x == 0) {
         for (int q = 0; q < NST; q++) mbar_init(&bar[q], 1);
         mbar_fence_init();
@@ -604,9 +718,7 @@ __global__ void __launch_bounds__(256, TmaTile<S>::CTAS) k_step_tma(const __grid
     auto issue = [&](int tile, int st) {
         const int i0 = (tile % tiles_x) * TT::W, j0 = 1 + (tile / tiles_x) * TT::H;
         mbar_arrive_expect_tx(&bar[st], 9u * SH::BOX);
-#pragma unroll 1
-        for (int v = 0; v < 9; v++)
-            tma_load_3d(smem + st * SH::STAGE + v * SH::PLANE, &tm, i0 - TT::HALO, j0 - 1, v, &bar[st]);
+        tma_load_3d(smem + st * SH::STAGE, &tm, i0 - TT::HALO, j0 - 1, 0, &bar[st]);
     };
     // Tiles are handed out by a counter, so CTAs that start late (behind the
     // boundary blocks) take fewer tiles and the step ends evenly. The stage of
@@ -640,24 +752,11 @@ __global__ void __launch_bounds__(256, TmaTile<S>::CTAS) k_step_tma(const __grid
         const int tile = s_tile[st];
         if (tile < 0 || !s_ok) break;
         const int i0 = (tile % tiles_x) * TT::W, j0 = 1 + (tile / tiles_x) * TT::H;
-        if constexpr (std::is_same<S, StoreF16>::value && !CM) {
-            if (forced) tma_tile_pairs_f16<true>(smem + st * SH::STAGE, B, L, t, i0, j0);
-            else tma_tile_pairs_f16<false>(smem + st * SH::STAGE, B, L, t, i0, j0);
-        } else {
-            if (forced) tma_tile_sites<CM, true, S>(smem + st * SH::STAGE, B, L, t, i0, j0);
-            else tma_tile_sites<CM, false, S>(smem + st * SH::STAGE, B, L, t, i0, j0);
-        }
+        if (forced) tma_tile_sites<CM, true, S>(smem + st * SH::STAGE, B, L, t, i0, j0);
+        else tma_tile_sites<CM, false, S>(smem + st * SH::STAGE, B, L, t, i0, j0);
         __syncthreads();
     }
-    // the last CTA to finish clears the counters for the next launch
-    if (threadIdx.x == 0) {
-        __threadfence();
-        if (atomicAdd(&ctr[1], 1) == ncta - 1) {
-            ctr[0] = 0;
-            ctr[1] = 0;
-            __threadfence();
-        }
-    }
+    step_tma_done(ctr, ncta);
 }
 
 // The tensor map of one population buffer: dims (pitch, Ny, 9 planes), box
@@ -677,7 +776,7 @@ static cudaError_t plane_tensor_map(CUtensorMap* tm, const void* base, const Lat
     using SH = TmaShape<S>;
     const cuuint64_t dims[3] = {(cuuint64_t)L.pitch, (cuuint64_t)L.Ny, 9};
     const cuuint64_t strides[2] = {(cuuint64_t)L.pitch * TT::ELEM, (cuuint64_t)L.S * TT::ELEM};
-    const cuuint32_t box[3] = {(cuuint32_t)SH::Wb, (cuuint32_t)SH::Hb, 1};
+    const cuuint32_t box[3] = {(cuuint32_t)SH::Wb, (cuuint32_t)SH::Hb, 9};
     const cuuint32_t estr[3] = {1, 1, 1};
     const CUresult r = encode(tm, TT::DTYPE, 3, const_cast<void*>(base), dims, strides, box, estr,
                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
