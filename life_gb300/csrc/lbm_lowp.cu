@@ -418,16 +418,17 @@ __global__ void __launch_bounds__(256, 6) k_step_lowp(const typename S::T* __res
 
 // ---- TMA-staged tiles ---------------------------------------------------
 //
-// A persistent CTA walks the interior tiles (W x H sites of rows 1..Ny-2 and
-// columns 1..Nx-2). For each tile one thread issues nine bulk tensor copies
-// (one per population plane) of the tile plus a halo of one row above and
-// below and HALO sites left and right (HALO keeps the box start on a 16-byte
-// boundary), into one of two shared-memory stages, while the CTA computes the
-// tile of the other stage; the copies' completion is counted on the stage's
-// mbarrier. The sites then read their nine pulled populations from shared
-// memory and finish exactly as in the one-site path (finish_site_lowp), so
-// the results are the same bits. The first blocks of the grid take the
-// boundary-condition sites and the periodic edge sites, as in k_step_lowp.
+// Persistent CTAs take the interior tiles (W x H sites of rows 1..Ny-2 and
+// columns 1..Nx-2) from a counter. For each tile one thread issues one bulk
+// tensor copy of the tile plus a halo of one row above and below and HALO
+// sites left and right (HALO keeps the box start on a 16-byte boundary), for
+// all nine population planes, into one of the shared-memory stages, while the
+// CTA computes an earlier tile; the copy's completion is counted on the
+// stage's mbarrier. The sites then read their nine pulled populations from
+// shared memory and finish exactly as in the one-site path
+// (finish_site_lowp), so the results are the same bits. The first blocks of
+// the grid take the boundary-condition sites and the periodic edge sites, as
+// in k_step_lowp.
 template <class S>
 struct TmaTile;
 #ifndef LIFE_TMA_F16_H
