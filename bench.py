@@ -845,7 +845,7 @@ def run_gb300(args, world, rank, local):
                          "frac": round(achieved / hbm, 4), "traffic": traffic,
                          "peak_source": f"{hbm_kind} hbm_gbs",
                          "kernel": ("k_interior_f64<BGK> + k_perimeter" if args.storage == "fp64" else
-                                    f"k_step_lowp<BGK,{form[2].upper()}> (boundary perimeter + interior, one launch per step)"),
+                                    f"k_step_tma<BGK,{form[2].upper()}> (boundary perimeter + TMA-staged interior tiles, one launch per step)"),
                          "algorithmic_bytes_per_site": bytes_per_site, "kernel_ms": round(inner_ms, 4)},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e, 1), "unit": "MLUPS", "h2d_bytes_per_step": round(h2d / args.steps),

@@ -446,9 +446,15 @@ struct TmaTile<StoreF16> {
     static constexpr int CTAS = LIFE_TMA_F16_CTAS;  // resident CTAs per SM the register budget is set for
     static constexpr CUtensorMapDataType DTYPE = CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
 };
+#ifndef LIFE_TMA_F32_H
+#define LIFE_TMA_F32_H 8
+#endif
+#ifndef LIFE_TMA_F32_CTAS
+#define LIFE_TMA_F32_CTAS 2
+#endif
 template <>
 struct TmaTile<StoreF32> {
-    static constexpr int W = 128, H = 4, HALO = 4, ELEM = 4, STAGES = 2, CTAS = 3;
+    static constexpr int W = 128, H = LIFE_TMA_F32_H, HALO = 4, ELEM = 4, STAGES = 2, CTAS = LIFE_TMA_F32_CTAS;
     static constexpr CUtensorMapDataType DTYPE = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
 };
 template <class S>
@@ -500,86 +506,94 @@ __device__ __forceinline__ void tma_tile_sites(const unsigned char* stage, typen
     }
 }
 
-// FP16 BGK tiles with two x-adjacent sites per thread (an even column and the
-// next): half2 loads where the pulled pair is aligned (directions with no x
-// component), the collision in packed FP32x2 (V2), and one half2 store per
+// Two adjacent stored values as FP32 deviations, and back, exactly as
+// S::dev / S::put treat each one (the FP16 values are converted one at a time).
+template <class S>
+struct PairIO;
+template <>
+struct PairIO<StoreF16> {
+    __device__ static __forceinline__ V2 load2(const __half* p, int v) {  // p 4-byte aligned
+        const __half2 h = *reinterpret_cast<const __half2*>(p);
+        return v2(__half2float(__low2half(h)), __half2float(__high2half(h))) * h16_scale(v);
+    }
+    __device__ static __forceinline__ V2 load11(const __half* p, int v) {
+        return v2(__half2float(p[0]), __half2float(p[1])) * h16_scale(v);
+    }
+    __device__ static __forceinline__ void store2(__half* p, V2 g, int v) {  // p 4-byte aligned
+        const V2 o = g * h16_inv(v);
+        *reinterpret_cast<__half2*>(p) = __halves2half2(__float2half_rn(o.x()), __float2half_rn(o.y()));
+    }
+};
+template <>
+struct PairIO<StoreF32> {
+    __device__ static __forceinline__ V2 load2(const float* p, int) {  // p 8-byte aligned
+        const float2 f = *reinterpret_cast<const float2*>(p);
+        return v2(f.x, f.y);
+    }
+    __device__ static __forceinline__ V2 load11(const float* p, int) { return v2(p[0], p[1]); }
+    __device__ static __forceinline__ void store2(float* p, V2 g, int) {  // p 8-byte aligned
+        *reinterpret_cast<float2*>(p) = make_float2(g.x(), g.y());
+    }
+};
+
+// BGK tiles with two x-adjacent sites per thread (an even column and the
+// next): paired loads where the pulled pair is aligned (directions with no x
+// component), the collision in packed FP32x2 (V2), and one paired store per
 // direction. Each lane computes exactly what finish_site_lowp computes for
 // its site (the same operations in the same order), so the results are the
 // same bits. Pairs with a site outside columns 1..Nx-2, or reaching the
 // convective outlet's last three columns (which also write side outputs),
 // take the one-site path.
 // The pair of columns (ii, ii+1) of tile row jj.
-template <bool FORCED>
-__device__ __forceinline__ void tma_pair_f16(const unsigned char* stage, __half* __restrict__ B, const LatDev& L,
-                                             int t, int i0, int j0, int jj, int ii) {
-    using S = StoreF16;
+template <bool FORCED, class S>
+__device__ __forceinline__ void tma_pair(const unsigned char* stage, typename S::T* __restrict__ B, const LatDev& L,
+                                         int t, int i0, int j0, int jj, int ii) {
+    using T = typename S::T;
     using TT = TmaTile<S>;
     using SH = TmaShape<S>;
     const int i = i0 + ii;
     const bool full = i >= 1 && i + 1 <= L.Nx - 2 && !(L.convective && i + 1 >= L.Nx - 3);
-    {
-        const int j = j0 + jj;
-        if (j > L.Ny - 2) return;
-        if (!full) {
-            for (int q = 0; q < 2; q++) {
-                const int iq = i + q;
-                if (iq < 1 || iq > L.Nx - 2) continue;
-                float g[9];
+    const int j = j0 + jj;
+    if (j > L.Ny - 2) return;
+    if (!full) {
+        for (int q = 0; q < 2; q++) {
+            const int iq = i + q;
+            if (iq < 1 || iq > L.Nx - 2) continue;
+            float g[9];
 #pragma unroll
-                for (int v = 0; v < 9; v++) {
-                    const __half* plane = reinterpret_cast<const __half*>(stage + v * SH::PLANE);
-                    g[v] = S::dev(plane[(jj + 1 - cy_of(v)) * SH::Wb + (ii + q + TT::HALO - cx_of(v))], v);
-                }
-                finish_site_lowp<false, FORCED, S>(g, B, L, t, iq, j);
+            for (int v = 0; v < 9; v++) {
+                const T* plane = reinterpret_cast<const T*>(stage + v * SH::PLANE);
+                g[v] = S::dev(plane[(jj + 1 - cy_of(v)) * SH::Wb + (ii + q + TT::HALO - cx_of(v))], v);
             }
-            return;
+            finish_site_lowp<false, FORCED, S>(g, B, L, t, iq, j);
         }
-        V2 g[9];
-#pragma unroll
-        for (int v = 0; v < 9; v++) {
-            const __half* plane = reinterpret_cast<const __half*>(stage + v * SH::PLANE);
-            const int at = (jj + 1 - cy_of(v)) * SH::Wb + (ii + TT::HALO - cx_of(v));
-            if (cx_of(v) == 0) {
-                // (ii + HALO) is even: an aligned pair, converted one half at
-                // a time as the one-site path does
-                const __half2 h = *reinterpret_cast<const __half2*>(plane + at);
-                g[v] = v2(__half2float(__low2half(h)), __half2float(__high2half(h))) * h16_scale(v);
-            } else {
-                g[v] = v2(__half2float(plane[at]), __half2float(plane[at + 1])) * h16_scale(v);
-            }
-        }
-        float Fxd = 0.0f, Fyd = 0.0f, Gxd = 0.0f, Gyd = 0.0f;
-        if (FORCED) {
-            force_xy_at_f(L, t, Fxd, Fyd);
-            force_xy_at_f(L, t + 1, Gxd, Gyd);
-        }
-        const V2 dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
-        const V2 rho = 1.0f + dr;
-        const V2 mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
-        const V2 my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
-        const V2 inv = v2(__frcp_rn(rho.x()), __frcp_rn(rho.y()));
-        const V2 px = FORCED ? fmaf(0.5f, Fxd, mx) : mx, py = FORCED ? fmaf(0.5f, Fyd, my) : my;
-        const V2 ux = px * inv, uy = py * inv;
-        V2 gs[9];
-        collide_dev32<false, FORCED>(g, dr, rho, mx, my, ux, uy, px, py, inv, Gxd, Gyd, L.omega_f, gs);
-        __half2* out = reinterpret_cast<__half2*>(B + (size_t)j * L.pitch + i);
-#pragma unroll
-        for (int v = 0; v < 9; v++) {
-            // one conversion per value, as the one-site path (S::put) rounds
-            const V2 o = gs[v] * h16_inv(v);
-            out[(size_t)v * (L.S >> 1)] = __halves2half2(__float2half_rn(o.x()), __float2half_rn(o.y()));
-        }
+        return;
     }
-}
-
-// A whole tile by the CTA (the pairs of 64 columns on rows threadIdx / 64).
-template <bool FORCED>
-__device__ __forceinline__ void tma_tile_pairs_f16(const unsigned char* stage, __half* __restrict__ B,
-                                                   const LatDev& L, int t, int i0, int j0) {
-    constexpr int PW = TmaTile<StoreF16>::W / 2;
-    const int ii = 2 * ((int)threadIdx.x % PW);
-    for (int jj = (int)threadIdx.x / PW; jj < TmaTile<StoreF16>::H; jj += (int)blockDim.x / PW)
-        tma_pair_f16<FORCED>(stage, B, L, t, i0, j0, jj, ii);
+    V2 g[9];
+#pragma unroll
+    for (int v = 0; v < 9; v++) {
+        const T* plane = reinterpret_cast<const T*>(stage + v * SH::PLANE);
+        const int at = (jj + 1 - cy_of(v)) * SH::Wb + (ii + TT::HALO - cx_of(v));
+        // (ii + HALO) is even: the pair of a direction with no x component is aligned
+        g[v] = cx_of(v) == 0 ? PairIO<S>::load2(plane + at, v) : PairIO<S>::load11(plane + at, v);
+    }
+    float Fxd = 0.0f, Fyd = 0.0f, Gxd = 0.0f, Gyd = 0.0f;
+    if (FORCED) {
+        force_xy_at_f(L, t, Fxd, Fyd);
+        force_xy_at_f(L, t + 1, Gxd, Gyd);
+    }
+    const V2 dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
+    const V2 rho = 1.0f + dr;
+    const V2 mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
+    const V2 my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
+    const V2 inv = v2(__frcp_rn(rho.x()), __frcp_rn(rho.y()));
+    const V2 px = FORCED ? fmaf(0.5f, Fxd, mx) : mx, py = FORCED ? fmaf(0.5f, Fyd, my) : my;
+    const V2 ux = px * inv, uy = py * inv;
+    V2 gs[9];
+    collide_dev32<false, FORCED>(g, dr, rho, mx, my, ux, uy, px, py, inv, Gxd, Gyd, L.omega_f, gs);
+    T* out = B + (size_t)j * L.pitch + i;
+#pragma unroll
+    for (int v = 0; v < 9; v++) PairIO<S>::store2(out + (size_t)v * L.S, gs[v], v);
 }
 
 // The last CTA of a launch to finish clears the tile counters for the next
@@ -596,7 +610,7 @@ __device__ __forceinline__ void step_tma_done(int* ctr, int ncta) {
     }
 }
 
-// FP16 BGK tiles with a pipeline per warp instead of CTA barriers: the warps
+// BGK tiles with a pipeline per warp instead of CTA barriers: the warps
 // share each tile's site pairs (two sites per lane per pass). Stage s has a
 // "full" mbarrier (the producer's arrival with the copies' byte count, or a
 // plain arrival with tile -1 when the counter is exhausted) and an "empty"
@@ -605,9 +619,10 @@ __device__ __forceinline__ void step_tma_done(int* ctr, int ncta) {
 // k-1 with tile k+NST-1 once all warps have released it. A warp therefore
 // waits only for its own data and, through the producer, for the slowest
 // warp two tiles back, not for every warp at every tile.
-__device__ __forceinline__ void tma_tiles_by_warp(const CUtensorMap& tm, __half* __restrict__ B, const LatDev& L,
-                                                  int t, int tiles_x, int ntiles, unsigned char* smem) {
-    using S = StoreF16;
+template <class S>
+__device__ __forceinline__ void tma_tiles_by_warp(const CUtensorMap& tm, typename S::T* __restrict__ B,
+                                                  const LatDev& L, int t, int tiles_x, int ntiles,
+                                                  unsigned char* smem) {
     using TT = TmaTile<S>;
     using SH = TmaShape<S>;
     constexpr int NST = SH::NST, NW = 8;
@@ -668,8 +683,8 @@ __device__ __forceinline__ void tma_tiles_by_warp(const CUtensorMap& tm, __half*
         const int i0 = (tile % tiles_x) * TT::W, j0 = 1 + (tile / tiles_x) * TT::H;
         // pair p of the tile: row p / 64, columns 2 (p % 64) and the next
         for (int p = warp * 32 + lane; p < TT::H * (TT::W / 2); p += NW * 32) {
-            if (forced) tma_pair_f16<true>(smem + st * SH::STAGE, B, L, t, i0, j0, p / (TT::W / 2), 2 * (p % (TT::W / 2)));
-            else tma_pair_f16<false>(smem + st * SH::STAGE, B, L, t, i0, j0, p / (TT::W / 2), 2 * (p % (TT::W / 2)));
+            if (forced) tma_pair<true, S>(smem + st * SH::STAGE, B, L, t, i0, j0, p / (TT::W / 2), 2 * (p % (TT::W / 2)));
+            else tma_pair<false, S>(smem + st * SH::STAGE, B, L, t, i0, j0, p / (TT::W / 2), 2 * (p % (TT::W / 2)));
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[st]);
@@ -703,8 +718,8 @@ __global__ void __launch_bounds__(256, TmaTile<S>::CTAS) k_step_tma(const __grid
                                                            ~static_cast<uintptr_t>(127));
     const int ncta = (int)gridDim.x - pb;
     int* ctr = L.tile_ctr;  // [0]: tiles handed out, [1]: CTAs finished
-    if constexpr (std::is_same<S, StoreF16>::value && !CM) {
-        tma_tiles_by_warp(tm, B, L, t, tiles_x, ntiles, smem);
+    if constexpr (!CM) {
+        tma_tiles_by_warp<S>(tm, B, L, t, tiles_x, ntiles, smem);
         step_tma_done(ctr, ncta);
         return;
     }
@@ -819,12 +834,12 @@ int tma_timeouts() {
     return h;
 }
 
-// Which step kernel a reduced-precision case uses: the TMA-staged tiles for
-// FP16 storage (whose one-site kernel is bound by instruction issue and load
-// latency, not by HBM), the one-site kernel for FP32 storage (within 10 % of
-// the HBM roofline already; the staged tiles' halo rows cost it more than the
-// staging saves). LIFE_STEP_KERNEL=site|tma overrides, for measurements and
-// for the tests that compare the two bit for bit.
+// Which step kernel a reduced-precision case uses: the TMA-staged tiles
+// (k_step_tma) for both storage forms; the one-site kernel (k_step_lowp) is
+// kept for comparison. Measured at 4096^2: FP16 95.6-99.6k (one-site) against
+// 140-145k MLUPS (staged), FP32 85.8-86.3k against 90.2-90.9k.
+// LIFE_STEP_KERNEL=site|tma overrides, for measurements and for the tests
+// that compare the two bit for bit.
 enum { STEP_SITE = 1, STEP_TMA = 3 };
 static int step_kernel(int prec) {
     static int forced = -1;
@@ -835,7 +850,8 @@ static int step_kernel(int prec) {
         else if (e && !strcmp(e, "tma")) forced = STEP_TMA;
     }
     if (forced) return forced;
-    return prec == LIFE_PREC_F16 ? STEP_TMA : STEP_SITE;
+    (void)prec;
+    return STEP_TMA;
 }
 
 cudaError_t launch_step_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {

@@ -1,11 +1,11 @@
 """The one-launch step kernels of the reduced-precision forms (lattices of
 2^22 sites or more) against each other and against the separate perimeter +
 interior kernels of the host-driven loop: k_step_tma (TMA-staged tiles, the
-FP16 form's default, LIFE_STEP_KERNEL=tma), k_step_lowp (one site per thread,
-the FP32 form's default, LIFE_STEP_KERNEL=site) and
-LIFE_CASE_HOSTLOOP=1 must give the same bits after N steps, for BGK and
-central moments, with and without a step force, with a convective outlet,
-periodic x walls and an odd width."""
+default of both forms, LIFE_STEP_KERNEL=tma; BGK takes two sites per thread
+with packed f32x2 arithmetic), k_step_lowp (one site per thread,
+LIFE_STEP_KERNEL=site) and LIFE_CASE_HOSTLOOP=1 must give the same bits after
+N steps, for BGK and central moments, with and without a step force, with a
+convective outlet, periodic x walls and an odd width."""
 import os
 import subprocess
 import sys
