@@ -153,10 +153,8 @@ static int upload_case_table(LifeBatch* b) {
 // FP64 chains; on smaller lattices the separate perimeter kernel (no register
 // cap, so no spills) runs beside the interior instead.
 static bool fused_step(const LifeBatch* b) {
-    if (b->cases.size() != 1 || b->prec == LIFE_PREC_F64) return false;
-    const LifeCase* c = b->cases[0];
     // (a per-site force is taken only by the separate interior kernel)
-    return !c->site_force && (long long)c->Nx * c->Ny >= (1LL << 22);
+    return b->cases.size() == 1 && case_fused_step(b->cases[0]);
 }
 
 static cudaError_t launch_batch_interior(LifeBatch* b, int phase, cudaStream_t s) {
@@ -439,6 +437,14 @@ static int self_batch(LifeCase* c) {
     b->ring_end.assign(1, 0);
     c->self_batch = b;
     return LIFE_OK;
+}
+
+bool case_graphs_ready(const LifeCase* c) {
+    return c->self_batch && c->self_batch->exec[0] && c->self_batch->exec[1];
+}
+
+bool case_fused_step(const LifeCase* c) {
+    return c->p.precision != LIFE_PREC_F64 && !c->site_force && (long long)c->Nx * c->Ny >= (1LL << 22);
 }
 
 int case_graph_steps(LifeCase* c, int nsteps, cudaEvent_t start, cudaEvent_t stop) {

@@ -3,7 +3,7 @@
 // form shares (boundary sites, start-up, restart, export). Compiled with
 // --fmad=false (see the header of lbm_device.cuh).
 //
-//   k_init          initial equilibrium state and the first collision
+//   k_init_rows/fill initial equilibrium state and the first collision
 //   k_interior_f64  fused pull-stream + macroscopic + collision of the next
 //                   step for fluid sites (one read and one write of the nine
 //                   populations per site)
@@ -15,6 +15,8 @@
 //   k_maxvel        max |u| and NaN scan
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "collide_cm.cuh"
 #include "lbm_device.cuh"
 #include "lbm_kernels.h"
@@ -22,48 +24,54 @@
 namespace life {
 
 // GridClass::initialiseGrid (reference src/Grid.cpp:998-1061): rho = 1,
-// initial velocity, f = feq; then the collision of step t0+1.
+// initial velocity, f = feq; then the collision of step t0+1. Every site of
+// row j starts from the equilibrium at rho = 1 of one of two velocities: the
+// row's (uniform, or the inlet profile at j) or zero at a wall site. The two
+// variants of every row are formed once (k_init_rows: a thread per row and
+// variant, the FP64 chain of store_collided's arithmetic), then every site
+// stores its variant (k_init_fill, a write of the lattice).
+template <class S>
+struct InitRow {
+    typename S::T out[9];  // the stored populations after the first collision
+    double f[9], u[2];     // the state before it (outlet side outputs, corner history)
+};
+
 template <bool CM, class S>
-__global__ void k_init(typename S::T* __restrict__ B, LatDev L, int t0) {
-    // Every site of row j starts from the equilibrium at rho = 1 of one of two
-    // velocities: the row's (uniform, or the inlet profile at j) or zero at a
-    // wall site. Two threads form the two variants' populations and their
-    // collision for the first step (store_collided's arithmetic) once; every
-    // site then stores its variant.
-    __shared__ typename S::T s_out[2][9];
-    __shared__ double s_f[2][9];
-    __shared__ double s_u[2][2];
-    const int j = blockIdx.y;
-    if (threadIdx.x < 2) {
-        const int w = threadIdx.x;
-        double ux, uy;
-        if (w == 1 || L.init_mode == 0) { ux = 0.0; uy = 0.0; }
-        else if (L.init_mode == 1) { ux = L.u_in[j * 2]; uy = L.u_in[j * 2 + 1]; }
-        else { ux = L.u0x; uy = L.u0y; }
-        const double rho = 1.0;
-        double f[9], fs[9], Fx, Fy;
+__global__ void k_init_rows(InitRow<S>* __restrict__ rows, LatDev L, int t0) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = k >> 1, w = k & 1;
+    if (j >= L.Ny) return;
+    double ux, uy;
+    if (w == 1 || L.init_mode == 0) { ux = 0.0; uy = 0.0; }
+    else if (L.init_mode == 1) { ux = L.u_in[j * 2]; uy = L.u_in[j * 2 + 1]; }
+    else { ux = L.u0x; uy = L.u0y; }
+    const double rho = 1.0;
+    double f[9], fs[9], Fx, Fy;
 #pragma unroll
-        for (int v = 0; v < 9; v++) f[v] = equilibrium<CM>(v, rho, ux, uy);
-        force_xy_next(L, t0 + 1, rho, Fx, Fy);
-        collide<CM>(f, rho, ux, uy, Fx + 0.0, Fy + 0.0, L.omega, L.cs, fs);
+    for (int v = 0; v < 9; v++) f[v] = equilibrium<CM>(v, rho, ux, uy);
+    force_xy_next(L, t0 + 1, rho, Fx, Fy);
+    collide<CM>(f, rho, ux, uy, Fx + 0.0, Fy + 0.0, L.omega, L.cs, fs);
+    InitRow<S>& r = rows[k];
 #pragma unroll
-        for (int v = 0; v < 9; v++) {
-            s_out[w][v] = S::save(fs[v], v);
-            s_f[w][v] = f[v];
-        }
-        s_u[w][0] = ux;
-        s_u[w][1] = uy;
+    for (int v = 0; v < 9; v++) {
+        r.out[v] = S::save(fs[v], v);
+        r.f[v] = f[v];
     }
-    __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    r.u[0] = ux;
+    r.u[1] = uy;
+}
+
+template <class S>
+__global__ void k_init_fill(typename S::T* __restrict__ B, const InitRow<S>* __restrict__ rows, LatDev L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     if (i >= L.Nx) return;
     const int type = site_type(L, i, j);
-    const int w = type == LIFE_WALL ? 1 : 0;
-    outlet_outputs(L, i, j, s_f[w], s_u[w][0], s_u[w][1]);
-    store_history(L, type, i, j, 1.0, s_u[w][0], s_u[w][1]);
+    const InitRow<S>& r = rows[2 * j + (type == LIFE_WALL ? 1 : 0)];
+    outlet_outputs(L, i, j, r.f, r.u[0], r.u[1]);
+    store_history(L, type, i, j, 1.0, r.u[0], r.u[1]);
     const size_t s = (size_t)j * L.pitch + i;
 #pragma unroll
-    for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = s_out[w][v];
+    for (int v = 0; v < 9; v++) B[(size_t)v * L.S + s] = r.out[v];
 }
 
 // One time step, interior sites, FP64: S_t from P_t (A), then P_{t+1} into B.
@@ -209,35 +217,109 @@ __global__ void k_state(typename S::T* __restrict__ B, LatDev L, int t, const do
     store_collided<CM, S>(B, L, t + 1, i, j, f, rho, ux, uy, fibm_in[id * 2], fibm_in[id * 2 + 1]);
 }
 
+// In the reduced-precision forms a fluid site without an IBM force gets its
+// velocity exactly as the step kernels form it, in FP32 (finish_site_lowp:
+// deviations, 1/rho correctly rounded, momentum with the half force), and
+// its density as 1 + the FP32 deviation sum in FP64; the FP64 path
+// (site_state) would spend ~50 FP64 operations per site on the narrow FP64
+// pipe. Boundary and IBM-corrected sites, populations requested, and the
+// per-site force take the FP64 path, as their kernels do.
+template <class S>
+__device__ __forceinline__ bool export_fluid_lowp(const typename S::T* __restrict__ P, const LatDev& L, int t, int i,
+                                                  int j, bool allowed, double& rho, double& ux, double& uy) {
+    if constexpr (std::is_same<S, StoreF64>::value) {
+        return false;
+    } else {
+        if (!allowed || L.site_force || site_type(L, i, j) != LIFE_FLUID) return false;
+        if (L.force_ibm) {
+            const size_t s = (size_t)j * L.pitch + i;
+            if (L.force_ibm[s] != 0.0 || L.force_ibm[L.S + s] != 0.0) return false;
+        }
+        float g[9];
+#pragma unroll
+        for (int v = 0; v < 9; v++) {
+            int si = i - cx_of(v), sj = j - cy_of(v);
+            si = si < 0 ? si + L.Nx : (si >= L.Nx ? si - L.Nx : si);
+            sj = sj < 0 ? sj + L.Ny : (sj >= L.Ny ? sj - L.Ny : sj);
+            g[v] = S::dev(P[(size_t)v * L.S + (size_t)sj * L.pitch + si], v);
+        }
+        float Fxd = 0.0f, Fyd = 0.0f;
+        if (L.womersley || L.Fx0_f != 0.0f || L.Fy0_f != 0.0f) force_xy_at_f(L, t, Fxd, Fyd);
+        const float dr = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7])) + g[8];
+        const float rf = 1.0f + dr;
+        const float mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
+        const float my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
+        const float inv = __frcp_rn(rf);
+        const bool forced = L.womersley || L.Fx0_f != 0.0f || L.Fy0_f != 0.0f;
+        const float px = forced ? fmaf(0.5f, Fxd, mx) : mx, py = forced ? fmaf(0.5f, Fyd, my) : my;
+        rho = 1.0 + (double)dr;
+        ux = (double)(px * inv);
+        uy = (double)(py * inv);
+        return true;
+    }
+}
+
 // Reference-layout export of the state after step t (what
-// GridClass::writeRestart dumps, src/Grid.cpp:1191-1222).
+// GridClass::writeRestart dumps, src/Grid.cpp:1191-1222). The reference
+// layout is column-major in the device's terms (id = i*Ny + j), so a block
+// computes a 32 x 32 tile of sites with i fastest (the pulls read whole rows
+// of each population plane) and writes rho, u and force_ibm through shared
+// memory with j fastest (whole runs of the output); f, exported for restart
+// sets and parity checks, is written per site.
 template <bool CM, class S>
-__global__ void k_export(const typename S::T* __restrict__ P, LatDev L, int t, double* __restrict__ rho_out,
-                             double* __restrict__ u_out, double* __restrict__ f_out, double* __restrict__ fibm_out,
-                             int i0, int i1) {
+__global__ void __launch_bounds__(256) k_export(const typename S::T* __restrict__ P, LatDev L, int t,
+                                                double* __restrict__ rho_out, double* __restrict__ u_out,
+                                                double* __restrict__ f_out, double* __restrict__ fibm_out, int i0,
+                                                int i1) {
     // columns i0 <= i < i1 (their reference-layout rows id = i*Ny + j are
     // one contiguous range of the output)
-    const int i = i0 + blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-    if (i >= i1) return;
-    double f[9], rho, ux, uy;
-    site_state<CM, S>(P, L, t, i, j, f, rho, ux, uy);
-    double Ix = 0.0, Iy = 0.0;
-    if (L.force_ibm) {
-        const size_t s = (size_t)j * L.pitch + i;
-        Ix = L.force_ibm[s];
-        Iy = L.force_ibm[L.S + s];
-        if (Ix != 0.0 || Iy != 0.0) {
-            double Fx, Fy;
-            force_xy_of(L, t, i, j, Fx, Fy);
-            macroscopic_ibm(f, Fx, Fy, Ix, Iy, rho, ux, uy);
+    __shared__ double s_rho[32][33];
+    __shared__ double2 s_u[32][33], s_fi[32][33];
+    const int ib = i0 + blockIdx.x * 32, jb = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i = ib + tx;
+#pragma unroll 1
+    for (int q = ty; q < 32; q += 8) {
+        const int j = jb + q;
+        if (i >= i1 || j >= L.Ny) continue;
+        double f[9], rho, ux, uy;
+        double Ix = 0.0, Iy = 0.0;
+        if (export_fluid_lowp<S>(P, L, t, i, j, f_out == nullptr, rho, ux, uy)) {
+            s_rho[tx][q] = rho;
+            s_u[tx][q] = make_double2(ux, uy);
+            s_fi[tx][q] = make_double2(0.0, 0.0);
+            continue;
+        }
+        site_state<CM, S>(P, L, t, i, j, f, rho, ux, uy);
+        if (L.force_ibm) {
+            const size_t s = (size_t)j * L.pitch + i;
+            Ix = L.force_ibm[s];
+            Iy = L.force_ibm[L.S + s];
+            if (Ix != 0.0 || Iy != 0.0) {
+                double Fx, Fy;
+                force_xy_of(L, t, i, j, Fx, Fy);
+                macroscopic_ibm(f, Fx, Fy, Ix, Iy, rho, ux, uy);
+            }
+        }
+        s_rho[tx][q] = rho;
+        s_u[tx][q] = make_double2(ux, uy);
+        s_fi[tx][q] = make_double2(Ix, Iy);
+        if (f_out) {
+            const size_t id = (size_t)i * L.Ny + j;
+            for (int v = 0; v < 9; v++) f_out[id * 9 + v] = f[v];
         }
     }
-    const size_t id = (size_t)i * L.Ny + j;
-    if (rho_out) rho_out[id] = rho;
-    if (u_out) { u_out[id * 2] = ux; u_out[id * 2 + 1] = uy; }
-    if (f_out)
-        for (int v = 0; v < 9; v++) f_out[id * 9 + v] = f[v];
-    if (fibm_out) { fibm_out[id * 2] = Ix; fibm_out[id * 2 + 1] = Iy; }
+    __syncthreads();
+    // transposed: thread tx now walks j
+#pragma unroll 1
+    for (int r = ty; r < 32; r += 8) {
+        const int io = ib + r, jo = jb + tx;
+        if (io >= i1 || jo >= L.Ny) continue;
+        const size_t id = (size_t)io * L.Ny + jo;
+        if (rho_out) rho_out[id] = s_rho[r][tx];
+        if (u_out) reinterpret_cast<double2*>(u_out)[id] = s_u[r][tx];
+        if (fibm_out) reinterpret_cast<double2*>(fibm_out)[id] = s_fi[r][tx];
+    }
 }
 
 // The arrays GridClass::writeVTK writes (src/Grid.cpp:860-893), in VTK point
@@ -351,9 +433,20 @@ static inline dim3 grid_of(const LatDev& L) { return dim3((L.Nx + 127) / 128, L.
         }                                                                                               \
     } while (0)
 
-cudaError_t launch_init(void* B, const LatDev& L, int t0, cudaStream_t s) {
-    LIFE_DISPATCH(k_init, , B, L, t0);
+template <bool CM, class S>
+static cudaError_t init_t(void* B, void* scratch, const LatDev& L, int t0, cudaStream_t s) {
+    InitRow<S>* rows = reinterpret_cast<InitRow<S>*>(scratch);
+    k_init_rows<CM, S><<<(2 * L.Ny + 127) / 128, 128, 0, s>>>(rows, L, t0);
+    k_init_fill<S><<<grid_of(L), 128, 0, s>>>((typename S::T*)B, rows, L);
     return cudaGetLastError();
+}
+
+// scratch: device memory for 2 Ny InitRow records (the second population
+// buffer, unused before the first step).
+cudaError_t launch_init(void* B, void* scratch, const LatDev& L, int t0, cudaStream_t s) {
+    if (L.prec == LIFE_PREC_F64) return L.cm ? init_t<true, StoreF64>(B, scratch, L, t0, s) : init_t<false, StoreF64>(B, scratch, L, t0, s);
+    if (L.prec == LIFE_PREC_F32) return L.cm ? init_t<true, StoreF32>(B, scratch, L, t0, s) : init_t<false, StoreF32>(B, scratch, L, t0, s);
+    return L.cm ? init_t<true, StoreF16>(B, scratch, L, t0, s) : init_t<false, StoreF16>(B, scratch, L, t0, s);
 }
 
 cudaError_t launch_interior_f64(const double* A, double* B, const LatDev& L, int t, cudaStream_t s) {
@@ -407,16 +500,16 @@ cudaError_t launch_export(const void* P, const LatDev& L, int t, bool initial, d
         return cudaGetLastError();
     }
     if (i1 <= i0) return cudaSuccess;
-    const dim3 g((i1 - i0 + 127) / 128, L.Ny);
+    const dim3 g((i1 - i0 + 31) / 32, (L.Ny + 31) / 32), blk(32, 8);
     if (L.prec == LIFE_PREC_F64) {
-        if (L.cm) k_export<true, StoreF64><<<g, 128, 0, s>>>((const double*)P, L, t, rho, u, f, fibm, i0, i1);
-        else k_export<false, StoreF64><<<g, 128, 0, s>>>((const double*)P, L, t, rho, u, f, fibm, i0, i1);
+        if (L.cm) k_export<true, StoreF64><<<g, blk, 0, s>>>((const double*)P, L, t, rho, u, f, fibm, i0, i1);
+        else k_export<false, StoreF64><<<g, blk, 0, s>>>((const double*)P, L, t, rho, u, f, fibm, i0, i1);
     } else if (L.prec == LIFE_PREC_F32) {
-        if (L.cm) k_export<true, StoreF32><<<g, 128, 0, s>>>((const float*)P, L, t, rho, u, f, fibm, i0, i1);
-        else k_export<false, StoreF32><<<g, 128, 0, s>>>((const float*)P, L, t, rho, u, f, fibm, i0, i1);
+        if (L.cm) k_export<true, StoreF32><<<g, blk, 0, s>>>((const float*)P, L, t, rho, u, f, fibm, i0, i1);
+        else k_export<false, StoreF32><<<g, blk, 0, s>>>((const float*)P, L, t, rho, u, f, fibm, i0, i1);
     } else {
-        if (L.cm) k_export<true, StoreF16><<<g, 128, 0, s>>>((const __half*)P, L, t, rho, u, f, fibm, i0, i1);
-        else k_export<false, StoreF16><<<g, 128, 0, s>>>((const __half*)P, L, t, rho, u, f, fibm, i0, i1);
+        if (L.cm) k_export<true, StoreF16><<<g, blk, 0, s>>>((const __half*)P, L, t, rho, u, f, fibm, i0, i1);
+        else k_export<false, StoreF16><<<g, blk, 0, s>>>((const __half*)P, L, t, rho, u, f, fibm, i0, i1);
     }
     return cudaGetLastError();
 }

@@ -8,7 +8,7 @@ namespace life {
 
 // All launchers take the population buffers as untyped pointers; their
 // element type follows L.prec (double / float / __half).
-cudaError_t launch_init(void* B, const LatDev& L, int t0, cudaStream_t s);
+cudaError_t launch_init(void* B, void* scratch, const LatDev& L, int t0, cudaStream_t s);
 cudaError_t launch_interior_f64(const double* A, double* B, const LatDev& L, int t, cudaStream_t s);
 cudaError_t launch_interior_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s);
 cudaError_t launch_perimeter(const void* A, void* B, const LatDev& L, int t, cudaStream_t s);

@@ -413,7 +413,7 @@ extern "C" int life_case_create(const LifeCaseParams* params, const LifeBodyDesc
         return rc;
     }
     LatDev L = lattice_view(c, 0);
-    e = launch_init(c->P[0], L, 0, c->stream);
+    e = launch_init(c->P[0], c->P[1], L, 0, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) {
         free_case(c);
@@ -456,9 +456,15 @@ struct StepTiming {
     int launches = 0;
 };
 
+// Runs shorter than this, before any step graph exists, launch their kernels
+// directly: capturing and instantiating the two step graphs costs about as
+// much host time as a few large steps, and the same kernels run either way.
+constexpr int kDirectMaxSteps = 64;
+
 static int run_steps(LifeCase* c, int nsteps, StepTiming* tm) {
     int rc;
-    if (!c->host_steps) {
+    const bool direct = !c->host_steps && !tm && nsteps < kDirectMaxSteps && !case_graphs_ready(c);
+    if (!c->host_steps && !direct) {
         // the case's captured step graphs; the same kernels in the same order
         if ((rc = case_graph_steps(c, nsteps, tm ? tm->start : nullptr, tm ? tm->stop : nullptr))) return rc;
         if (tm) tm->launches = case_kernels_per_step(c) * nsteps;
@@ -490,21 +496,28 @@ static int run_steps(LifeCase* c, int nsteps, StepTiming* tm) {
             if (e != cudaSuccess) return cuda_fail(e, "outlet");
             if (tm) tm->launches++;
         }
-        // The boundary-condition perimeter runs on a side stream, overlapped
-        // with the interior kernel: both read only A and write disjoint sites
-        // of B. The main stream waits for it before anything reads B.
-        cudaEventRecord(c->ev_fork, c->stream);
-        cudaStreamWaitEvent(c->side, c->ev_fork, 0);
-        e = launch_perimeter(A, B, L, tt, c->side);
-        if (e != cudaSuccess) return cuda_fail(e, "perimeter step");
-        cudaEventRecord(c->ev_join, c->side);
-        if (tm) cudaEventRecord(tm->ev[2 * k], c->stream);
-        e = L.prec == LIFE_PREC_F64 ? launch_interior_f64((const double*)A, (double*)B, L, tt, c->stream)
-                                    : launch_interior_lowp(A, B, L, tt, c->stream);
-        if (e != cudaSuccess) return cuda_fail(e, "interior step");
-        if (tm) cudaEventRecord(tm->ev[2 * k + 1], c->stream);
-        cudaStreamWaitEvent(c->stream, c->ev_join, 0);
-        if (tm) tm->launches += 2;
+        if (direct && case_fused_step(c)) {
+            // the one-launch step kernel of the step graphs
+            e = launch_step_lowp(A, B, L, tt, c->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "step");
+        } else {
+            // The boundary-condition perimeter runs on a side stream,
+            // overlapped with the interior kernel: both read only A and write
+            // disjoint sites of B. The main stream waits for it before
+            // anything reads B.
+            cudaEventRecord(c->ev_fork, c->stream);
+            cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+            e = launch_perimeter(A, B, L, tt, c->side);
+            if (e != cudaSuccess) return cuda_fail(e, "perimeter step");
+            cudaEventRecord(c->ev_join, c->side);
+            if (tm) cudaEventRecord(tm->ev[2 * k], c->stream);
+            e = L.prec == LIFE_PREC_F64 ? launch_interior_f64((const double*)A, (double*)B, L, tt, c->stream)
+                                        : launch_interior_lowp(A, B, L, tt, c->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "interior step");
+            if (tm) cudaEventRecord(tm->ev[2 * k + 1], c->stream);
+            cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+            if (tm) tm->launches += 2;
+        }
         if (c->obj.hasIBM) {
             int before = c->ibm_launches;
             if ((rc = ibm_step(c, tt, A, B))) return rc;

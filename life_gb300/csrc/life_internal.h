@@ -120,6 +120,11 @@ void batch_free(LifeBatch* b);
 // nsteps steps of one case through its cached step graphs (asynchronous);
 // with start/stop, CUDA events recorded around them on the case's stream.
 int case_graph_steps(LifeCase* c, int nsteps, cudaEvent_t start, cudaEvent_t stop);
+// Whether the case's step graphs exist (captured by an earlier run).
+bool case_graphs_ready(const LifeCase* c);
+// Whether a step of the case is one launch of the reduced-precision step
+// kernel (which also takes the boundary sites).
+bool case_fused_step(const LifeCase* c);
 // Mean device time of the case's interior kernel alone over reps launches.
 int case_interior_ms(LifeCase* c, int reps, float* ms);
 // Kernel nodes of one captured step of the case (0 before the first capture).

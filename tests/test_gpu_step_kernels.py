@@ -57,3 +57,40 @@ def test_step_kernels_bit_identical(kind, prec):
     host = digest(kind, prec, {"LIFE_CASE_HOSTLOOP": "1"})
     assert one == host, "one-site step kernel vs host-driven kernels"
     assert tma == one, "TMA-staged step kernel vs one-site step kernel"
+
+
+DIRECT = r"""
+import hashlib, sys
+sys.path.insert(0, '.'); sys.path.insert(0, 'tests/golden')
+from cases import golden_cases
+from life_gb300.case import CaseParams, VELOCITY, WALL
+from life_gb300.lib import Case
+name, split = sys.argv[1], [int(x) for x in sys.argv[2:]]
+if name == 'cavity':
+    omega = 1.0 / 0.56
+    p = CaseParams(Nx=2049, Ny=2048, height_p=2047.0, rho_p=1.0, nu_p=(1.0 / omega - 0.5) / 3.0, omega=omega,
+                   wall_left=WALL, wall_right=WALL, wall_bottom=WALL, wall_top=VELOCITY, uxInlet_p=0.1, precision=1)
+    b = []
+else:
+    p, b = golden_cases()[name]
+with Case(p, b) as c:
+    for n in split:
+        c.step(n)
+    fl = c.fields(("rho", "u"))
+print("DIGEST", hashlib.sha256(fl["rho"].tobytes() + fl["u"].tobytes()).hexdigest())
+"""
+
+
+@pytest.mark.parametrize("name", ["cavity", "cylinder_rigid_cm", "filament_flex_deflect", "womersley_gravity_cm"])
+def test_direct_and_graph_steps_identical(name):
+    """Runs shorter than 64 steps launch kernels directly until step graphs
+    exist; 100 steps as one call (graphs), as 30 + 70 (direct, then graphs)
+    and as 30 + 30 + 40 (direct throughout) end in the same bits."""
+    from life_gb300.build import build
+    build()
+    out = []
+    for split in (["100"], ["30", "70"], ["30", "30", "40"]):
+        res = subprocess.run([sys.executable, "-c", DIRECT, name] + split, cwd=ROOT, capture_output=True, text=True)
+        assert res.returncode == 0, res.stderr[-2000:]
+        out.append([ln for ln in res.stdout.splitlines() if ln.startswith("DIGEST")][-1])
+    assert out[0] == out[1] == out[2]
