@@ -157,11 +157,16 @@ static bool fused_step(const LifeBatch* b) {
     return b->cases.size() == 1 && case_fused_step(b->cases[0]);
 }
 
-static cudaError_t launch_batch_interior(LifeBatch* b, int phase, cudaStream_t s) {
+// The interior launch of one batch step. `h`/`d`: the host and device copies
+// of the case table (the batch's own, or the scratch table of time_interior).
+static cudaError_t launch_batch_interior(LifeBatch* b, int phase, cudaStream_t s, const BatchLatCase* h = nullptr,
+                                         const BatchLatCase* d = nullptr) {
+    if (!h) h = b->h_cases.data();
+    if (!d) d = b->d_cases;
     if (b->cases.size() == 1) {
         // one case: its own interior kernel (one CTA row segment per block);
         // in the reduced-precision forms the launch also takes the perimeter
-        const BatchLatCase& C = b->h_cases[0];
+        const BatchLatCase& C = h[0];
         const LatDev& L = C.L[phase];
         const int t = b->cases[0]->t + 1 + phase;  // ignored: kernels read *L.t_dev + L.t_off
         if (b->prec == LIFE_PREC_F64) return launch_interior_f64((const double*)C.A[phase], (double*)C.B[phase], L, t, s);
@@ -169,10 +174,8 @@ static cudaError_t launch_batch_interior(LifeBatch* b, int phase, cudaStream_t s
         return launch_interior_lowp(C.A[phase], C.B[phase], L, t, s);
     }
     if (b->prec == LIFE_PREC_F64)
-        return launch_interior_batch_f64(b->d_cases, b->d_tile_case, b->ntiles, b->tile_w, b->tile_h, b->grid, phase,
-                                         s);
-    return launch_interior_batch_lowp(b->prec, b->d_cases, b->d_tile_case, b->ntiles, b->tile_w, b->tile_h, b->grid,
-                                      phase, s);
+        return launch_interior_batch_f64(d, b->d_tile_case, b->ntiles, b->tile_w, b->tile_h, b->grid, phase, s);
+    return launch_interior_batch_lowp(b->prec, d, b->d_tile_case, b->ntiles, b->tile_w, b->tile_h, b->grid, phase, s);
 }
 
 // Before a step from state t the step tables must hold t+1 and t+2; when they
@@ -562,30 +565,48 @@ extern "C" int life_batch_set_tile(LifeBatch* b, int32_t tile_w, int32_t tile_h)
 }
 
 // Times the batched interior kernel alone (phase 0, `reps` launches after two
-// warm-up launches). It rewrites the next-step buffers, which the next step
-// writes again in full; the outlet columns it also writes are saved first and
-// put back.
+// warm-up launches) without touching any case's state: a copy of the case
+// table sends every output of the launch (the populations, the outlet
+// columns, the per-site densities and corner velocities) to scratch memory,
+// so a later export or step sees exactly the state the last step left.
 static int time_interior(LifeBatch* b, int reps, float* ms) {
-    std::vector<double*> saved;
-    for (LifeCase* c : b->cases) {
-        double* s = nullptr;
-        if (c->d_outlet_u) {
-            CK(cudaMalloc(&s, sizeof(double) * 6 * c->Ny));
-            CK(cudaMemcpyAsync(s, c->d_outlet_u, sizeof(double) * 6 * c->Ny, cudaMemcpyDeviceToDevice, b->stream));
-        }
-        saved.push_back(s);
+    const int n = (int)b->cases.size();
+    std::vector<BatchLatCase> h = b->h_cases;
+    size_t total = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = total;
+        total += (bytes + 255) / 256 * 256;
+        return at;
+    };
+    std::vector<size_t> oP(n), oU(n), oF(n), oC(n), oR(n);
+    for (int k = 0; k < n; k++) {
+        const LifeCase* c = b->cases[k];
+        oP[k] = take((size_t)9 * c->S * c->elem);
+        oU[k] = take(sizeof(double) * 6 * c->Ny);
+        oF[k] = take(sizeof(double) * 3 * c->Ny);
+        oC[k] = take(sizeof(double) * 8);
+        oR[k] = c->site_force ? take(sizeof(double) * c->S) : 0;
     }
-    for (int r = 0; r < 2; r++) CK(launch_batch_interior(b, 0, b->stream));
-    CK(cudaEventRecord(b->t0, b->stream));
-    for (int r = 0; r < reps; r++) CK(launch_batch_interior(b, 0, b->stream));
-    CK(cudaEventRecord(b->t1, b->stream));
-    for (size_t k = 0; k < b->cases.size(); k++)
-        if (saved[k])
-            CK(cudaMemcpyAsync(b->cases[k]->d_outlet_u, saved[k], sizeof(double) * 6 * b->cases[k]->Ny,
-                               cudaMemcpyDeviceToDevice, b->stream));
-    CK(cudaStreamSynchronize(b->stream));
-    for (double* s : saved)
-        if (s) cudaFree(s);
+    const size_t table = take(sizeof(BatchLatCase) * n);
+    char* scratch = nullptr;
+    CK(cudaMalloc(&scratch, total));
+    for (int k = 0; k < n; k++)
+        for (int p = 0; p < 2; p++) {
+            h[k].B[p] = scratch + oP[k];
+            h[k].L[p].outlet_u = reinterpret_cast<double*>(scratch + oU[k]);
+            h[k].L[p].outlet_f_next = reinterpret_cast<double*>(scratch + oF[k]);
+            h[k].L[p].corner_next = reinterpret_cast<double*>(scratch + oC[k]);
+            if (b->cases[k]->site_force) h[k].L[p].rho_next = reinterpret_cast<double*>(scratch + oR[k]);
+        }
+    BatchLatCase* d = reinterpret_cast<BatchLatCase*>(scratch + table);
+    cudaError_t e = cudaMemcpyAsync(d, h.data(), sizeof(BatchLatCase) * n, cudaMemcpyHostToDevice, b->stream);
+    for (int r = 0; r < 2 && e == cudaSuccess; r++) e = launch_batch_interior(b, 0, b->stream, h.data(), d);
+    if (e == cudaSuccess) e = cudaEventRecord(b->t0, b->stream);
+    for (int r = 0; r < reps && e == cudaSuccess; r++) e = launch_batch_interior(b, 0, b->stream, h.data(), d);
+    if (e == cudaSuccess) e = cudaEventRecord(b->t1, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    cudaFree(scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "interior timing");
     float t = 0.f;
     CK(cudaEventElapsedTime(&t, b->t0, b->t1));
     *ms = t / reps;

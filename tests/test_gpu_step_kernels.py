@@ -94,3 +94,43 @@ def test_direct_and_graph_steps_identical(name):
         assert res.returncode == 0, res.stderr[-2000:]
         out.append([ln for ln in res.stdout.splitlines() if ln.startswith("DIGEST")][-1])
     assert out[0] == out[1] == out[2]
+
+
+TIMED = r"""
+import hashlib, sys
+sys.path.insert(0, '.'); sys.path.insert(0, 'tests/golden')
+from cases import golden_cases
+from life_gb300.case import CaseParams, VELOCITY, WALL
+from life_gb300.lib import Case
+name, first, timed = sys.argv[1], int(sys.argv[2]), int(sys.argv[3])
+if name == 'cavity':
+    omega = 1.0 / 0.56
+    p = CaseParams(Nx=2049, Ny=2048, height_p=2047.0, rho_p=1.0, nu_p=(1.0 / omega - 0.5) / 3.0, omega=omega,
+                   wall_left=WALL, wall_right=WALL, wall_bottom=WALL, wall_top=VELOCITY, uxInlet_p=0.1, precision=1)
+    b = []
+else:
+    p, b = golden_cases()[name]
+with Case(p, b) as c:
+    c.step(first)
+    if timed:
+        c.bench_steps(timed)
+    fl = c.fields(("rho", "u", "f"))
+print("DIGEST", hashlib.sha256(fl["rho"].tobytes() + fl["u"].tobytes() + fl["f"].tobytes()).hexdigest())
+"""
+
+
+@pytest.mark.parametrize("name", ["cavity", "cylinder_rigid_cm", "channel_convective_freeslip_cm"])
+@pytest.mark.parametrize("first", [5, 6])
+def test_interior_timing_leaves_the_state_untouched(name, first):
+    """life_case_bench_steps times the interior launch alone after its steps;
+    those extra launches write to scratch memory only, so the fields after
+    first + 20 timed steps equal those of first + 20 plain steps, for either
+    parity of the step graphs."""
+    from life_gb300.build import build
+    build()
+    out = []
+    for args in ([str(first), "20"], [str(first + 20), "0"]):
+        res = subprocess.run([sys.executable, "-c", TIMED, name] + args, cwd=ROOT, capture_output=True, text=True)
+        assert res.returncode == 0, res.stderr[-2000:]
+        out.append([ln for ln in res.stdout.splitlines() if ln.startswith("DIGEST")][-1])
+    assert out[0] == out[1]
