@@ -1,0 +1,33 @@
+// Correctly rounded FP64 division through a reciprocal, shared by the lattice
+// kernels (the velocity of every site) and the FEM band solve.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace life {
+
+// a / b correctly rounded (round to nearest), given y = RN(1/b): Markstein's
+// method (P. Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al.,
+// Handbook of Floating-Point Arithmetic, "Markstein's theorem"): q0 = RN(a y)
+// is within 1.5 ulp of a/b, one correction q1 = RN(q0 + RN(a - b q0) y)
+// brings it within one ulp, and then the residual a - b q1 is exact and
+// RN(q1 + (a - b q1) y) = RN(a/b). The theorem needs the intermediates in the
+// normal range, so operands outside a safe exponent window (tested on the
+// bits, with integer operations) take the hardware division.
+// life_selftest_division checks this function against a / b.
+__device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
+    const unsigned long long ba = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long bb = (unsigned long long)__double_as_longlong(b);
+    const int ea = (int)(ba >> 52) & 0x7ff, eb = (int)(bb >> 52) & 0x7ff;
+    const bool b_ok = eb > 200 && eb < 1800;
+    // a zero numerator: the signed zero a / b is a * y (y has the sign of b)
+    if ((ba << 1) == 0ull && b_ok) return a * y;
+    const bool a_ok = ea > 200 && ea < 1800;
+    if (!(a_ok && b_ok && ea - eb > -700 && ea - eb < 700)) return a / b;
+    const double q0 = a * y;
+    const double r0 = fma(-b, q0, a);
+    const double q1 = fma(r0, y, q0);
+    const double r1 = fma(-b, q1, a);
+    return fma(r1, y, q1);
+}
+
+}  // namespace life

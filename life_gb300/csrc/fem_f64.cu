@@ -24,6 +24,7 @@
 
 #include "band_lu.h"
 #include "crtrig.h"
+#include "div_rn.cuh"
 #include "fem_kernels.h"
 
 namespace life {
@@ -470,27 +471,6 @@ __device__ void band_factor_smem(double* Bd, int nn, int kl, int ku, int W, int*
     }
 }
 
-// a / b correctly rounded (round to nearest), given y = RN(1/b): Markstein's
-// method (P. Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al.,
-// Handbook of Floating-Point Arithmetic, "Markstein's theorem"): q0 = RN(a y)
-// is within 1.5 ulp of a/b, one correction q1 = RN(q0 + RN(a - b q0) y)
-// brings it within one ulp, and then the residual a - b q1 is exact and
-// RN(q1 + (a - b q1) y) = RN(a/b). The theorem needs the intermediates in the
-// normal range, so operands outside a safe exponent window take the hardware
-// division. life_selftest_division checks this function against a / b.
-__device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
-    const int ea = (int)((unsigned long long)__double_as_longlong(a) >> 52) & 0x7ff;
-    const int eb = (int)((unsigned long long)__double_as_longlong(b) >> 52) & 0x7ff;
-    const bool a_ok = (a == 0.0) || (ea > 200 && ea < 1800);
-    const bool b_ok = eb > 200 && eb < 1800;
-    if (!(a_ok && b_ok && (a == 0.0 || (ea - eb > -700 && ea - eb < 700)))) return a / b;
-    const double q0 = a * y;
-    const double r0 = fma(-b, q0, a);
-    const double q1 = fma(r0, y, q0);
-    const double r1 = fma(-b, q1, a);
-    return fma(r1, y, q1);
-}
-
 __global__ void k_selftest_division(long long n, unsigned long long seed, unsigned long long* bad) {
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
         // splitmix64 streams for the two operands; exponents over a wide range
@@ -508,7 +488,10 @@ __global__ void k_selftest_division(long long n, unsigned long long seed, unsign
         const long long xb = (long long)(1023 + (long long)((w >> 24) % span) - span / 2);
         const unsigned long long ba = (u & 0x800fffffffffffffull) | ((unsigned long long)(xa < 1 ? 1 : (xa > 2046 ? 2046 : xa)) << 52);
         const unsigned long long bb = (v & 0x800fffffffffffffull) | ((unsigned long long)(xb < 1 ? 1 : (xb > 2046 ? 2046 : xb)) << 52);
-        const double a = __longlong_as_double((long long)ba), b = __longlong_as_double((long long)bb);
+        // one numerator in 64 is a signed zero (the velocity of a site at rest)
+        const double a = ((w >> 40) & 63) == 0 ? __longlong_as_double((long long)(u & 0x8000000000000000ull))
+                                                : __longlong_as_double((long long)ba);
+        const double b = __longlong_as_double((long long)bb);
         const double ref = a / b;
         const double got = div_rn_recip(a, b, __drcp_rn(b));
         if (__double_as_longlong(ref) != __double_as_longlong(got) && !(ref != ref && got != got)) atomicAdd(bad, 1ull);

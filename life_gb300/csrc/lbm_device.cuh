@@ -17,6 +17,7 @@
 // reference's operation order, so a + b*c is rounded twice as g++ does on x86.
 #pragma once
 #include <cuda_fp16.h>
+#include "div_rn.cuh"
 
 #include <cstdint>
 
@@ -151,8 +152,10 @@ __device__ __forceinline__ void macroscopic(const double f[9], double Fx, double
         my = add_c(my, cy_of(v), f[v]);
     }
     rho = r;
-    ux = (mx + 0.5 * Fx) / r;
-    uy = (my + 0.5 * Fy) / r;
+    // (m + F/2) / rho, both quotients through one correctly rounded reciprocal
+    const double y = __drcp_rn(r);
+    ux = div_rn_recip(mx + 0.5 * Fx, r, y);
+    uy = div_rn_recip(my + 0.5 * Fy, r, y);
 }
 
 // macroscopic() for a zero force: m + 0.5 * (+-0) is m itself, since the
@@ -167,8 +170,9 @@ __device__ __forceinline__ void macroscopic_unforced(const double f[9], double& 
         my = add_c(my, cy_of(v), f[v]);
     }
     rho = r;
-    ux = mx / r;
-    uy = my / r;
+    const double y = __drcp_rn(r);
+    ux = div_rn_recip(mx, r, y);
+    uy = div_rn_recip(my, r, y);
 }
 
 // IBMNodeClass::updateMacroscopic form (src/IBMNode.cpp:113-122): the IBM
@@ -183,8 +187,9 @@ __device__ __forceinline__ void macroscopic_ibm(const double f[9], double Fx, do
         my = add_c(my, cy_of(v), f[v]);
     }
     rho = r;
-    ux = (mx + 0.5 * (Fx + Ix)) / r;
-    uy = (my + 0.5 * (Fy + Iy)) / r;
+    const double y = __drcp_rn(r);
+    ux = div_rn_recip(mx + 0.5 * (Fx + Ix), r, y);
+    uy = div_rn_recip(my + 0.5 * (Fy + Iy), r, y);
 }
 
 // GridClass::equilibrium (src/Grid.cpp:249-264): 2nd-order Hermite (BGK) or
