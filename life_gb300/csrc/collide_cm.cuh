@@ -10,14 +10,19 @@ namespace life {
 template <bool UNF>
 __device__ __forceinline__ void collide_cm(const double f[9], double rho, double ux, double uy, double Fx, double Fy,
                            double omega, double cs, double fs[9]) {
-    double k4Pre = 0.0, k5Pre = 0.0;
+    // the two sums start at their first term rather than at +0 (see
+    // moment_sums: equal up to the sign of a zero, which pos_zero restores)
+    double k4Pre, k5Pre;
 #pragma unroll
     for (int v = 0; v < 9; v++) {
         double cx = cx_of(v) - ux;
         double cy = cy_of(v) - uy;
-        k4Pre += f[v] * (LSQ(cx) - LSQ(cy));
-        k5Pre += f[v] * cx * cy;
+        const double t4 = f[v] * (LSQ(cx) - LSQ(cy)), t5 = f[v] * cx * cy;
+        k4Pre = v == 0 ? t4 : k4Pre + t4;
+        k5Pre = v == 0 ? t5 : k5Pre + t5;
     }
+    k4Pre = pos_zero(k4Pre);
+    k5Pre = pos_zero(k5Pre);
     const double k0 = rho;
     const double k1 = 0.5 * Fx;
     const double k2 = 0.5 * Fy;

@@ -18,16 +18,19 @@ __device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
     const unsigned long long ba = (unsigned long long)__double_as_longlong(a);
     const unsigned long long bb = (unsigned long long)__double_as_longlong(b);
     const int ea = (int)(ba >> 52) & 0x7ff, eb = (int)(bb >> 52) & 0x7ff;
+    // a zero numerator runs the same steps (every intermediate is a zero) and
+    // then takes q0 = a * y, the signed zero a / b (y has the sign of b): the
+    // cost of a site does not depend on its velocity being zero
+    const bool a_zero = (ba << 1) == 0ull;
+    const bool a_ok = a_zero || (ea > 200 && ea < 1800 && ea - eb > -700 && ea - eb < 700);
     const bool b_ok = eb > 200 && eb < 1800;
-    // a zero numerator: the signed zero a / b is a * y (y has the sign of b)
-    if ((ba << 1) == 0ull && b_ok) return a * y;
-    const bool a_ok = ea > 200 && ea < 1800;
-    if (!(a_ok && b_ok && ea - eb > -700 && ea - eb < 700)) return a / b;
+    if (!(a_ok && b_ok)) return a / b;
     const double q0 = a * y;
     const double r0 = fma(-b, q0, a);
     const double q1 = fma(r0, y, q0);
     const double r1 = fma(-b, q1, a);
-    return fma(r1, y, q1);
+    const double q = fma(r1, y, q1);
+    return a_zero ? q0 : q;
 }
 
 }  // namespace life

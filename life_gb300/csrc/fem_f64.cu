@@ -1081,7 +1081,44 @@ __global__ void __launch_bounds__(256) k_fem_dynamic(FsiDev F, MarkerDev M) {
         }
     }
     __syncthreads();
-    update_fem_values(B);
+    // updateFEMValues at U = U_n: subiteration 0 evaluates it and keeps the
+    // node positions and element values (length, angle, cos, sin); the later
+    // subiterations restart from the same U_n and copy them back
+    {
+        double* cNode = reinterpret_cast<double*>(cMv + n) + (nn + 1) / 2;
+        double* cEl = cNode + 3 * (size_t)B.nNodes;
+        if (!reuse) {
+            update_fem_values(B);
+            for (int q = threadIdx.x; q < B.nNodes; q += blockDim.x) {
+                const double* nd = B.node + q * 6;
+                cNode[q * 3 + 0] = nd[2];
+                cNode[q * 3 + 1] = nd[3];
+                cNode[q * 3 + 2] = nd[5];
+            }
+            for (int e = threadIdx.x; e < B.nEl; e += blockDim.x) {
+                const double* el = B.el + (size_t)e * EL_STRIDE;
+                cEl[e * 4 + 0] = el[EL_ANG];
+                cEl[e * 4 + 1] = el[EL_L];
+                cEl[e * 4 + 2] = el[EL_COS];
+                cEl[e * 4 + 3] = el[EL_SIN];
+            }
+        } else {
+            for (int q = threadIdx.x; q < B.nNodes; q += blockDim.x) {
+                double* nd = B.node + q * 6;
+                nd[2] = cNode[q * 3 + 0];
+                nd[3] = cNode[q * 3 + 1];
+                nd[5] = cNode[q * 3 + 2];
+            }
+            for (int e = threadIdx.x; e < B.nEl; e += blockDim.x) {
+                double* el = B.el + (size_t)e * EL_STRIDE;
+                el[EL_ANG] = cEl[e * 4 + 0];
+                el[EL_L] = cEl[e * 4 + 1];
+                el[EL_COS] = cEl[e * 4 + 2];
+                el[EL_SIN] = cEl[e * 4 + 3];
+            }
+            __syncthreads();
+        }
+    }
     // constructRVector (src/FEMBody.cpp:226-234; FEMElementClass::loadVector,
     // src/FEMElement.cpp:27-69): contributions per force-map entry, then an
     // ordered assembly.

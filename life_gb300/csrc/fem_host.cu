@@ -147,7 +147,7 @@ int setup_fem(LifeCase* c) {
         }
         fStart[f.nEl] = (int)fNode.size();
         D.nfmap = (int)fNode.size();
-        if ((rc = upload(c, &D.pool, pool)) || (rc = fallocT(c, &D.lu_cache, fem_cache_doubles(n, D.bc))) ||
+        if ((rc = upload(c, &D.pool, pool)) || (rc = fallocT(c, &D.lu_cache, fem_cache_doubles(n, D.bc, D.nNodes, D.nEl))) ||
             (rc = upload(c, &D.node, node)) || (rc = upload(c, &D.el, el)) ||
             (rc = fallocT(c, &D.elscr, (size_t)f.nEl * ES_STRIDE)) || (rc = upload(c, &D.fmapStart, fStart)) ||
             (rc = upload(c, &D.fmapEl, fEl)) || (rc = upload(c, &D.fmapNode, fNode)) || (rc = upload(c, &D.fmapZ, fZ)) ||

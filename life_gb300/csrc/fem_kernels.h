@@ -23,9 +23,9 @@ enum { EL_L0, EL_L, EL_ANG, EL_A, EL_I, EL_E, EL_RHO, EL_COS, EL_SIN, EL_M = 9, 
 enum { ES_M = 0, ES_K = 36, ES_F = 72, ES_STRIDE = 78 };
 
 // Doubles of FemBodyDev::lu_cache for n DOFs of which bc are constrained.
-inline size_t fem_cache_doubles(int n, int bc) {
+inline size_t fem_cache_doubles(int n, int bc, int nNodes, int nEl) {
     const size_t nn = (size_t)(n - bc);
-    return nn * 16 + nn + 2 * (size_t)n + (nn + 1) / 2;
+    return nn * 16 + nn + 2 * (size_t)n + (nn + 1) / 2 + 3 * (size_t)nNodes + 4 * (size_t)nEl;
 }
 
 struct FemBodyDev {
@@ -35,7 +35,8 @@ struct FemBodyDev {
     double* pool;      // [NVEC][n]
     // First Newton iteration of the step, kept by subiteration 0 for the later
     // subiterations (fem_cache_doubles): LU band [nn][16], pivot reciprocals
-    // [nn], internal force [n], M * Newmark vector [n], pivots [nn] (ints)
+    // [nn], internal force [n], M * Newmark vector [n], pivots [nn] (ints),
+    // and the node positions [nNodes][3] and element values [nEl][4] at U_n
     double* lu_cache;
     double* node;      // [nNodes][6]: pos0x, pos0y, posx, posy, angle0, angle
     double* el;        // [nEl][EL_STRIDE]

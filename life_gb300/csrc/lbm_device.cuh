@@ -141,16 +141,47 @@ __device__ __forceinline__ double add_c(double acc, int c, double x) {
     return c == 0 ? acc : (c > 0 ? acc + x : acc - x);
 }
 
+// -0 -> +0 on the bits (integer operations, not the FP64 unit)
+__device__ __forceinline__ double pos_zero(double s) {
+    const long long b = __double_as_longlong(s);
+    return __longlong_as_double(b == (long long)0x8000000000000000ull ? 0ll : b);
+}
+
+// The reference's density and momentum sums (src/Grid.cpp:285-293) start at
+// +0. Here each starts at its first term instead (+-f, one FP64 add fewer
+// per sum). The two running sums then differ at most in the sign of a zero:
+// a round-to-nearest sum is -0 only when both of its terms are, so the
+// reference's sums are never -0, and where this sum holds -0 the
+// reference's holds +0, while any nonzero term makes them equal again.
+// pos_zero() on the result gives the reference's bits.
+__device__ __forceinline__ void moment_sums(const double f[9], double& r, double& mx, double& my) {
+    r = f[0];
+    mx = 0.0;
+    my = 0.0;
+    bool hx = false, hy = false;
+#pragma unroll
+    for (int v = 1; v < 9; v++) {
+        r = r + f[v];
+        const int cx = cx_of(v), cy = cy_of(v);
+        if (cx != 0) {
+            mx = hx ? add_c(mx, cx, f[v]) : (cx > 0 ? f[v] : -f[v]);
+            hx = true;
+        }
+        if (cy != 0) {
+            my = hy ? add_c(my, cy, f[v]) : (cy > 0 ? f[v] : -f[v]);
+            hy = true;
+        }
+    }
+    r = pos_zero(r);
+    mx = pos_zero(mx);
+    my = pos_zero(my);
+}
+
 // GridClass::macroscopic (src/Grid.cpp:282-299)
 __device__ __forceinline__ void macroscopic(const double f[9], double Fx, double Fy, double& rho,
                                             double& ux, double& uy) {
-    double r = 0.0, mx = 0.0, my = 0.0;
-#pragma unroll
-    for (int v = 0; v < 9; v++) {
-        r = r + f[v];
-        mx = add_c(mx, cx_of(v), f[v]);
-        my = add_c(my, cy_of(v), f[v]);
-    }
+    double r, mx, my;
+    moment_sums(f, r, mx, my);
     rho = r;
     // (m + F/2) / rho, both quotients through one correctly rounded reciprocal
     const double y = __drcp_rn(r);
@@ -162,13 +193,8 @@ __device__ __forceinline__ void macroscopic(const double f[9], double Fx, double
 // momentum sums start at +0 and a round-to-nearest sum is -0 only when both
 // of its terms are, so they are never -0.
 __device__ __forceinline__ void macroscopic_unforced(const double f[9], double& rho, double& ux, double& uy) {
-    double r = 0.0, mx = 0.0, my = 0.0;
-#pragma unroll
-    for (int v = 0; v < 9; v++) {
-        r = r + f[v];
-        mx = add_c(mx, cx_of(v), f[v]);
-        my = add_c(my, cy_of(v), f[v]);
-    }
+    double r, mx, my;
+    moment_sums(f, r, mx, my);
     rho = r;
     const double y = __drcp_rn(r);
     ux = div_rn_recip(mx, r, y);
@@ -179,13 +205,8 @@ __device__ __forceinline__ void macroscopic_unforced(const double f[9], double& 
 // force enters the velocity at support sites.
 __device__ __forceinline__ void macroscopic_ibm(const double f[9], double Fx, double Fy, double Ix,
                                                 double Iy, double& rho, double& ux, double& uy) {
-    double r = 0.0, mx = 0.0, my = 0.0;
-#pragma unroll
-    for (int v = 0; v < 9; v++) {
-        r = r + f[v];
-        mx = add_c(mx, cx_of(v), f[v]);
-        my = add_c(my, cy_of(v), f[v]);
-    }
+    double r, mx, my;
+    moment_sums(f, r, mx, my);
     rho = r;
     const double y = __drcp_rn(r);
     ux = div_rn_recip(mx + 0.5 * (Fx + Ix), r, y);
