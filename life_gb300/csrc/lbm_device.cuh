@@ -74,6 +74,11 @@ struct StoreF32 {
     __device__ static __forceinline__ T save(double f, int v) { return (float)(f - wgt(v)); }
     __device__ static __forceinline__ float dev(T x, int) { return x; }      // g_v
     __device__ static __forceinline__ T put(float g, int) { return g; }
+    // the stored value as a float and its deviation (here the same)
+    static constexpr bool SCALED = false;
+    __device__ static __forceinline__ float raw(T x) { return x; }
+    __device__ static __forceinline__ float scaled(float r, int) { return r; }
+    __device__ static __forceinline__ T put_raw(float r) { return r; }
 };
 struct StoreF16 {
     using T = __half;
@@ -86,6 +91,12 @@ struct StoreF16 {
     }
     __device__ static __forceinline__ float dev(T x, int v) { return __half2float(x) * h16_scale(v); }
     __device__ static __forceinline__ T put(float g, int v) { return __float2half_rn(g * h16_inv(v)); }
+    // the stored value as a float (the deviation divided by the direction's
+    // power-of-two scale) and its deviation
+    static constexpr bool SCALED = true;
+    __device__ static __forceinline__ float raw(T x) { return __half2float(x); }
+    __device__ static __forceinline__ float scaled(float r, int v) { return r * h16_scale(v); }
+    __device__ static __forceinline__ T put_raw(float r) { return __float2half_rn(r); }
 };
 
 // Site type from the wall configuration; y walls override x walls at the

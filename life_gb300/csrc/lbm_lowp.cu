@@ -77,8 +77,14 @@ __device__ __forceinline__ V2 operator+(V2 a, V2 b) {
     asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.b) : "l"(a.b), "l"(b.b));
     return r;
 }
+// negation flips the sign bits (two integer operations; the collision below
+// puts its signs into constants instead)
 __device__ __forceinline__ V2 operator-(V2 a) { return V2{a.b ^ 0x8000000080000000ull}; }
-__device__ __forceinline__ V2 operator-(V2 a, V2 b) { return a + (-b); }
+__device__ __forceinline__ V2 operator-(V2 a, V2 b) {
+    V2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.b) : "l"(a.b), "l"(b.b));
+    return r;
+}
 __device__ __forceinline__ V2 operator*(V2 a, V2 b) {
     V2 r;
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.b) : "l"(a.b), "l"(b.b));
@@ -142,26 +148,55 @@ __device__ __forceinline__ T cdot(int v, T a, T b) {
 // multiply-add. A compiler that fuses a product into a following addition
 // (as one did for the packed two-site form) then has nothing to fuse, so the
 // one-site and two-site forms round identically.
-template <bool CM, bool FORCED, class T>
-__device__ __forceinline__ void collide_dev32(const T g[9], T dr, T rho, T mx, T my, T ux, T uy, T px, T py, T inv,
-                                              float Gx, float Gy, float omega, T gs[9]) {
+// RAW (BGK with FP16 storage): r holds the stored values (g_v = r_v s_v with
+// the direction's power-of-two scale s_v), and gs receives the stored values
+// of the result, g*_v / s_v. Multiplying by a power of two commutes with
+// round-to-nearest (no result comes near the FP32 subnormal range), so
+// w / s_v (w (...) - g_v) rounds to the same value divided by s_v, and the
+// relaxation with r_v in place of g_v gives g*_v / s_v with no multiply per
+// direction on the way out.
+template <bool CM, bool FORCED, bool RAW = false, class T>
+__device__ __forceinline__ void collide_dev32(const T g[9], const T r[9], T dr, T rho, T mx, T my, T ux, T uy, T px,
+                                              T py, T inv, float Gx, float Gy, float omega, T gs[9]) {
     if (!CM) {
-        const T usq15 = 1.5f * fmaf(ux, ux, uy * uy);
+        // Signs sit in constants, not in negations of values (free for one
+        // float, but two integer operations for a packed pair); each rewrite
+        // below is exact (negation commutes with round-to-nearest), so every
+        // value is the one of the plain form
+        //   inner = fma(4.5 cu, cu, fma(3, cu, -1.5 u.u)),
+        //   g* = fma(omega, fma(w, fma(rho, inner, dr), -g), g).
+        // A direction's c.u is s c0 with s = +-1 and c0 one of ux, uy,
+        // cs = c.u of (1,1), cd = c.u of (1,-1): (4.5 c.u) c.u = (4.5 c0) c0,
+        // fma(3, c.u, x) = fma(3 s, c0, x), and fma(w, z, -g) = -fma(-w, z, g),
+        // so g* = fma(-omega, fma(-w, z, g), g).
+        const T nusq = (-1.5f) * fmaf(ux, ux, uy * uy);
         const T uF = FORCED ? fmaf(ux, Gx, uy * Gy) : zero_of<T>();
         const float fo = fmaf(-0.5f, omega, 1.0f);
-        const T cs = (px + py) * inv, cd = (px - py) * inv;  // c.u of (1,1) and (1,-1)
+        const T cs = (px + py) * inv, cd = (px - py) * inv;
+        const T c0[4] = {ux, uy, cs, cd};
+        T q4[4], q3[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            q4[k] = 4.5f * c0[k];
+            if (FORCED) q3[k] = 3.0f * c0[k];
+        }
 #pragma unroll
         for (int v = 0; v < 9; v++) {
             const float w = wgt_f(v);
             const int cx = cx_of(v), cy = cy_of(v);
-            const T cu = cy == 0 ? (cx == 0 ? zero_of<T>() : (cx > 0 ? ux : -ux))
-                       : cx == 0 ? (cy > 0 ? uy : -uy)
-                       : cx == cy ? (cx > 0 ? cs : -cs) : (cx > 0 ? cd : -cd);
-            const T inner = fmaf(4.5f * cu, cu, fmaf(3.0f, cu, -usq15));
-            const T a = fmaf(omega, fmaf(w, fmaf(rho, inner, dr), -g[v]), g[v]);
+            const int k = cy == 0 ? 0 : (cx == 0 ? 1 : (cx == cy ? 2 : 3));
+            const float sg = (cx != 0 ? cx : cy) > 0 ? 1.0f : -1.0f;
+            const bool rest = cx == 0 && cy == 0;
+            const T inner = rest ? fmaf(zero_of<T>(), zero_of<T>(), fmaf(3.0f, zero_of<T>(), nusq))
+                                 : fmaf(q4[k], c0[k], fmaf(3.0f * sg, c0[k], nusq));
+            const float sv = RAW ? h16_inv(v) : 1.0f;
+            const T gv = RAW ? r[v] : g[v];
+            const T a = fmaf(-omega, fmaf(-(w * sv), fmaf(rho, inner, dr), gv), gv);
             if (FORCED) {
+                // fma(3 c.u, cF, cF - u.F) = fma(3 c0, s cF, cF - u.F)
                 const float cF = cdot(v, Gx, Gy);
-                const T Fv = (3.0f * w) * fmaf(3.0f * cu, cF, cF - uF);
+                const T t = rest ? fmaf(zero_of<T>(), cF, cF - uF) : fmaf(q3[k], sg * cF, cF - uF);
+                const T Fv = ((3.0f * w) * sv) * t;
                 gs[v] = fmaf(fo, Fv, a);
             } else {
                 gs[v] = a;
@@ -233,7 +268,7 @@ __device__ __forceinline__ void collide_dev32(const T g[9], T dr, T rho, T mx, T
 }
 
 template <bool CM, bool FORCED, class S, bool SITE = false>
-__device__ __forceinline__ void finish_site_lowp(const float g[9], typename S::T* __restrict__ B, const LatDev& L,
+__device__ __forceinline__ void finish_site_lowp(const float r[9], typename S::T* __restrict__ B, const LatDev& L,
                                                  int t, int i, int j);
 
 // One interior site, reduced-precision storage. Sites on a boundary-condition
@@ -243,31 +278,35 @@ __device__ __forceinline__ void interior_site_lowp_f(const typename S::T* __rest
                                                      const LatDev& L, int t, int i, int j) {
     if (site_type(L, i, j) != LIFE_FLUID) return;
     const bool edge = (i == 0) | (i == L.Nx - 1) | (j == 0) | (j == L.Ny - 1);
-    float g[9];
+    float r[9];
     const size_t base = (size_t)j * L.pitch + i;
     if (!edge) {
 #pragma unroll
         for (int v = 0; v < 9; v++)
-            g[v] = S::dev(A[(size_t)v * L.S + base - cx_of(v) - (long long)cy_of(v) * L.pitch], v);
+            r[v] = S::raw(A[(size_t)v * L.S + base - cx_of(v) - (long long)cy_of(v) * L.pitch]);
     } else {
 #pragma unroll
         for (int v = 0; v < 9; v++) {
             int si = i - cx_of(v), sj = j - cy_of(v);
             si = si < 0 ? si + L.Nx : (si >= L.Nx ? si - L.Nx : si);
             sj = sj < 0 ? sj + L.Ny : (sj >= L.Ny ? sj - L.Ny : sj);
-            g[v] = S::dev(A[(size_t)v * L.S + (size_t)sj * L.pitch + si], v);
+            r[v] = S::raw(A[(size_t)v * L.S + (size_t)sj * L.pitch + si]);
         }
     }
-    finish_site_lowp<CM, FORCED, S, SITE>(g, B, L, t, i, j);
+    finish_site_lowp<CM, FORCED, S, SITE>(r, B, L, t, i, j);
 }
 
-// The rest of an interior site once its nine pulled deviations g are in
-// registers: moments, outlet columns, collision, store. SITE: the case has a
-// per-site force (WOMERSLEY with gravity; a separate instantiation, used only
-// by the kernels that take such cases).
+// The rest of an interior site once its nine pulled stored values r (as
+// floats) are in registers: deviations, moments, outlet columns, collision,
+// store. SITE: the case has a per-site force (WOMERSLEY with gravity; a
+// separate instantiation, used only by the kernels that take such cases).
 template <bool CM, bool FORCED, class S, bool SITE>
-__device__ __forceinline__ void finish_site_lowp(const float g[9], typename S::T* __restrict__ B, const LatDev& L,
+__device__ __forceinline__ void finish_site_lowp(const float r[9], typename S::T* __restrict__ B, const LatDev& L,
                                                  int t, int i, int j) {
+    constexpr bool RAW = S::SCALED && !CM;
+    float g[9];
+#pragma unroll
+    for (int v = 0; v < 9; v++) g[v] = S::scaled(r[v], v);
     const size_t base = (size_t)j * L.pitch + i;
     float Fxd = 0.0f, Fyd = 0.0f, Gxd = 0.0f, Gyd = 0.0f;
     if (FORCED) {
@@ -295,9 +334,9 @@ __device__ __forceinline__ void finish_site_lowp(const float g[9], typename S::T
         L.outlet_u[((size_t)c * L.Ny + j) * 2 + 1] = uy;
     }
     float gs[9];
-    collide_dev32<CM, FORCED>(g, dr, rho, mx, my, ux, uy, px, py, inv, Gxd, Gyd, L.omega_f, gs);
+    collide_dev32<CM, FORCED, RAW>(g, r, dr, rho, mx, my, ux, uy, px, py, inv, Gxd, Gyd, L.omega_f, gs);
 #pragma unroll
-    for (int v = 0; v < 9; v++) B[(size_t)v * L.S + base] = S::put(gs[v], v);
+    for (int v = 0; v < 9; v++) B[(size_t)v * L.S + base] = RAW ? S::put_raw(gs[v]) : S::put(gs[v], v);
 }
 
 // Whether step forces exist at all for this case (a value every thread of a
@@ -496,43 +535,41 @@ __device__ __forceinline__ void tma_tile_sites(const unsigned char* stage, typen
     for (int jj = (int)threadIdx.x / TT::W; jj < TT::H; jj += (int)blockDim.x / TT::W) {
         const int j = j0 + jj;
         if (j > L.Ny - 2) break;
-        float g[9];
+        float r[9];
 #pragma unroll
         for (int v = 0; v < 9; v++) {
             const typename S::T* plane = reinterpret_cast<const typename S::T*>(stage + v * SH::PLANE);
-            g[v] = S::dev(plane[(jj + 1 - cy_of(v)) * SH::Wb + (ii + TT::HALO - cx_of(v))], v);
+            r[v] = S::raw(plane[(jj + 1 - cy_of(v)) * SH::Wb + (ii + TT::HALO - cx_of(v))]);
         }
-        finish_site_lowp<CM, FORCED, S>(g, B, L, t, i, j);
+        finish_site_lowp<CM, FORCED, S>(r, B, L, t, i, j);
     }
 }
 
-// Two adjacent stored values as FP32 deviations, and back, exactly as
-// S::dev / S::put treat each one (the FP16 values are converted one at a time).
+// Two adjacent stored values as floats (S::raw of each), and back (S::put_raw).
 template <class S>
 struct PairIO;
 template <>
 struct PairIO<StoreF16> {
-    __device__ static __forceinline__ V2 load2(const __half* p, int v) {  // p 4-byte aligned
+    __device__ static __forceinline__ V2 load2(const __half* p) {  // p 4-byte aligned
         const __half2 h = *reinterpret_cast<const __half2*>(p);
-        return v2(__half2float(__low2half(h)), __half2float(__high2half(h))) * h16_scale(v);
+        return v2(__half2float(__low2half(h)), __half2float(__high2half(h)));
     }
-    __device__ static __forceinline__ V2 load11(const __half* p, int v) {
-        return v2(__half2float(p[0]), __half2float(p[1])) * h16_scale(v);
+    __device__ static __forceinline__ V2 load11(const __half* p) {
+        return v2(__half2float(p[0]), __half2float(p[1]));
     }
-    __device__ static __forceinline__ void store2(__half* p, V2 g, int v) {  // p 4-byte aligned
-        const V2 o = g * h16_inv(v);
+    __device__ static __forceinline__ void store2(__half* p, V2 o) {  // p 4-byte aligned
         *reinterpret_cast<__half2*>(p) = __halves2half2(__float2half_rn(o.x()), __float2half_rn(o.y()));
     }
 };
 template <>
 struct PairIO<StoreF32> {
-    __device__ static __forceinline__ V2 load2(const float* p, int) {  // p 8-byte aligned
+    __device__ static __forceinline__ V2 load2(const float* p) {  // p 8-byte aligned
         const float2 f = *reinterpret_cast<const float2*>(p);
         return v2(f.x, f.y);
     }
-    __device__ static __forceinline__ V2 load11(const float* p, int) { return v2(p[0], p[1]); }
-    __device__ static __forceinline__ void store2(float* p, V2 g, int) {  // p 8-byte aligned
-        *reinterpret_cast<float2*>(p) = make_float2(g.x(), g.y());
+    __device__ static __forceinline__ V2 load11(const float* p) { return v2(p[0], p[1]); }
+    __device__ static __forceinline__ void store2(float* p, V2 o) {  // p 8-byte aligned
+        *reinterpret_cast<float2*>(p) = make_float2(o.x(), o.y());
     }
 };
 
@@ -559,23 +596,24 @@ __device__ __forceinline__ void tma_pair(const unsigned char* stage, typename S:
         for (int q = 0; q < 2; q++) {
             const int iq = i + q;
             if (iq < 1 || iq > L.Nx - 2) continue;
-            float g[9];
+            float r[9];
 #pragma unroll
             for (int v = 0; v < 9; v++) {
                 const T* plane = reinterpret_cast<const T*>(stage + v * SH::PLANE);
-                g[v] = S::dev(plane[(jj + 1 - cy_of(v)) * SH::Wb + (ii + q + TT::HALO - cx_of(v))], v);
+                r[v] = S::raw(plane[(jj + 1 - cy_of(v)) * SH::Wb + (ii + q + TT::HALO - cx_of(v))]);
             }
-            finish_site_lowp<false, FORCED, S>(g, B, L, t, iq, j);
+            finish_site_lowp<false, FORCED, S>(r, B, L, t, iq, j);
         }
         return;
     }
-    V2 g[9];
+    V2 r[9], g[9];
 #pragma unroll
     for (int v = 0; v < 9; v++) {
         const T* plane = reinterpret_cast<const T*>(stage + v * SH::PLANE);
         const int at = (jj + 1 - cy_of(v)) * SH::Wb + (ii + TT::HALO - cx_of(v));
         // (ii + HALO) is even: the pair of a direction with no x component is aligned
-        g[v] = cx_of(v) == 0 ? PairIO<S>::load2(plane + at, v) : PairIO<S>::load11(plane + at, v);
+        r[v] = cx_of(v) == 0 ? PairIO<S>::load2(plane + at) : PairIO<S>::load11(plane + at);
+        g[v] = S::SCALED ? r[v] * h16_scale(v) : r[v];
     }
     float Fxd = 0.0f, Fyd = 0.0f, Gxd = 0.0f, Gyd = 0.0f;
     if (FORCED) {
@@ -590,10 +628,10 @@ __device__ __forceinline__ void tma_pair(const unsigned char* stage, typename S:
     const V2 px = FORCED ? fmaf(0.5f, Fxd, mx) : mx, py = FORCED ? fmaf(0.5f, Fyd, my) : my;
     const V2 ux = px * inv, uy = py * inv;
     V2 gs[9];
-    collide_dev32<false, FORCED>(g, dr, rho, mx, my, ux, uy, px, py, inv, Gxd, Gyd, L.omega_f, gs);
+    collide_dev32<false, FORCED, S::SCALED>(g, r, dr, rho, mx, my, ux, uy, px, py, inv, Gxd, Gyd, L.omega_f, gs);
     T* out = B + (size_t)j * L.pitch + i;
 #pragma unroll
-    for (int v = 0; v < 9; v++) PairIO<S>::store2(out + (size_t)v * L.S, gs[v], v);
+    for (int v = 0; v < 9; v++) PairIO<S>::store2(out + (size_t)v * L.S, gs[v]);
 }
 
 // The last CTA of a launch to finish clears the tile counters for the next
