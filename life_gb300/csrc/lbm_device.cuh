@@ -152,6 +152,22 @@ __device__ __forceinline__ double add_c(double acc, int c, double x) {
     return c == 0 ? acc : (c > 0 ? acc + x : acc - x);
 }
 
+// 1/rho of the reduced-precision forms: the hardware approximation
+// (rcp.approx.ftz.f32) refined by one Newton-Raphson step, y + y (1 - rho y)
+// in two fused multiply-adds (the textbook iteration for a reciprocal). For
+// the densities of a flow (rho near 1) the result is within one unit in the
+// last place of 1/rho, and every kernel that forms a site's velocity in
+// FP32 uses this function, so they agree bit for bit.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_lowp(float rho) {
+    const float y = rcp_approx(rho);
+    return fmaf(y, fmaf(-rho, y, 1.0f), y);
+}
+
 // -0 -> +0 on the bits (integer operations, not the FP64 unit)
 __device__ __forceinline__ double pos_zero(double s) {
     const long long b = __double_as_longlong(s);

@@ -219,7 +219,7 @@ __global__ void k_state(typename S::T* __restrict__ B, LatDev L, int t, const do
 
 // In the reduced-precision forms a fluid site without an IBM force gets its
 // velocity exactly as the step kernels form it, in FP32 (finish_site_lowp:
-// deviations, 1/rho correctly rounded, momentum with the half force), and
+// deviations, 1/rho by rcp_lowp, momentum with the half force), and
 // its density as 1 + the FP32 deviation sum in FP64; the FP64 path
 // (site_state) would spend ~50 FP64 operations per site on the narrow FP64
 // pipe. Boundary and IBM-corrected sites, populations requested, and the
@@ -249,7 +249,7 @@ __device__ __forceinline__ bool export_fluid_lowp(const typename S::T* __restric
         const float rf = 1.0f + dr;
         const float mx = (g[1] - g[2]) + (g[5] - g[6]) + (g[7] - g[8]);
         const float my = (g[3] - g[4]) + (g[5] - g[6]) + (g[8] - g[7]);
-        const float inv = __frcp_rn(rf);
+        const float inv = rcp_lowp(rf);
         const bool forced = L.womersley || L.Fx0_f != 0.0f || L.Fy0_f != 0.0f;
         const float px = forced ? fmaf(0.5f, Fxd, mx) : mx, py = forced ? fmaf(0.5f, Fyd, my) : my;
         rho = 1.0 + (double)dr;
