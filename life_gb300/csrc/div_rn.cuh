@@ -3,7 +3,20 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 namespace life {
+
+// the bits of a double (device intrinsic, or a copy on the host)
+__host__ __device__ __forceinline__ unsigned long long div_bits(double x) {
+#ifdef __CUDA_ARCH__
+    return (unsigned long long)__double_as_longlong(x);
+#else
+    unsigned long long u;
+    std::memcpy(&u, &x, sizeof u);
+    return u;
+#endif
+}
 
 // a / b correctly rounded (round to nearest), given y = RN(1/b): Markstein's
 // method (P. Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al.,
@@ -13,10 +26,12 @@ namespace life {
 // RN(q1 + (a - b q1) y) = RN(a/b). The theorem needs the intermediates in the
 // normal range, so operands outside a safe exponent window (tested on the
 // bits, with integer operations) take the hardware division.
-// life_selftest_division checks this function against a / b.
-__device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
-    const unsigned long long ba = (unsigned long long)__double_as_longlong(a);
-    const unsigned long long bb = (unsigned long long)__double_as_longlong(b);
+// life_selftest_division checks this function against a / b on the device,
+// and the host build of the same function is checked against IEEE division
+// by the CPU tests.
+__host__ __device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
+    const unsigned long long ba = div_bits(a);
+    const unsigned long long bb = div_bits(b);
     const int ea = (int)(ba >> 52) & 0x7ff, eb = (int)(bb >> 52) & 0x7ff;
     // a zero numerator runs the same steps (every intermediate is a zero) and
     // then takes q0 = a * y, the signed zero a / b (y has the sign of b): the
