@@ -9,7 +9,8 @@
 //                   populations per site)
 //   k_perimeter     the same for boundary-condition sites, with the
 //                   regularised / convective conditions applied
-//   k_outlet_f64    convective outlet speed (sequential mean, as the reference)
+//   k_outlet_f64    convective outlet speed (sequential mean, as the reference;
+//                   a fixed-order tree sum for the reduced-precision forms)
 //   k_state         collision from an explicit state (restart read)
 //   k_export        reference-layout fields of the current step
 //   k_maxvel        max |u| and NaN scan
@@ -177,20 +178,38 @@ __global__ void k_outlet_f64(LatDev L, double* __restrict__ delU) {
     const double* u1 = L.outlet_u + (size_t)2 * Ny * 2;  // column Nx-1
     const double* u2 = L.outlet_u + (size_t)1 * Ny * 2;  // column Nx-2
     const double* u3 = L.outlet_u;                       // column Nx-3
-    // All threads stage the outlet column through shared memory; one thread
-    // then adds it up in j order.
-    double acc = 0.0;
-    for (int j0 = 0; j0 < Ny; j0 += 1024) {
-        const int m = Ny - j0 < 1024 ? Ny - j0 : 1024;
+    if (L.prec != LIFE_PREC_F64) {
+        // Reduced-precision forms (whose state is not the reference's bits):
+        // a tree sum in a fixed order (strided per thread, then the warps,
+        // then the warp sums in order), the same on every run; a chain of
+        // ~15 dependent FP64 additions instead of Ny.
+        __shared__ double wsum[32];
+        double part = 0.0;
+        for (int j = threadIdx.x; j < Ny; j += blockDim.x) part += u1[j * 2];
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+        if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = part;
         __syncthreads();
-        for (int j = threadIdx.x; j < m; j += blockDim.x) col[j] = u1[(j0 + j) * 2];
-        __syncthreads();
-        if (threadIdx.x == 0)
-            for (int j = 0; j < m; j++) acc += col[j];
-    }
-    if (threadIdx.x == 0) {
-        acc /= (double)Ny;
-        uOut_s = acc;
+        if (threadIdx.x == 0) {
+            double a = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) a += wsum[w];
+            uOut_s = a / (double)Ny;
+        }
+    } else {
+        // All threads stage the outlet column through shared memory; one
+        // thread then adds it up in j order, as the reference does.
+        double acc = 0.0;
+        for (int j0 = 0; j0 < Ny; j0 += 1024) {
+            const int m = Ny - j0 < 1024 ? Ny - j0 : 1024;
+            __syncthreads();
+            for (int j = threadIdx.x; j < m; j += blockDim.x) col[j] = u1[(j0 + j) * 2];
+            __syncthreads();
+            if (threadIdx.x == 0)
+                for (int j = 0; j < m; j++) acc += col[j];
+        }
+        if (threadIdx.x == 0) {
+            acc /= (double)Ny;
+            uOut_s = acc;
+        }
     }
     __syncthreads();
     const double uOut = uOut_s;
