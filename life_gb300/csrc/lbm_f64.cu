@@ -493,9 +493,11 @@ int batch_blocks_per_sm_f64(int tile_w) {
 
 cudaError_t launch_perimeter(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
     if (L.prec != LIFE_PREC_F64) return launch_perimeter_lowp(A, B, L, t, s);
+    // one warp per block, spread over the SMs' FP64 units (as the
+    // reduced-precision perimeter)
     const int n = 2 * L.Nx + 2 * (L.Ny - 2);
-    if (L.cm) k_perimeter<true, StoreF64><<<(n + 127) / 128, 128, 0, s>>>((const double*)A, (double*)B, L, t);
-    else k_perimeter<false, StoreF64><<<(n + 127) / 128, 128, 0, s>>>((const double*)A, (double*)B, L, t);
+    if (L.cm) k_perimeter<true, StoreF64><<<(n + 31) / 32, 32, 0, s>>>((const double*)A, (double*)B, L, t);
+    else k_perimeter<false, StoreF64><<<(n + 31) / 32, 32, 0, s>>>((const double*)A, (double*)B, L, t);
     return cudaGetLastError();
 }
 

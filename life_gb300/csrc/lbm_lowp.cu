@@ -408,15 +408,18 @@ __global__ void k_perimeter_lowp(const typename S::T* __restrict__ A, typename S
     perimeter_site<CM, S>(A, B, L, step_t(L, t), blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// One warp per block: a boundary site is a long FP64 chain, and an SM's FP64
+// unit is narrow, so the sites are spread over as many SMs as possible
+// rather than packed four warps to an SM.
 cudaError_t launch_perimeter_lowp(const void* A, void* B, const LatDev& L, int t, cudaStream_t s) {
     const int n = 2 * L.Nx + 2 * (L.Ny - 2);
-    const int g = (n + 127) / 128;
+    const int g = (n + 31) / 32;
     if (L.prec == LIFE_PREC_F32) {
-        if (L.cm) k_perimeter_lowp<true, StoreF32><<<g, 128, 0, s>>>((const float*)A, (float*)B, L, t);
-        else k_perimeter_lowp<false, StoreF32><<<g, 128, 0, s>>>((const float*)A, (float*)B, L, t);
+        if (L.cm) k_perimeter_lowp<true, StoreF32><<<g, 32, 0, s>>>((const float*)A, (float*)B, L, t);
+        else k_perimeter_lowp<false, StoreF32><<<g, 32, 0, s>>>((const float*)A, (float*)B, L, t);
     } else {
-        if (L.cm) k_perimeter_lowp<true, StoreF16><<<g, 128, 0, s>>>((const __half*)A, (__half*)B, L, t);
-        else k_perimeter_lowp<false, StoreF16><<<g, 128, 0, s>>>((const __half*)A, (__half*)B, L, t);
+        if (L.cm) k_perimeter_lowp<true, StoreF16><<<g, 32, 0, s>>>((const __half*)A, (__half*)B, L, t);
+        else k_perimeter_lowp<false, StoreF16><<<g, 32, 0, s>>>((const __half*)A, (__half*)B, L, t);
     }
     return cudaGetLastError();
 }
