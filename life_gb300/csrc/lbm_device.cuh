@@ -148,7 +148,7 @@ __device__ __forceinline__ void gather(const typename S::T* __restrict__ P, cons
 // does not form them. A component of +-1 multiplies exactly. The remaining
 // terms keep the reference's order. (After unrolling, the component tests are
 // compile-time constants.)
-__device__ __forceinline__ double add_c(double acc, int c, double x) {
+__host__ __device__ __forceinline__ double add_c(double acc, int c, double x) {
     return c == 0 ? acc : (c > 0 ? acc + x : acc - x);
 }
 
@@ -168,10 +168,9 @@ __device__ __forceinline__ float rcp_lowp(float rho) {
     return fmaf(y, fmaf(-rho, y, 1.0f), y);
 }
 
-// -0 -> +0 on the bits (integer operations, not the FP64 unit)
-__device__ __forceinline__ double pos_zero(double s) {
-    const long long b = __double_as_longlong(s);
-    return __longlong_as_double(b == (long long)0x8000000000000000ull ? 0ll : b);
+// -0 -> +0, tested on the bits (integer operations, not the FP64 unit)
+__host__ __device__ __forceinline__ double pos_zero(double s) {
+    return div_bits(s) == 0x8000000000000000ull ? 0.0 : s;
 }
 
 // The reference's density and momentum sums (src/Grid.cpp:285-293) start at
@@ -180,8 +179,9 @@ __device__ __forceinline__ double pos_zero(double s) {
 // a round-to-nearest sum is -0 only when both of its terms are, so the
 // reference's sums are never -0, and where this sum holds -0 the
 // reference's holds +0, while any nonzero term makes them equal again.
-// pos_zero() on the result gives the reference's bits.
-__device__ __forceinline__ void moment_sums(const double f[9], double& r, double& mx, double& my) {
+// pos_zero() on the result gives the reference's bits. (Also built for the
+// host, where the CPU tests compare it with the reference's literal sums.)
+__host__ __device__ __forceinline__ void moment_sums(const double f[9], double& r, double& mx, double& my) {
     r = f[0];
     mx = 0.0;
     my = 0.0;
