@@ -1,8 +1,8 @@
 """Argument checks of the C-ABI that run before any device work, so they are
 exercised here without a GPU: every rejected call returns LIFE_ERR_INVALID,
 leaves the output handle NULL and sets a message naming the problem. The
-convective-wall message is the reference's own (GridClass::GridClass,
-src/Grid.cpp:1295-1299: only the right boundary may be convective)."""
+convective-wall message is the reference's own (GridClass::initialiseGrid,
+src/Grid.cpp:918-920: only the right boundary may be convective)."""
 import ctypes as C
 import dataclasses
 
